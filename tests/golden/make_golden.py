@@ -1,0 +1,278 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run here, where the reference checkout exists (FDTD_REFERENCE_ROOT, default
+/root/reference), after ``python oracle/build_ref.py``:
+
+    python tests/golden/make_golden.py
+
+Fixtures (seeded random inputs, reference outputs, all in the C-order
+(nx, ny, nz) layout of this package, with comparison masks):
+
+  yee_numpy.npz     2nd_order-Yee/Numpy/fdtd3d.py update_e/update_h/pbc,
+                    several steps, odd sizes (bit-exact target)
+  kemp_core.npz     KEMP/v0.7_pml/fdtd3d/cpu/src/core.c (coeff_use '' and
+                    'eh', pad 0..3), one update each, inputs as in
+                    KEMP/v0.7_pml/fdtd3d/util/common_random.py:8-39
+  cpml_kufdtd.npz   kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c
+                    update_{x,y,z}_{e,h}, front and back, remapped to this
+                    package's slab layout (kappa = 1), masks cover the cells
+                    both conventions update
+  symp_c.npz        4th_order-Symplectic/Python-C/dielectric.c update_h /
+                    update_e on Fortran-order arrays, compared on
+                    [:-1, :-1, :-1] where the C loop bounds and the CUDA
+                    index ranges agree
+"""
+import ctypes as C
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REF = os.environ.get("FDTD_REFERENCE_ROOT", "/root/reference")
+
+from oracle import build_ref  # noqa: E402
+
+F32 = np.float32
+
+
+def _load_module(name, path):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def yee_numpy(rng):
+    fd = _load_module("ref_fdtd3d", os.path.join(REF, "2nd_order-Yee/Numpy/fdtd3d.py"))
+    out = {}
+    cases = [((9, 8, 12), 4, 0), ((7, 10, 13), 3, 0), ((5, 6, 7), 5, 0), ((8, 9, 10), 3, 7)]
+    for n, (shape, nsteps, pbc_axes) in enumerate(cases):
+        names = ["ex", "ey", "ez", "hx", "hy", "hz"]
+        f = {k: rng.standard_normal(shape).astype(F32) for k in names}
+        ce = [rng.random(shape, dtype=F32) * F32(0.5) for _ in range(3)]
+        src = (shape[0] // 2, shape[1] // 2, shape[2] // 2)
+        amps = rng.standard_normal(nsteps).astype(F32)
+        for k in names:
+            out["c%d_in_%s" % (n, k)] = f[k].copy()
+        for q, k in enumerate(("cex", "cey", "cez")):
+            out["c%d_in_%s" % (n, k)] = ce[q]
+        out["c%d_amps" % n] = amps
+        out["c%d_src" % n] = np.array(src)
+        out["c%d_meta" % n] = np.array([nsteps, pbc_axes])
+        dirs = "".join(a for b, a in ((1, "x"), (2, "y"), (4, "z")) if pbc_axes & b)
+        for t in range(nsteps):
+            fd.update_e(f["ex"], f["ey"], f["ez"], f["hx"], f["hy"], f["hz"], *ce)
+            if dirs:
+                fd.update_pbc_e(dirs, f["ex"], f["ey"], f["ez"])
+            f["ez"][src] += amps[t]
+            fd.update_h(f["ex"], f["ey"], f["ez"], f["hx"], f["hy"], f["hz"])
+            if dirs:
+                fd.update_pbc_h(dirs, f["hx"], f["hy"], f["hz"])
+        for k in names:
+            out["c%d_out_%s" % (n, k)] = f[k]
+    out["ncases"] = np.array(len(cases))
+    return out
+
+
+def kemp_core(rng):
+    out = {}
+    n = 0
+    nx, ny = 6, 7
+    for coeff_use in ("", "eh"):
+        for nz in (13, 14, 15, 16):
+            pad = (-nz) % 4
+            lib = np.ctypeslib.load_library(os.path.basename(build_ref.kemp_lib_path(coeff_use, pad)),
+                                            os.path.dirname(build_ref.kemp_lib_path(coeff_use, pad)))
+            for ufunc in ("e", "h"):
+                shape = (nx, ny, nz)
+                pitch = (nx, ny, nz + pad)
+                if ufunc == "e":
+                    ehs = [np.zeros(shape, F32) for _ in range(3)] + [rng.random(shape, dtype=F32) for _ in range(3)]
+                else:
+                    ehs = [rng.random(shape, dtype=F32) for _ in range(3)] + [np.zeros(shape, F32) for _ in range(3)]
+                if coeff_use:
+                    ces = [rng.random(shape, dtype=F32) for _ in range(3)]
+                    chs = [rng.random(shape, dtype=F32) for _ in range(3)]
+                else:
+                    ces = [np.full(shape, 0.5, F32) for _ in range(3)]
+                    chs = [np.full(shape, 0.5, F32) for _ in range(3)]
+                pe = [np.zeros(pitch, F32) for _ in range(6)]
+                for a, b in zip(pe, ehs):
+                    a[:, :, :nz] = b
+                pce = [np.zeros(pitch, F32) for _ in range(3)]
+                pch = [np.zeros(pitch, F32) for _ in range(3)]
+                for a, b in zip(pce, ces):
+                    a[:, :, :nz] = b
+                for a, b in zip(pch, chs):
+                    a[:, :, :nz] = b
+                args = [C.c_int(nx), C.c_int(ny), C.c_int(nz + pad)] + [C.c_void_p(a.ctypes.data) for a in pe]
+                if ufunc == "e":
+                    if coeff_use:
+                        args += [C.c_void_p(a.ctypes.data) for a in pce]
+                    lib.update_e(*args)
+                else:
+                    if coeff_use:
+                        args += [C.c_void_p(a.ctypes.data) for a in pch]
+                    lib.update_h(*args)
+                tag = "c%d_" % n
+                out[tag + "meta"] = np.array([nz, pad, 1 if coeff_use else 0, 0 if ufunc == "e" else 1])
+                for q, k in enumerate(["ex", "ey", "ez", "hx", "hy", "hz"]):
+                    out[tag + "in_" + k] = ehs[q]
+                    out[tag + "out_" + k] = pe[q][:, :, :nz].copy()
+                for q, k in enumerate(["cex", "cey", "cez"]):
+                    out[tag + "in_" + k] = ces[q]
+                for q, k in enumerate(["chx", "chy", "chz"]):
+                    out[tag + "in_" + k] = chs[q]
+                n += 1
+    out["ncases"] = np.array(n)
+    return out
+
+
+def cpml_kufdtd(rng):
+    """Run the reference's non-kappa CPML routines and remap to the slab layout."""
+    sys.path.insert(0, build_ref.OUT)
+    import ref_cpml_non_kappa as ref
+    out = {}
+    n = 0
+    Nx, Ny, Nz, P = 9, 8, 12, 3     # Npml+1 multiple of 4 for the z routines
+    shape = (Nx, Ny, Nz)
+    for axis in range(3):
+        for which in ("e", "h"):
+            for backward in (0, 1):
+                E = [rng.standard_normal(shape).astype(F32) for _ in range(3)]
+                H = [rng.standard_normal(shape).astype(F32) for _ in range(3)]
+                CE = [rng.random(shape, dtype=F32) for _ in range(3)]
+                rb = rng.random(2 * (P + 1), dtype=F32)
+                ra = (rng.random(2 * (P + 1), dtype=F32) - F32(0.5))
+                if axis == 0:
+                    kshape = (P, Ny - 1, Nz)
+                elif axis == 1:
+                    kshape = (Nx - 1, P, Nz)
+                else:
+                    kshape = (Nx - 1, Ny - 1, P + 1)
+                kpsi = [rng.standard_normal(kshape).astype(F32) for _ in range(2)]
+                if axis == 2:       # the kpml=0 / k=Nz-1 planes are outside this package's slabs
+                    for p in kpsi:
+                        p[:, :, 0 if backward == 0 else P] = 0
+                ex, ey, ez = [a.copy() for a in E]
+                hx, hy, hz = [a.copy() for a in H]
+                kp = [p.copy() for p in kpsi]
+                fn = getattr(ref, "update_%s_%s" % ("xyz"[axis], which))
+                if which == "e":
+                    flds = {0: (ey, ez, hy, hz, CE[1], CE[2]), 1: (ex, ez, hx, hz, CE[0], CE[2]),
+                            2: (ex, ey, hx, hy, CE[0], CE[1])}[axis]
+                else:
+                    flds = {0: (ey, ez, hy, hz), 1: (ex, ez, hx, hz), 2: (ex, ey, hx, hy)}[axis]
+                fn(1, Nx, Ny, Nz, P, backward, *flds, kp[0], kp[1], rb, ra)
+                # remap: tables and psi into the slab layout (2P entries)
+                if which == "e":
+                    tb, ta = rb[1:2 * P + 1], ra[1:2 * P + 1]
+                else:
+                    tb = np.concatenate([rb[1:P + 1], rb[P + 2:2 * P + 2]])
+                    ta = np.concatenate([ra[1:P + 1], ra[P + 2:2 * P + 2]])
+                n_ax = shape[axis]
+                sl = np.arange(P) if backward == 0 else np.arange(P, 2 * P)
+                if which == "e":
+                    nodes = [s + 1 if s < P else n_ax - P - 1 + (s - P) for s in sl]
+                else:
+                    nodes = [s + 1 if s < P else n_ax - P + (s - P) for s in sl]
+                mshape = [(2 * P, Ny, Nz), (Nx, 2 * P, Nz), (Nx, Ny, 2 * P)][axis]
+                psi_in = [np.zeros(mshape, F32) for _ in range(2)]
+                psi_out = [np.zeros(mshape, F32) for _ in range(2)]
+                pmask = np.zeros(mshape, bool)
+                for q, (s, node) in enumerate(zip(sl, nodes)):
+                    ip = q  # reference slab plane index (ipml/jpml) or kpml
+                    for r in range(2):
+                        if axis == 0:
+                            psi_in[r][s, 1:, :] = kpsi[r][ip]
+                            psi_out[r][s, 1:, :] = kp[r][ip]
+                        elif axis == 1:
+                            flat_in = kpsi[r].reshape(-1).reshape(P, Nx - 1, Nz)
+                            flat_out = kp[r].reshape(-1).reshape(P, Nx - 1, Nz)
+                            psi_in[r][1:, s, :] = flat_in[ip]
+                            psi_out[r][1:, s, :] = flat_out[ip]
+                        else:
+                            kp_idx = node - (0 if backward == 0 else Nz - P - 1)
+                            psi_in[r][1:, 1:, s] = kpsi[r][:, :, kp_idx]
+                            psi_out[r][1:, 1:, s] = kp[r][:, :, kp_idx]
+                # comparison region: transverse interior, both conventions update it
+                fmask = np.zeros(shape, bool)
+                for s, node in zip(sl, nodes):
+                    if axis == 0:
+                        fmask[node, 1:Ny - 1, 1:Nz - 1] = True
+                        pmask[s, 1:Ny - 1, 1:Nz - 1] = True
+                    elif axis == 1:
+                        fmask[1:Nx - 1, node, 1:Nz - 1] = True
+                        pmask[1:Nx - 1, s, 1:Nz - 1] = True
+                    else:
+                        fmask[1:Nx - 1, 1:Ny - 1, node] = True
+                        pmask[1:Nx - 1, 1:Ny - 1, s] = True
+                tag = "c%d_" % n
+                out[tag + "meta"] = np.array([axis, 0 if which == "e" else 1, backward, P])
+                for q, k in enumerate(("ex", "ey", "ez")):
+                    out[tag + "in_" + k] = E[q]
+                    out[tag + "out_" + k] = [ex, ey, ez][q]
+                for q, k in enumerate(("hx", "hy", "hz")):
+                    out[tag + "in_" + k] = H[q]
+                    out[tag + "out_" + k] = [hx, hy, hz][q]
+                for q, k in enumerate(("cex", "cey", "cez")):
+                    out[tag + "in_" + k] = CE[q]
+                out[tag + "tb"] = tb
+                out[tag + "ta"] = ta
+                out[tag + "psi_in0"], out[tag + "psi_in1"] = psi_in
+                out[tag + "psi_out0"], out[tag + "psi_out1"] = psi_out
+                out[tag + "fmask"] = fmask
+                out[tag + "pmask"] = pmask
+                n += 1
+    out["ncases"] = np.array(n)
+    out["shape"] = np.array(shape)
+    return out
+
+
+def symp_c(rng):
+    sys.path.insert(0, build_ref.OUT)
+    import ref_symp_dielectric as ref
+    out = {}
+    n = 0
+    for shape in ((9, 8, 10), (7, 11, 9)):
+        nx, ny, nz = shape
+        for which in ("h", "e"):
+            coef = F32(rng.standard_normal())
+            f = [np.asfortranarray(rng.standard_normal(shape).astype(F32)) for _ in range(6)]
+            c = [np.asfortranarray(rng.random(shape, dtype=F32)) for _ in range(3)]
+            ins = [np.ascontiguousarray(a) for a in f]
+            if which == "h":
+                ref.update_h(nx, ny, nz, float(coef), *f, *c)
+            else:
+                ref.update_e(nx, ny, nz, float(coef), *f, *c)
+            tag = "c%d_" % n
+            out[tag + "meta"] = np.array([0 if which == "h" else 1])
+            out[tag + "coef"] = np.array(coef, F32)
+            for q, k in enumerate(("ex", "ey", "ez", "hx", "hy", "hz")):
+                out[tag + "in_" + k] = ins[q]
+                out[tag + "out_" + k] = np.ascontiguousarray(f[q])
+            for q, k in enumerate(("c0", "c1", "c2")):
+                out[tag + "in_" + k] = np.ascontiguousarray(c[q])
+            n += 1
+    out["ncases"] = np.array(n)
+    return out
+
+
+def main():
+    if not build_ref.build():
+        raise SystemExit("reference checkout or x86_64 host not available")
+    rng = np.random.default_rng(20261203)
+    for name, fn in (("yee_numpy", yee_numpy), ("kemp_core", kemp_core),
+                     ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c)):
+        data = fn(rng)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **data)
+        print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

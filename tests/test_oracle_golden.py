@@ -1,0 +1,147 @@
+"""Pin the CPU oracle against outputs of the reference itself.
+
+The fixtures in tests/golden/ were produced by tests/golden/make_golden.py
+from the reference's NumPy step (2nd_order-Yee/Numpy/fdtd3d.py), the KEMP
+SSE/OpenMP core (KEMP/v0.7_pml/fdtd3d/cpu/src/core.c), the kuFDTD CPML C
+routines (kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c) and the 4th-order C
+extension (4th_order-Symplectic/Python-C/dielectric.c).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+NAMES = ("ex", "ey", "ez", "hx", "hy", "hz")
+
+
+def _load(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name + ".npz"))
+
+
+def test_oracle_matches_numpy_reference_bit_exact(golden_dir):
+    d = _load(golden_dir, "yee_numpy")
+    for n in range(int(d["ncases"])):
+        t = "c%d_" % n
+        f = {k: d[t + "in_" + k].copy() for k in NAMES}
+        ce = [d[t + "in_" + k] for k in ("cex", "cey", "cez")]
+        nsteps, axes = d[t + "meta"]
+        src = tuple(int(v) for v in d[t + "src"])
+        for s in range(int(nsteps)):
+            oracle.update_e(*(f[k] for k in NAMES), *ce)
+            if axes:
+                oracle.pbc_e(int(axes), f["ex"], f["ey"], f["ez"])
+            f["ez"][src] = f["ez"][src] + d[t + "amps"][s]
+            oracle.update_h(*(f[k] for k in NAMES))
+            if axes:
+                oracle.pbc_h(int(axes), f["hx"], f["hy"], f["hz"])
+        for k in NAMES:
+            np.testing.assert_array_equal(f[k], d[t + "out_" + k], err_msg="case %d %s" % (n, k))
+
+
+def test_oracle_matches_kemp_core(golden_dir):
+    """KEMP groups the curl as (a-b)-(c-d), NumPy as ((a-b)-c)+d: the two
+    agree to a few ulp, so this check bounds the difference at 4 ulp of the
+    largest term instead of bit equality."""
+    d = _load(golden_dir, "kemp_core")
+    for n in range(int(d["ncases"])):
+        t = "c%d_" % n
+        nz, pad, coeff, ufunc = (int(v) for v in d[t + "meta"])
+        f = {k: d[t + "in_" + k].copy() for k in NAMES}
+        if ufunc == 0:
+            oracle.update_e(*(f[k] for k in NAMES), *(d[t + "in_" + k] for k in ("cex", "cey", "cez")))
+            comps = NAMES[:3]
+        else:
+            ch = [d[t + "in_" + k] for k in ("chx", "chy", "chz")] if coeff else [None] * 3
+            oracle.update_h(*(f[k] for k in NAMES), *ch)
+            comps = NAMES[3:]
+        for k in comps:
+            ref = d[t + "out_" + k]
+            tol = 4 * np.finfo(np.float32).eps * max(1.0, np.abs(ref).max())
+            assert np.abs(f[k] - ref).max() <= tol, (n, k)
+
+
+def test_oracle_cpml_matches_kufdtd_bit_exact(golden_dir):
+    """With kappa = 1 (km1 = 0) the kappa-CPML restatement reduces exactly to
+    the reference's non-kappa CPML."""
+    d = _load(golden_dir, "cpml_kufdtd")
+    for n in range(int(d["ncases"])):
+        t = "c%d_" % n
+        axis, which, backward, P = (int(v) for v in d[t + "meta"])
+        E = [d[t + "in_" + k].copy() for k in NAMES[:3]]
+        H = [d[t + "in_" + k].copy() for k in NAMES[3:]]
+        CE = [d[t + "in_" + k] for k in ("cex", "cey", "cez")]
+        npml = [0, 0, 0]
+        npml[axis] = P
+        faces = 1 << (2 * axis + backward)
+        zero = np.zeros(2 * P)
+        tables = {}
+        for w in ("e", "h"):
+            for name, val in (("b", d[t + "tb"]), ("a", d[t + "ta"]), ("km1", zero)):
+                tables["%s_%s" % (name, w)] = [val if a == axis else None for a in range(3)]
+        psi = [None] * 6
+        psi[2 * axis] = d[t + "psi_in0"].copy()
+        psi[2 * axis + 1] = d[t + "psi_in1"].copy()
+        if which == 0:
+            oracle.cpml_e(npml, faces, tables, *E, *H, *CE, psi)
+            upd, comps = E, NAMES[:3]
+        else:
+            oracle.cpml_h(npml, faces, tables, *E, *H, psi)
+            upd, comps = H, NAMES[3:]
+        fm = d[t + "fmask"]
+        pm = d[t + "pmask"]
+        assert fm.any() and pm.any()
+        for arr, k in zip(upd, comps):
+            np.testing.assert_array_equal(arr[fm], d[t + "out_" + k][fm], err_msg="case %d %s" % (n, k))
+        for r in range(2):
+            np.testing.assert_array_equal(psi[2 * axis + r][pm], d[t + "psi_out%d" % r][pm],
+                                          err_msg="case %d psi%d" % (n, r))
+
+
+def test_oracle_symplectic_matches_reference_c_bit_exact(golden_dir):
+    d = _load(golden_dir, "symp_c")
+    for n in range(int(d["ncases"])):
+        t = "c%d_" % n
+        which = int(d[t + "meta"][0])
+        f = [d[t + "in_" + k].copy() for k in NAMES]
+        c = [d[t + "in_" + k] for k in ("c0", "c1", "c2")]
+        coef = d[t + "coef"][()]
+        if which == 0:
+            oracle.symp_h(coef, *f, *c)
+            comps = range(3, 6)
+        else:
+            oracle.symp_e(coef, *f, *c)
+            comps = range(0, 3)
+        for q in comps:
+            np.testing.assert_array_equal(f[q][:-1, :-1, :-1], d[t + "out_" + NAMES[q]][:-1, :-1, :-1],
+                                          err_msg="case %d %s" % (n, NAMES[q]))
+
+
+def test_oracle_fp64_matches_fp32_roughly():
+    rng = np.random.default_rng(1)
+    shape = (10, 11, 12)
+    f32 = {k: rng.standard_normal(shape).astype(np.float32) for k in NAMES}
+    f64 = {k: v.astype(np.float64) for k, v in f32.items()}
+    ce = [np.full(shape, 0.5, np.float32) for _ in range(3)]
+    for _ in range(20):
+        oracle.update_e(*(f32[k] for k in NAMES), *ce)
+        oracle.update_h(*(f32[k] for k in NAMES))
+        oracle.update_e(*(f64[k] for k in NAMES), *(c.astype(np.float64) for c in ce))
+        oracle.update_h(*(f64[k] for k in NAMES))
+    for k in NAMES:
+        err = np.abs(f32[k] - f64[k]).max() / np.abs(f64[k]).max()
+        assert err < 1e-5
+
+
+@pytest.mark.parametrize("npml", [4, 12])
+def test_cpml_tables_shape_and_range(npml):
+    t = oracle.cpml_tables(npml)
+    for k in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h"):
+        assert t[k].shape == (2 * npml,)
+    assert np.all((t["b_e"] > 0) & (t["b_e"] <= 1))
+    assert np.all(t["a_e"] <= 0)
+    assert np.all((t["km1_e"] <= 0) & (t["km1_e"] > -1))
+    # front slab is the mirror of the back slab
+    np.testing.assert_allclose(t["b_e"][:npml][::-1], t["b_e"][npml:])
+    np.testing.assert_allclose(t["b_h"][:npml][::-1], t["b_h"][npml:])

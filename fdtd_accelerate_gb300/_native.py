@@ -1,0 +1,129 @@
+"""ctypes binding of libfdtd_gb300.so (the C ABI declared in include/fdtd_gb300.h).
+
+The library is loaded from this package directory.  There is no CPU
+fallback: if the library is missing or CUDA is unavailable, the calls raise.
+"""
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libfdtd_gb300.so")
+
+FDTD_OK = 0
+FDTD_ERR_ARG = 1
+FDTD_ERR_SHAPE = 2
+FDTD_ERR_ALIGN = 3
+FDTD_ERR_CUDA = 4
+FDTD_ERR_TIMEOUT = 5
+FDTD_ERR_UNSUPPORTED = 6
+FDTD_ERR_CAPACITY = 7
+
+P = C.c_void_p
+I32 = C.c_int32
+I64 = C.c_int64
+F32 = C.c_float
+
+
+class Grid(C.Structure):
+    _fields_ = [("nx", I64), ("ny", I64), ("nz", I64), ("sx", I64), ("sy", I64)]
+
+
+class Cpml(C.Structure):
+    _fields_ = [("npml", I32 * 3), ("faces", I32),
+                ("b_e", P * 3), ("a_e", P * 3), ("km1_e", P * 3),
+                ("b_h", P * 3), ("a_h", P * 3), ("km1_h", P * 3)]
+
+
+class Psi(C.Structure):
+    _fields_ = [("e", P * 6), ("h", P * 6)]
+
+
+class Sources(C.Structure):
+    _fields_ = [("nsrc", I32), ("ijk", P), ("comp", P), ("amp", P), ("namp", I64)]
+
+
+class YeeState(C.Structure):
+    _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3)]
+
+
+class Tile(C.Structure):
+    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32)]
+
+
+class FdtdError(RuntimeError):
+    def __init__(self, status, fn, msg):
+        super().__init__("%s failed: %s (status %d)" % (fn, msg, status))
+        self.status = status
+
+
+_SIGS = {
+    "fdtd_status_string": (C.c_char_p, [C.c_int]),
+    "fdtd_last_cuda_error": (C.c_int, []),
+    "fdtd_update_e_f32": (C.c_int, [C.POINTER(Grid)] + [P] * 9 + [P]),
+    "fdtd_update_h_f32": (C.c_int, [C.POINTER(Grid)] + [P] * 9 + [P]),
+    "fdtd_update_pbc_e_f32": (C.c_int, [C.POINTER(Grid), I32, P, P, P, P]),
+    "fdtd_update_pbc_h_f32": (C.c_int, [C.POINTER(Grid), I32, P, P, P, P]),
+    "fdtd_cpml_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml)] + [P] * 9 + [C.POINTER(Psi), P]),
+    "fdtd_cpml_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml)] + [P] * 9 + [C.POINTER(Psi), P]),
+    "fdtd_add_sources_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Sources), I64, P, P, P, P]),
+    "fdtd_step_unfused_f32": (C.c_int, [C.POINTER(Grid), P, P, P, C.POINTER(Cpml), C.POINTER(Psi),
+                                        C.POINTER(Sources), I64, P]),
+    "fdtd_symplectic_h_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),
+    "fdtd_symplectic_e_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),
+    "fdtd_yee_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
+                                       C.POINTER(Sources), C.POINTER(Tile), P, I32]),
+    "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),
+    "fdtd_yee_plan_current": (C.c_int, [P]),
+    "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
+    "fdtd_yee_plan_destroy": (C.c_int, [P]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the library (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libfdtd_gb300.so not built: run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'` "
+                              "or `python fdtd_accelerate_gb300/build.py`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    L = lib()
+    return [n for n in _SIGS if getattr(L, n, None) is not None]
+
+
+def status_string(st):
+    return lib().fdtd_status_string(st).decode()
+
+
+def check(st, fn):
+    if st == FDTD_OK:
+        return
+    msg = status_string(st)
+    if st == FDTD_ERR_CUDA:
+        msg += " (cudaError %d)" % lib().fdtd_last_cuda_error()
+    if st in (FDTD_ERR_ARG, FDTD_ERR_SHAPE, FDTD_ERR_ALIGN, FDTD_ERR_CAPACITY):
+        raise ValueError("%s failed: %s (status %d)" % (fn, msg, st))
+    if st == FDTD_ERR_TIMEOUT:
+        raise TimeoutError("%s failed: %s" % (fn, msg))
+    if st == FDTD_ERR_UNSUPPORTED:
+        raise NotImplementedError("%s failed: %s" % (fn, msg))
+    raise FdtdError(st, fn, msg)
+
+
+def call(name, *args):
+    st = getattr(lib(), name)(*args)
+    check(st, name)

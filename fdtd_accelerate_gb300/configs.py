@@ -1,0 +1,123 @@
+"""Seeded synthetic workloads (the reference publishes no datasets).
+
+Positions of the staggered components in cell units (the Yee grid implied
+by the forward E / backward H differences of 2nd_order-Yee/Numpy/fdtd3d.py):
+    ex[i,j,k] at (i, j+1/2, k+1/2)   ey at (i+1/2, j, k+1/2)   ez at (i+1/2, j+1/2, k)
+Permittivity is sampled at those points (as kuFDTD/v0.2.0/dim3/cpu/matter.py:74-79
+does) and CE = dt / eps_r with dt = 0.5 (matter.py:81-83).
+
+Workloads
+  plain128   128^3, PEC walls, vacuum, Ez point source at the centre,
+             Gaussian-modulated sine (f dt = 0.05, width 30 steps, t0 = 150)
+  cpml1024   1024 x 1024 x 512, 12-cell CPML on all faces (m=4, R=1e-8,
+             kappa_max=5, alpha_max=0.05), 200 seeded spheres (radius 5..40,
+             eps_r U[1,12]), 6 seeded dipoles (delays t0 in [100, 300])
+"""
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .sources import gaussian_sine
+
+__all__ = ["Workload", "plain128", "cpml1024", "scaled", "paint_spheres", "ce_from_spheres",
+           "random_spheres", "random_dipoles", "STAGGER"]
+
+# offsets of (ex, ey, ez) sample points from (i, j, k)
+STAGGER = ((0.0, 0.5, 0.5), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0))
+
+
+@dataclass
+class Workload:
+    name: str
+    shape: tuple
+    steps: int
+    npml: int = 0
+    spheres: list = field(default_factory=list)   # (cx, cy, cz, r, eps_r)
+    dipoles: list = field(default_factory=list)   # (comp, (i, j, k), t0)
+    seed: int = 0
+    pulse_width: float = 30.0
+    pulse_freq: float = 0.05
+    dt: float = 0.5
+
+    @property
+    def cells(self):
+        return int(np.prod(self.shape))
+
+    def source_list(self, nsteps=None):
+        """(comp, ijk, FP64 amplitude table indexed by step number 0..nsteps)."""
+        n = self.steps if nsteps is None else nsteps
+        t = np.arange(n + 1, dtype=np.float64)
+        return [(c, ijk, gaussian_sine(t, t0, self.pulse_width, self.pulse_freq)) for c, ijk, t0 in self.dipoles]
+
+
+def random_spheres(rng, shape, count, rmin, rmax, eps_lo, eps_hi):
+    out = []
+    for _ in range(count):
+        c = [float(rng.uniform(0, n)) for n in shape]
+        r = int(rng.integers(rmin, rmax + 1))
+        eps = float(rng.uniform(eps_lo, eps_hi))
+        out.append((c[0], c[1], c[2], r, eps))
+    return out
+
+
+def random_dipoles(rng, shape, count, margin, t0_lo=100.0, t0_hi=300.0):
+    out = []
+    for _ in range(count):
+        ijk = tuple(int(rng.integers(margin, n - margin)) for n in shape)
+        comp = ("ex", "ey", "ez")[int(rng.integers(0, 3))]
+        out.append((comp, ijk, float(rng.uniform(t0_lo, t0_hi))))
+    return out
+
+
+def plain128(steps=1000):
+    return Workload("plain 2nd-order Yee 128x128x128 PEC vacuum", (128, 128, 128), steps, npml=0,
+                    dipoles=[("ez", (64, 64, 64), 150.0)])
+
+
+def cpml1024(steps=2000, shape=(1024, 1024, 512), seed=20261203, nspheres=200, npml=12, ndipoles=6):
+    rng = np.random.default_rng(seed)
+    spheres = random_spheres(rng, shape, nspheres, 5, 40, 1.0, 12.0)
+    dipoles = random_dipoles(rng, shape, ndipoles, npml + 2)
+    return Workload("Yee+CPML %dx%dx%d, %d-cell CPML, %d spheres, %d dipoles" % (*shape, npml, nspheres, ndipoles),
+                    tuple(shape), steps, npml=npml, spheres=spheres, dipoles=dipoles, seed=seed)
+
+
+def scaled(work, shape, steps=None):
+    """Same construction at another size (spheres scaled with the grid)."""
+    f = [a / b for a, b in zip(shape, work.shape)]
+    sph = [(cx * f[0], cy * f[1], cz * f[2], max(1, int(round(r * min(f)))), e) for cx, cy, cz, r, e in work.spheres]
+    dip = [(c, tuple(min(max(int(v * s), work.npml + 2), n - work.npml - 3) for v, s, n in zip(ijk, f, shape)), t0)
+           for c, ijk, t0 in work.dipoles]
+    return Workload(work.name + " (scaled to %dx%dx%d)" % tuple(shape), tuple(shape),
+                    work.steps if steps is None else steps, npml=work.npml, spheres=sph, dipoles=dip,
+                    seed=work.seed, pulse_width=work.pulse_width, pulse_freq=work.pulse_freq, dt=work.dt)
+
+
+def paint_spheres(shape, spheres, offset, device="cpu", dtype=torch.float32):
+    """eps_r sampled at grid points (i, j, k) + offset; spheres painted in order."""
+    nx, ny, nz = shape
+    eps = torch.ones(shape, dtype=dtype, device=device)
+    for cx, cy, cz, r, e in spheres:
+        lo = [max(0, int(math.floor(c - o - r))) for c, o in zip((cx, cy, cz), offset)]
+        hi = [min(n, int(math.ceil(c - o + r)) + 1) for c, o, n in zip((cx, cy, cz), offset, shape)]
+        if any(h <= l for l, h in zip(lo, hi)):
+            continue
+        x = torch.arange(lo[0], hi[0], device=device, dtype=torch.float64) + offset[0] - cx
+        y = torch.arange(lo[1], hi[1], device=device, dtype=torch.float64) + offset[1] - cy
+        z = torch.arange(lo[2], hi[2], device=device, dtype=torch.float64) + offset[2] - cz
+        d2 = x[:, None, None] ** 2 + y[None, :, None] ** 2 + z[None, None, :] ** 2
+        inside = d2 <= float(r) ** 2
+        sub = eps[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+        sub[inside] = e
+    return eps
+
+
+def ce_from_spheres(shape, spheres, dt=0.5, device="cpu"):
+    """(cex, cey, cez) = dt / eps_r at the staggered component points, FP32."""
+    out = []
+    for off in STAGGER:
+        eps = paint_spheres(shape, spheres, off, device=device, dtype=torch.float64)
+        out.append((dt / eps).to(torch.float32))
+    return out

@@ -1,0 +1,69 @@
+// Shared helpers for the sm_103a kernels and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fdtd_gb300.h"
+
+namespace fdtd {
+
+// Thread-local record of the last CUDA error seen by an entry point.
+void set_cuda_error(cudaError_t e);
+
+// Check a launch; map CUDA failures to FDTD_ERR_CUDA.
+inline int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return FDTD_ERR_CUDA;
+    }
+    return FDTD_OK;
+}
+
+#define FDTD_TRY(expr)                  \
+    do {                                \
+        int _st = (expr);               \
+        if (_st != FDTD_OK) return _st; \
+    } while (0)
+
+struct Grid {
+    int64_t nx, ny, nz, sx, sy;
+};
+
+inline int validate_grid(const fdtd_grid *g, Grid *out) {
+    if (!g) return FDTD_ERR_ARG;
+    if (g->nx < 1 || g->ny < 1 || g->nz < 1) return FDTD_ERR_SHAPE;
+    if (g->sy < g->nz || g->sx < g->ny * g->sy) return FDTD_ERR_SHAPE;
+    if (g->nx > 65535 || g->ny > 65535) return FDTD_ERR_SHAPE;  // grid.y/z launch limits
+    *out = Grid{g->nx, g->ny, g->nz, g->sx, g->sy};
+    return FDTD_OK;
+}
+
+template <typename... P>
+inline bool all_nonnull(P... p) {
+    return ((p != nullptr) && ...);
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Round-to-nearest arithmetic that the compiler may not contract into FMA:
+// the kernels reproduce the rounding of the reference's NumPy expressions.
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+// ((a - b) - c) + d : the grouping NumPy uses for `a - b - c + d`.
+__device__ __forceinline__ float curl4(float a, float b, float c, float d) {
+    return fadd(fsub(fsub(a, b), c), d);
+}
+
+// CPML slab index -> node index (front slab s < P at s+1, back slab at
+// n-P-1+(s-P) for E nodes, n-P+(s-P) for H nodes).
+__device__ __forceinline__ int64_t slab_node_e(int64_t s, int64_t P, int64_t n) {
+    return s < P ? s + 1 : n - P - 1 + (s - P);
+}
+__device__ __forceinline__ int64_t slab_node_h(int64_t s, int64_t P, int64_t n) {
+    return s < P ? s + 1 : n - P + (s - P);
+}
+
+}  // namespace fdtd

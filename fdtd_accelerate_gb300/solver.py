@@ -1,0 +1,172 @@
+"""Whole-simulation driver for the 2nd-order Yee step on one GPU.
+
+YeeSolver owns a z-padded, double-buffered device state (E, H, E-psi) plus
+the coefficient arrays, the CPML layer and the point sources, and advances
+it with the fused kernel (one HBM pass per step, fdtd_yee_plan_* in the C
+ABI) or, for checking, with the unfused reference-shaped kernels
+(fdtd_step_unfused_f32).  Both give bit-identical results.
+
+Step order and time index follow the reference's loop
+(2nd_order-Yee/CUDA/fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:718-742,
+KEMP/v0.7_pml/fdtd3d/main.py:296-326): step number t starts at 1 and the
+source amplitude used in step t is table[t].
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .cpml import CpmlLayer
+from .sources import PointSources
+
+__all__ = ["YeeSolver", "padded_nz", "FIELD_NAMES"]
+
+FIELD_NAMES = ("ex", "ey", "ez", "hx", "hy", "hz")
+
+
+def padded_nz(nz, align=4):
+    """z pitch: a multiple of 4 floats keeps rows 16-byte aligned for TMA."""
+    return (nz + align - 1) // align * align
+
+
+class YeeSolver:
+    def __init__(self, shape, ce=None, npml=0, faces=0x3F, cpml_params=None, sources=(),
+                 device="cuda", tile=None, z_align=4):
+        nx, ny, nz = (int(v) for v in shape)
+        self.shape = (nx, ny, nz)
+        self.device = torch.device(device)
+        self.nzp = padded_nz(nz, z_align)
+        dev = self.device
+        # state[b] : (6, nx, ny, nzp) for buffer b; views give (nx, ny, nz)
+        self._state = torch.zeros((2, 6, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        self._ce = torch.zeros((3, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        if ce is None:
+            self._ce[:, :, :, :nz] = 0.5
+        else:
+            for q in range(3):
+                self._ce[q, :, :, :nz] = torch.as_tensor(ce[q], dtype=torch.float32, device=dev)
+        self.cpml = CpmlLayer(self.shape, npml, faces, device=dev, double_buffer_e=True,
+                              **(cpml_params or {}))
+        self.sources = PointSources(self.shape, sources, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.cur = 0
+        self.tstep = 1
+        self.tile = tile
+        self._plan = None
+
+    # ------------------------------------------------------------------ views
+    def _views(self, b):
+        nz = self.shape[2]
+        return [self._state[b, q, :, :, :nz] for q in range(6)]
+
+    @property
+    def fields(self):
+        return dict(zip(FIELD_NAMES, self._views(self.cur)))
+
+    @property
+    def ce(self):
+        nz = self.shape[2]
+        return [self._ce[q, :, :, :nz] for q in range(3)]
+
+    def set_fields(self, **arrays):
+        f = self.fields
+        for k, v in arrays.items():
+            f[k].copy_(torch.as_tensor(v, dtype=torch.float32, device=self.device))
+
+    def load_host(self, fields, ce=None):
+        """Copy host arrays (ideally pinned) into the current state and,
+        optionally, the E coefficients; stream-ordered on the current stream."""
+        f = self.fields
+        for k, v in fields.items():
+            f[k].copy_(torch.as_tensor(v), non_blocking=True)
+        if ce is not None:
+            for q in range(3):
+                self.ce[q].copy_(torch.as_tensor(ce[q]), non_blocking=True)
+
+    def store_host(self, fields):
+        """Copy the current state into host arrays (dict of CPU tensors)."""
+        f = self.fields
+        for k, v in fields.items():
+            v.copy_(f[k], non_blocking=True)
+
+    def grid(self):
+        nx, ny, nz = self.shape
+        return N.Grid(nx, ny, nz, ny * self.nzp, self.nzp)
+
+    # ------------------------------------------------------------------ fused
+    def _state_struct(self):
+        s = N.YeeState()
+        for b in range(2):
+            for q in range(6):
+                s.f[b][q] = self._state[b, q].data_ptr()
+                e = self.cpml.psi_e[b][q]
+                s.psi_e[b][q] = e.data_ptr() if e is not None else None
+        for q in range(6):
+            h = self.cpml.psi_h[q]
+            s.psi_h[q] = h.data_ptr() if h is not None else None
+        for q in range(3):
+            s.ce[q] = self._ce[q].data_ptr()
+        return s
+
+    def plan(self):
+        if self._plan is None:
+            g = self.grid()
+            st = self._state_struct()
+            cp = self.cpml.struct()
+            src = self.sources.struct()
+            tile = N.Tile(*(self.tile or (0, 0, 0)))
+            h = C.c_void_p()
+            with torch.cuda.device(self.device):
+                N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
+                       C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), self.cur)
+            self._plan = h
+        return self._plan
+
+    def step(self, n=1):
+        """Advance n steps with the fused kernel (one launch per step)."""
+        plan = self.plan()
+        L = N.lib()
+        L.fdtd_yee_plan_set_current(plan, self.cur)
+        with torch.cuda.device(self.device):
+            stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            N.call("fdtd_yee_plan_run", plan, int(self.tstep), int(n), stream)
+        self.cur = L.fdtd_yee_plan_current(plan)
+        self.tstep += n
+
+    def step_unfused(self, n=1):
+        """Advance n steps in place with the reference-shaped kernels."""
+        g = self.grid()
+        cp = self.cpml.struct()
+        psi = self.cpml.psi_struct(self.cur)
+        src = self.sources.struct()
+        f = (C.c_void_p * 6)(*[self._state[self.cur, q].data_ptr() for q in range(6)])
+        ce = (C.c_void_p * 3)(*[self._ce[q].data_ptr() for q in range(3)])
+        with torch.cuda.device(self.device):
+            stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            for _ in range(n):
+                N.call("fdtd_step_unfused_f32", C.byref(g), f, ce, None,
+                       C.byref(cp) if self.cpml.active else None, C.byref(psi),
+                       C.byref(src), int(self.tstep), stream)
+                self.tstep += 1
+
+    def check_status(self):
+        """Raise if a bounded device wait expired in an earlier step."""
+        v = int(self.status.item())
+        if v:
+            self.status.zero_()
+            N.check(v, "fdtd_yee_plan_run (device status)")
+
+    def psi_e(self):
+        return self.cpml.psi_e[self.cur]
+
+    def close(self):
+        if self._plan is not None:
+            N.lib().fdtd_yee_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

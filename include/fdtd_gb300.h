@@ -1,0 +1,170 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 (sm_103a) Yee time-step engine.
+ *
+ * Plain C: pointers, sizes, an opaque stream handle.  All field pointers
+ * are DEVICE pointers to float32 arrays of logical shape (nx, ny, nz),
+ * z fastest, with element strides sx (x) and sy (y) and unit z stride --
+ * the memory layout of the reference's C-order NumPy field arrays (and of
+ * KEMP's z-padded arrays).  Every entry point is stream-ordered (no host
+ * synchronisation), allocates no device memory, never exits the process,
+ * and returns an fdtd_status.  `stream` is a cudaStream_t (NULL = legacy
+ * default stream).
+ *
+ * Reference interfaces replaced (paths inside wbkifun/fdtd_accelerate):
+ *   fdtd_update_e_f32      2nd_order-Yee/Numpy/fdtd3d.py:10-13 update_e;
+ *                          2nd_order-Yee/python-C/dielectric-sse-omp.c:68-121;
+ *                          KEMP/v0.7_pml/fdtd3d/cpu/src/core.c:11 (ctypes
+ *                          argtypes KEMP/v0.7_pml/fdtd3d/cpu/core.py:89-105)
+ *   fdtd_update_h_f32      2nd_order-Yee/Numpy/fdtd3d.py:4-7 update_h;
+ *                          KEMP/v0.7_pml/fdtd3d/cpu/src/core.c:59 (ch arrays
+ *                          of coeff_use='h', naive/core.py:37-47)
+ *   fdtd_update_pbc_{e,h}  2nd_order-Yee/Numpy/fdtd3d.py:16-37
+ *   fdtd_cpml_{e,h}_f32    kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c:14-429
+ *                          update_{x,y,z}_{e,h} (one call covers all axes and
+ *                          faces), with the kappa term of
+ *                          kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c:238-263
+ *   fdtd_add_sources_f32   2nd_order-Yee/CUDA/fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:352-363
+ *                          updateSrc; KEMP/v0.7_pml/fdtd3d/naive/incident_direct.py:52-70
+ *   fdtd_step_unfused_f32  one time step in the order of
+ *                          fdtd3d_201_..._100000tstep.cu:718-742
+ *   fdtd_yee_plan_*        the same step, fused into one pass per step
+ *                          (no reference counterpart as one call; replaces
+ *                          the >= 15 launches per step of the loop above)
+ *   fdtd_symplectic_{h,e}_f32  4th_order-Symplectic/PyCUDA/100-base.py:10-44
+ *                          update_h / update_e (stage coefficient argument);
+ *                          4th_order-Symplectic/Python-C/dielectric.c:5-96
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FDTD_OK = 0,
+    FDTD_ERR_ARG = 1,         /* null pointer or invalid scalar argument   */
+    FDTD_ERR_SHAPE = 2,       /* extents / strides inconsistent            */
+    FDTD_ERR_ALIGN = 3,       /* pointer or stride alignment requirement   */
+    FDTD_ERR_CUDA = 4,        /* CUDA runtime/driver error (see fdtd_last_cuda_error) */
+    FDTD_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired        */
+    FDTD_ERR_UNSUPPORTED = 6, /* configuration not supported by this path  */
+    FDTD_ERR_CAPACITY = 7     /* request exceeds a fixed capacity          */
+} fdtd_status;
+
+/* Grid: logical extents and element strides (z stride is 1). */
+typedef struct {
+    int64_t nx, ny, nz;
+    int64_t sx, sy;
+} fdtd_grid;
+
+/* CPML: slab thickness per axis (0 = none), enabled faces (bit 2a = front,
+ * bit 2a+1 = back face of axis a), and device tables of 2*npml[a] entries:
+ * b, a and km1 = 1/kappa - 1, for E nodes and H nodes.  Slab index s < P is
+ * the front slab at node s+1; s >= P the back slab at node n-P-1+(s-P)
+ * (E) or n-P+(s-P) (H). */
+typedef struct {
+    int32_t npml[3];
+    int32_t faces;
+    const float *b_e[3], *a_e[3], *km1_e[3];
+    const float *b_h[3], *a_h[3], *km1_h[3];
+} fdtd_cpml;
+
+/* psi slabs, dense: x (2P, ny, nz), y (nx, 2P, nz), z (nx, ny, 2P).
+ * e: eyx, ezx, ezy, exy, exz, eyz     h: hyx, hzx, hzy, hxy, hxz, hyz
+ * (NULL allowed for an axis without PML). */
+typedef struct {
+    float *e[6];
+    float *h[6];
+} fdtd_psi;
+
+/* Soft sources: F[i,j,k] += amp[s*namp + t] for step t (0 <= t < namp),
+ * applied after the E update and its CPML correction, in list order.
+ * comp: 0..2 = ex, ey, ez.  All arrays are device arrays. */
+typedef struct {
+    int32_t nsrc;
+    const int32_t *ijk;   /* 3*nsrc */
+    const int32_t *comp;  /* nsrc   */
+    const float *amp;     /* nsrc*namp */
+    int64_t namp;
+} fdtd_sources;
+
+const char *fdtd_status_string(int status);
+int fdtd_last_cuda_error(void);
+
+/* ---- reference-shaped kernels (in place) ---------------------------- */
+int fdtd_update_e_f32(const fdtd_grid *g, float *ex, float *ey, float *ez,
+                      const float *hx, const float *hy, const float *hz,
+                      const float *cex, const float *cey, const float *cez, void *stream);
+/* ch pointers may be NULL: constant 0.5 (fdtd3d.py / KEMP coeff_use='') */
+int fdtd_update_h_f32(const fdtd_grid *g, const float *ex, const float *ey, const float *ez,
+                      float *hx, float *hy, float *hz,
+                      const float *chx, const float *chy, const float *chz, void *stream);
+/* axes: bit 0 = x, 1 = y, 2 = z */
+int fdtd_update_pbc_e_f32(const fdtd_grid *g, int32_t axes, float *ex, float *ey, float *ez, void *stream);
+int fdtd_update_pbc_h_f32(const fdtd_grid *g, int32_t axes, float *hx, float *hy, float *hz, void *stream);
+int fdtd_cpml_e_f32(const fdtd_grid *g, const fdtd_cpml *c,
+                    float *ex, float *ey, float *ez,
+                    const float *hx, const float *hy, const float *hz,
+                    const float *cex, const float *cey, const float *cez,
+                    const fdtd_psi *psi, void *stream);
+int fdtd_cpml_h_f32(const fdtd_grid *g, const fdtd_cpml *c,
+                    const float *ex, const float *ey, const float *ez,
+                    float *hx, float *hy, float *hz,
+                    const float *chx, const float *chy, const float *chz,
+                    const fdtd_psi *psi, void *stream);
+int fdtd_add_sources_f32(const fdtd_grid *g, const fdtd_sources *src, int64_t t,
+                         float *ex, float *ey, float *ez, void *stream);
+
+/* One whole step, unfused (update_e, cpml_e, sources, update_h, cpml_h),
+ * in place.  c and src may be NULL. */
+int fdtd_step_unfused_f32(const fdtd_grid *g, float *const f[6], const float *const ce[3],
+                          const float *const ch[3], const fdtd_cpml *c, const fdtd_psi *psi,
+                          const fdtd_sources *src, int64_t t, void *stream);
+
+/* ---- fused Yee step (one HBM pass per step) --------------------------- */
+/* State in two buffers (ping-pong): f[b] = ex,ey,ez,hx,hy,hz of buffer b,
+ * psi_e[b] the E-psi slabs of buffer b; psi_h is updated in place.
+ * Requirements: sx, sy multiples of 4 and 16-byte aligned base pointers;
+ * nx, ny, nz >= 2.  ch is the constant 0.5 on this path. */
+typedef struct {
+    float *f[2][6];
+    float *psi_e[2][6];
+    float *psi_h[6];
+    const float *ce[3];
+} fdtd_yee_state;
+
+typedef struct {
+    int32_t tile_y;       /* 0 = default */
+    int32_t x_chunk;      /* planes per work item, 0 = default */
+    int32_t ctas_per_sm;  /* 0 = default */
+} fdtd_tile;
+
+typedef struct fdtd_yee_plan fdtd_yee_plan;
+
+/* status_dev: device int32 the kernel sets non-zero when a bounded wait
+ * expires (may be NULL). cur: index of the buffer holding the state now. */
+int fdtd_yee_plan_create(fdtd_yee_plan **plan, const fdtd_grid *g, const fdtd_yee_state *st,
+                         const fdtd_cpml *c, const fdtd_sources *src, const fdtd_tile *tile,
+                         int32_t *status_dev, int32_t cur);
+int fdtd_yee_plan_run(fdtd_yee_plan *plan, int64_t t0, int64_t nsteps, void *stream);
+int fdtd_yee_plan_current(const fdtd_yee_plan *plan);
+int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
+int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
+
+/* ---- 4th-order symplectic stages (in place) --------------------------- */
+int fdtd_symplectic_h_f32(const fdtd_grid *g, float cl,
+                          const float *ex, const float *ey, const float *ez,
+                          float *hx, float *hy, float *hz,
+                          const float *chx, const float *chy, const float *chz, void *stream);
+int fdtd_symplectic_e_f32(const fdtd_grid *g, float dl,
+                          float *ex, float *ey, float *ez,
+                          const float *hx, const float *hy, const float *hz,
+                          const float *cex, const float *cey, const float *cez, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDTD_GB300_H */

@@ -1,0 +1,90 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry
+point declared in include/*.h, and rejects bad arguments before touching
+CUDA (argument validation runs on the host)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+from tests.conftest import ROOT
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(fdtd_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fdtd_accelerate_gb300 import _native, build
+    build()
+    return _native.lib()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for n in ("fdtd_update_e_f32", "fdtd_update_h_f32", "fdtd_cpml_e_f32", "fdtd_cpml_h_f32",
+              "fdtd_yee_plan_create", "fdtd_yee_plan_run", "fdtd_symplectic_h_f32"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings(lib):
+    from fdtd_accelerate_gb300 import _native as N
+    for st in range(8):
+        assert N.status_string(st)
+    assert N.status_string(0) == "ok"
+
+
+def test_validation_before_cuda(lib):
+    """Null pointers and inconsistent grids are rejected on the host."""
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(4, 5, 6, 30, 6)
+    null = [None] * 9
+    assert lib.fdtd_update_e_f32(C.byref(g), *null, None) == N.FDTD_ERR_ARG
+    bad = N.Grid(4, 5, 6, 29, 6)     # sx < ny*sy
+    assert lib.fdtd_update_h_f32(C.byref(bad), *null, None) == N.FDTD_ERR_SHAPE
+    bad = N.Grid(0, 5, 6, 30, 6)
+    assert lib.fdtd_update_e_f32(C.byref(bad), *null, None) == N.FDTD_ERR_SHAPE
+    assert lib.fdtd_update_pbc_e_f32(None, 1, None, None, None, None) == N.FDTD_ERR_ARG
+    h = C.c_void_p()
+    assert lib.fdtd_yee_plan_create(C.byref(h), C.byref(g), None, None, None, None, None, 0) == N.FDTD_ERR_ARG
+
+
+def test_plan_rejects_unaligned_strides(lib):
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(4, 5, 6, 30, 6)       # sy = 6 floats: rows not 16-byte aligned
+    st = N.YeeState()
+    for b in range(2):
+        for q in range(6):
+            st.f[b][q] = 0x1000 * (1 + q + 6 * b)
+    for q in range(3):
+        st.ce[q] = 0x100000 + 0x1000 * q
+    h = C.c_void_p()
+    status = C.c_int32(0)
+    r = lib.fdtd_yee_plan_create(C.byref(h), C.byref(g), C.byref(st), None, None, None,
+                                 C.byref(status), 0)
+    assert r == N.FDTD_ERR_ALIGN
+
+
+def test_error_mapping():
+    from fdtd_accelerate_gb300 import _native as N
+    with pytest.raises(ValueError):
+        N.check(N.FDTD_ERR_SHAPE, "f")
+    with pytest.raises(TimeoutError):
+        N.check(N.FDTD_ERR_TIMEOUT, "f")
+    with pytest.raises(NotImplementedError):
+        N.check(N.FDTD_ERR_UNSUPPORTED, "f")
+    with pytest.raises(RuntimeError):
+        N.check(N.FDTD_ERR_CUDA, "f")

@@ -1,0 +1,229 @@
+"""GPU parity of the 2nd-order Yee kernels against the oracle and the
+reference's golden outputs (bit-exact: the kernels evaluate the reference's
+FP32 expressions with the same rounding and no FMA contraction)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests.conftest import cuda_available
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not cuda_available(), reason="needs a CUDA GPU")]
+
+NAMES = ("ex", "ey", "ez", "hx", "hy", "hz")
+
+
+@pytest.fixture(scope="module")
+def fdtd():
+    import fdtd_accelerate_gb300 as F
+    F.build()
+    return F
+
+
+def _dev(a, pad=0):
+    """Device copy; pad > 0 gives a z-padded view with the same logical shape."""
+    nx, ny, nz = a.shape
+    if pad == 0:
+        return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    store = torch.zeros((nx, ny, nz + pad), dtype=torch.float32, device="cuda")
+    v = store[:, :, :nz]
+    v.copy_(torch.from_numpy(a))
+    return v
+
+
+def _host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,pad", [((9, 8, 12), 0), ((17, 19, 23), 0), ((17, 19, 23), 5),
+                                       ((2, 3, 4), 0), ((64, 33, 130), 2)])
+def test_update_e_h_bit_exact_vs_oracle(fdtd, shape, pad):
+    rng = np.random.default_rng(7)
+    h = {k: rng.standard_normal(shape).astype(np.float32) for k in NAMES}
+    ce = [rng.random(shape, dtype=np.float32) for _ in range(3)]
+    ch = [rng.random(shape, dtype=np.float32) for _ in range(3)]
+    d = {k: _dev(v, pad) for k, v in h.items()}
+    dce = [_dev(c, pad) for c in ce]
+    dch = [_dev(c, pad) for c in ch]
+    for step in range(3):
+        oracle.update_e(*(h[k] for k in NAMES), *ce)
+        fdtd.update_e(*(d[k] for k in NAMES), *dce)
+        if step == 1:
+            oracle.update_h(*(h[k] for k in NAMES), *ch)
+            fdtd.update_h(*(d[k] for k in NAMES), *dch)
+        else:
+            oracle.update_h(*(h[k] for k in NAMES))
+            fdtd.update_h(*(d[k] for k in NAMES))
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(d[k]), h[k], err_msg=k)
+
+
+def test_golden_numpy_reference_through_gpu(fdtd, golden_dir):
+    """Reference fdtd3d.py outputs (tests/golden/yee_numpy.npz) reproduced by
+    the GPU kernels called through the reference-shaped API."""
+    g = np.load(os.path.join(golden_dir, "yee_numpy.npz"))
+    for n in range(int(g["ncases"])):
+        t = "c%d_" % n
+        d = {k: _dev(g[t + "in_" + k]) for k in NAMES}
+        ce = [_dev(g[t + "in_" + k]) for k in ("cex", "cey", "cez")]
+        nsteps, axes = (int(v) for v in g[t + "meta"])
+        src = tuple(int(v) for v in g[t + "src"])
+        dirs = "".join(a for b, a in ((1, "x"), (2, "y"), (4, "z")) if axes & b)
+        for s in range(nsteps):
+            fdtd.update_e(*(d[k] for k in NAMES), *ce)
+            if dirs:
+                fdtd.update_pbc_e(dirs, d["ex"], d["ey"], d["ez"])
+            d["ez"][src] += float(g[t + "amps"][s])
+            fdtd.update_h(*(d[k] for k in NAMES))
+            if dirs:
+                fdtd.update_pbc_h(dirs, d["hx"], d["hy"], d["hz"])
+        for k in NAMES:
+            np.testing.assert_array_equal(_host(d[k]), g[t + "out_" + k], err_msg="case %d %s" % (n, k))
+
+
+def test_golden_kemp_core_through_gpu(fdtd, golden_dir):
+    """KEMP's SSE core groups the curl differently: agreement to 4 ulp."""
+    g = np.load(os.path.join(golden_dir, "kemp_core.npz"))
+    for n in range(int(g["ncases"])):
+        t = "c%d_" % n
+        nz, pad, coeff, ufunc = (int(v) for v in g[t + "meta"])
+        d = {k: _dev(g[t + "in_" + k], pad) for k in NAMES}
+        if ufunc == 0:
+            fdtd.update_e(*(d[k] for k in NAMES), *(_dev(g[t + "in_" + k], pad) for k in ("cex", "cey", "cez")))
+            comps = NAMES[:3]
+        else:
+            ch = [_dev(g[t + "in_" + k], pad) for k in ("chx", "chy", "chz")] if coeff else [None] * 3
+            fdtd.update_h(*(d[k] for k in NAMES), *ch)
+            comps = NAMES[3:]
+        for k in comps:
+            ref = g[t + "out_" + k]
+            tol = 4 * np.finfo(np.float32).eps * max(1.0, np.abs(ref).max())
+            assert np.abs(_host(d[k]) - ref).max() <= tol, (n, k)
+
+
+def _kappa_tables(npml):
+    t = [oracle.cpml_tables(p) for p in npml]
+    return {key: [t[a][key] if npml[a] else None for a in range(3)]
+            for key in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h")}
+
+
+@pytest.mark.parametrize("shape,npml,faces", [((20, 18, 22), (3, 4, 5), 0x3F), ((20, 18, 22), (3, 0, 5), 0x15),
+                                              ((31, 27, 16), (6, 6, 6), 0x2A)])
+def test_cpml_kernels_bit_exact_vs_oracle(fdtd, shape, npml, faces):
+    rng = np.random.default_rng(3)
+    f = {k: rng.standard_normal(shape).astype(np.float32) for k in NAMES}
+    ce = [rng.random(shape, dtype=np.float32) for _ in range(3)]
+    layer = fdtd.CpmlLayer(shape, npml, faces)
+    # the device layer's FP32 tables are the oracle's FP64 tables rounded once
+    tables = _kappa_tables(layer.npml)
+    for key in tables:
+        for a in range(3):
+            if layer.npml[a]:
+                np.testing.assert_array_equal(layer.tables[a][key].cpu().numpy(),
+                                              tables[key][a].astype(np.float32))
+    P = layer.npml
+    pshape = [(2 * P[0], shape[1], shape[2]), (shape[0], 2 * P[1], shape[2]), (shape[0], shape[1], 2 * P[2])]
+    psi_e = [np.zeros(pshape[a], np.float32) if P[a] else None for a in range(3) for _ in range(2)]
+    psi_h = [np.zeros(pshape[a], np.float32) if P[a] else None for a in range(3) for _ in range(2)]
+    d = {k: _dev(v) for k, v in f.items()}
+    dce = [_dev(c) for c in ce]
+    for _ in range(4):
+        oracle.update_e(*(f[k] for k in NAMES), *ce)
+        oracle.cpml_e(P, layer.faces, tables, *(f[k] for k in NAMES), *ce, psi_e)
+        oracle.update_h(*(f[k] for k in NAMES))
+        oracle.cpml_h(P, layer.faces, tables, *(f[k] for k in NAMES), psi_h)
+        fdtd.update_e(*(d[k] for k in NAMES), *dce)
+        layer.update_e(*(d[k] for k in NAMES), *dce)
+        fdtd.update_h(*(d[k] for k in NAMES))
+        layer.update_h(*(d[k] for k in NAMES))
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(d[k]), f[k], err_msg=k)
+    for q in range(6):
+        if psi_e[q] is not None:
+            np.testing.assert_array_equal(_host(layer.psi_e[0][q]), psi_e[q], err_msg="psi_e%d" % q)
+            np.testing.assert_array_equal(_host(layer.psi_h[q]), psi_h[q], err_msg="psi_h%d" % q)
+
+
+def _oracle_sim(work_shape, ce, npml, faces, sources, init):
+    tables = _kappa_tables(npml)
+    fields = {k: init[k].copy() for k in NAMES}
+    fields.update(cex=ce[0], cey=ce[1], cez=ce[2])
+    return oracle.OracleSim(fields, npml, faces, tables,
+                            [(c, ijk, a.astype(np.float32)) for c, ijk, a in sources])
+
+
+@pytest.mark.parametrize("shape,npml,tile", [
+    ((37, 29, 45), 5, None),
+    ((37, 29, 45), 5, (4, 7, 0)),
+    ((40, 33, 64), 6, (16, 16, 0)),
+    ((24, 20, 36), 0, (8, 5, 0)),
+    ((70, 9, 100), 3, (8, 64, 0)),
+])
+def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
+    from fdtd_accelerate_gb300 import configs
+    rng = np.random.default_rng(11)
+    spheres = configs.random_spheres(rng, shape, 6, 2, 6, 1.0, 12.0)
+    ce = [c.numpy() for c in configs.ce_from_spheres(shape, spheres)]
+    nsteps = 9
+    t = np.arange(nsteps + 2, dtype=np.float64)
+    sources = [("ez", (shape[0] // 2, shape[1] // 2, shape[2] // 2), fdtd.gaussian_sine(t, 3.0, 2.0, 0.1)),
+               ("ex", (npml + 2, shape[1] - npml - 3, npml + 2), fdtd.gaussian_sine(t, 5.0, 2.0, 0.1)),
+               ("ey", (shape[0] // 3, 1, shape[2] - 2), fdtd.gaussian_sine(t, 4.0, 3.0, 0.1))]
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    faces = 0x3F
+    sim = _oracle_sim(shape, ce, (npml,) * 3, faces, sources, init)
+    sim.step(nsteps)
+
+    fused = fdtd.YeeSolver(shape, ce=ce, npml=npml, faces=faces, sources=sources, tile=tile)
+    fused.set_fields(**init)
+    fused.step(nsteps)
+    unf = fdtd.YeeSolver(shape, ce=ce, npml=npml, faces=faces, sources=sources)
+    unf.set_fields(**init)
+    unf.step_unfused(nsteps)
+    torch.cuda.synchronize()
+    fused.check_status()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(unf.fields[k]), sim.f[k], err_msg="unfused " + k)
+        np.testing.assert_array_equal(_host(fused.fields[k]), sim.f[k], err_msg="fused " + k)
+    if npml:
+        for q in range(6):
+            np.testing.assert_array_equal(_host(fused.psi_e()[q]), sim.psi_e[q], err_msg="psi_e%d" % q)
+            np.testing.assert_array_equal(_host(fused.cpml.psi_h[q]), sim.psi_h[q], err_msg="psi_h%d" % q)
+
+
+def test_fused_then_unfused_interleave(fdtd):
+    shape = (33, 30, 40)
+    rng = np.random.default_rng(5)
+    init = {k: rng.standard_normal(shape).astype(np.float32) for k in NAMES}
+    a = fdtd.YeeSolver(shape, npml=4)
+    b = fdtd.YeeSolver(shape, npml=4)
+    a.set_fields(**init)
+    b.set_fields(**init)
+    a.step(3)
+    a.step_unfused(2)
+    a.step(2)
+    b.step_unfused(7)
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)
+
+
+def test_api_errors(fdtd):
+    a = torch.zeros((4, 5, 6), device="cuda")
+    with pytest.raises(TypeError):
+        fdtd.update_h(a, a, a, a, a, a.double())
+    with pytest.raises(TypeError):
+        fdtd.update_e(a, a, a, a, a, a, a, a, np.zeros((4, 5, 6), np.float32))
+    with pytest.raises(ValueError):
+        fdtd.update_h(a, a, a, a, a, torch.zeros((4, 5, 7), device="cuda"))
+    with pytest.raises(ValueError):
+        fdtd.update_h(a, a, a, a, a, a.cpu())
+    with pytest.raises(ValueError):
+        fdtd.update_pbc_e("xw", a, a, a)
+    with pytest.raises(ValueError):
+        fdtd.YeeSolver((10, 10, 10), npml=5)   # 2P+2 > n

@@ -47,7 +47,7 @@ class YeeState(C.Structure):
 
 
 class Tile(C.Structure):
-    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32)]
+    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32)]
 
 
 class FdtdError(RuntimeError):
@@ -75,6 +75,7 @@ _SIGS = {
     "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),
     "fdtd_yee_plan_current": (C.c_int, [P]),
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
+    "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
 }
 

@@ -1,7 +1,9 @@
 """In-tree build of libfdtd_gb300.so (sm_103a) with nvcc.
 
 Each csrc/*.cu translation unit is compiled in parallel with
-``-gencode arch=compute_103a,code=sm_103a -lineinfo``; the objects are
+``-gencode arch=compute_103a,code=sm_103a -lineinfo --fmad=false`` (no
+multiply-add contraction anywhere: every kernel reproduces the separately
+rounded products and sums of the reference's FP32 arithmetic); the objects are
 linked into fdtd_accelerate_gb300/libfdtd_gb300.so next to this file.
 Object files live in fdtd_accelerate_gb300/_build/.  A unit is rebuilt
 when it or any header is newer than its object.
@@ -19,7 +21,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libfdtd_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-O2",
               "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
 
 

@@ -3,7 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/fdtd_gb300.h"
+#include "fdtd_gb300.h"
 
 namespace fdtd {
 

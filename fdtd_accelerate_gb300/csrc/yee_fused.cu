@@ -31,36 +31,46 @@
 namespace fdtd {
 namespace fused {
 
-constexpr int TZ = 32;
-constexpr int HC = TZ + 8;  // H box: k0-4 .. k0+TZ+3 (needs k0-1 .. k0+TZ)
-constexpr int EC = TZ + 4;  // E/CE box: k0-4 .. k0+TZ-1 (needs k0-1 .. k0+TZ-1)
-constexpr int NS = 4;       // pipeline stages (planes in flight)
+// Tile: TZ cells along z (two per lane: lanes work on float2 pairs) x TY rows.
+constexpr int TZ = 64;
+constexpr int HC = TZ + 8;   // H box:    k0-4 .. k0+TZ+3 (needs k0-1 .. k0+TZ)
+constexpr int EC = TZ + 4;   // E/CE box: k0-4 .. k0+TZ-1 (needs k0-1 .. k0+TZ-1)
+constexpr int NCW = TZ + 4;  // E_new row stride; column c holds k = k0-2+c
 constexpr int MAX_LOCAL_SRC = 16;
 constexpr uint64_t WAIT_NS = 1000000000ull;  // a wait gives up after 1 s
 
 constexpr int al128(int b) { return (b + 127) / 128 * 128; }
 
-template <int TY>
+// Shared-memory layout of one CTA for tile height TY and NS pipeline stages.
+// Warps 0..TY-1 own rows j0..j0+TY-1 (E and H); warp TY recomputes E_new on
+// the halo row j0-1; warp TY+1 recomputes E_new on the halo column k0-1.
+template <int TY, int NS>
 struct Layout {
     static constexpr int HR = TY + 2, ER = TY + 1;
     static constexpr int HBOX = HR * HC, EBOX = ER * EC;  // floats per component box
     static constexpr int HBOXB = al128(HBOX * 4), EBOXB = al128(EBOX * 4);
     static constexpr int STAGE = 3 * HBOXB + 6 * EBOXB;  // H(3), E(3), CE(3)
     static constexpr uint32_t TX = 3 * HBOX * 4 + 6 * EBOX * 4;
-    static constexpr int NR = TY + 1, NC = TZ + 1;
-    static constexpr int ENEW = al128(3 * NR * NC * 4);
+    static constexpr int NR = TY + 1;
+    static constexpr int ENEWC = NR * NCW;  // floats per component
+    static constexpr int THREADS = (TY + 2) * 32;
+    static constexpr int ENEW = al128(3 * ENEWC * 4);
     static constexpr int SMEM = NS * STAGE + ENEW + 128 /*barriers*/ + 128 /*align slack*/;
+    // CTAs per SM the register budget is sized for (shared memory may allow fewer)
+    static constexpr int MINB = TY == 4 ? 3 : (TY == 8 ? 2 : 1);
 };
 
 struct TMaps {
     CUtensorMap h[3];   // hx, hy, hz of the input buffer, box (HC, TY+2, 1)
     CUtensorMap e[3];   // ex, ey, ez of the input buffer, box (EC, TY+1, 1)
     CUtensorMap ce[3];  // cex, cey, cez,                  box (EC, TY+1, 1)
+    CUtensorMap zpe[2]; // z-slab E psi (exz, eyz) of the input buffer, box (2P, TY+1, 1)
+    CUtensorMap zph[2]; // z-slab H psi (hxz, hyz),                    box (2P, TY+1, 1)
 };
 
 struct Params {
     int64_t nx, ny, nz, sx, sy;
-    int32_t ntz, nty, x_chunk;
+    int32_t ntz, nty, nxc, x_chunk;
     float *out[6];  // ex, ey, ez, hx, hy, hz of the output buffer
     const float *psi_e_in[6];
     float *psi_e_out[6];
@@ -76,6 +86,11 @@ struct Params {
     int64_t namp;
     int64_t t;
     int32_t *status;
+    // z-slab psi staged by TMA with the fields (tiles touching a z slab)
+    int32_t zpsi;         // 1 when the z-psi boxes are used
+    int32_t stage_bytes;  // bytes per pipeline stage (fields + z-psi boxes)
+    int32_t zbox;         // bytes per z-psi box in shared memory (128-aligned)
+    uint32_t tx_z;        // bytes the 4 z-psi boxes deliver
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -156,55 +171,89 @@ __device__ __forceinline__ float cpml_corr(float &psi, float b, float a, float k
     return fadd(fmul(km1, d), psi);
 }
 
-template <int TY>
-__global__ void __launch_bounds__(TY * 32)
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void st2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+#ifndef FDTD_PACKED_F32X2
+#define FDTD_PACKED_F32X2 0
+#endif
+#if FDTD_PACKED_F32X2
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b rounds exactly like a + (-b)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+#else
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(fadd(a.x, b.x), fadd(a.y, b.y)); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(fsub(a.x, b.x), fsub(a.y, b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(fmul(a.x, b.x), fmul(a.y, b.y)); }
+#endif
+__device__ __forceinline__ float2 curl4x2(float2 a, float2 b, float2 c, float2 d) {
+    return add2(sub2(sub2(a, b), c), d);
+}
+__device__ __forceinline__ float get(const float2 &v, int e) { return e ? v.y : v.x; }
+__device__ __forceinline__ void set(float2 &v, int e, float x) {
+    if (e) v.y = x; else v.x = x;
+}
+
+// CPML table entry of one slab node (b, a, 1/kappa - 1).
+struct Coef {
+    float b, a, km;
+};
+
+// psi <- b psi + a d; returns km1 d + psi (the CPML correction term)
+__device__ __forceinline__ float corr(float &psi, const Coef &c, float d) {
+    psi = fadd(fmul(c.b, psi), fmul(c.a, d));
+    return fadd(fmul(c.km, d), psi);
+}
+
+// Coefficients of slab node s from the shared-memory tables of one axis
+// (base = first of the six tables, n2 = 2P entries each; eh = 0 E, 1 H).
+__device__ __forceinline__ Coef tab_coef(const float *tabs, int base, int n2, int eh, int s) {
+    const float *t = tabs + base + eh * 3 * n2;
+    return Coef{t[s], t[n2 + s], t[2 * n2 + s]};
+}
+
+template <int TY, int NS>
+__global__ void __launch_bounds__(Layout<TY, NS>::THREADS, Layout<TY, NS>::MINB)
 k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
-    using L = Layout<TY>;
+    using L = Layout<TY, NS>;
+    // A stage is released one iteration after its plane was consumed, and each
+    // iteration holds two planes: fewer than 3 stages would wait on a plane
+    // that is only issued after the wait.
+    static_assert(NS >= 3, "the fused pipeline needs at least 3 stages");
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *enew = reinterpret_cast<float *>(smem + NS * L::STAGE);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * L::STAGE + L::ENEW);
+    float *enew = reinterpret_cast<float *>(smem + NS * p.stage_bytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * p.stage_bytes + L::ENEW);
+    float *Nx = enew, *Ny = enew + L::ENEWC, *Nz = enew + 2 * L::ENEWC;
+    // CPML tables in shared memory: tab[(axis*2 + eh)*3 + {b,a,km}] has 2P[axis] entries
+    float *tabs = reinterpret_cast<float *>(smem + NS * p.stage_bytes + L::ENEW + 128);
 
     __shared__ int s_abort;
     __shared__ int s_nls;
-    __shared__ int s_ls_i[MAX_LOCAL_SRC], s_ls_r[MAX_LOCAL_SRC], s_ls_c[MAX_LOCAL_SRC];
+    __shared__ int s_ls_i[MAX_LOCAL_SRC], s_ls_j[MAX_LOCAL_SRC], s_ls_k[MAX_LOCAL_SRC];
     __shared__ int s_ls_comp[MAX_LOCAL_SRC], s_ls_s[MAX_LOCAL_SRC];
 
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int item = blockIdx.x;
-    const int tzi = item % p.ntz, tyi = (item / p.ntz) % p.nty, xci = item / (p.ntz * p.nty);
-    const int64_t k0 = (int64_t)tzi * TZ, j0 = (int64_t)tyi * TY;
-    const int64_t x0 = (int64_t)xci * p.x_chunk;
-    const int64_t x1 = min(x0 + (int64_t)p.x_chunk, p.nx);
-    const int64_t i_start = x0 > 0 ? x0 - 1 : 0;
-    const int64_t last_plane = x1;  // H(x1) feeds E(x1-1); beyond nx the box is zero-filled
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // Roles.  E phase: warps 0..TY-1 -> own row r = warp+1 (j = j0+warp), pair
+    // k = k0+2*lane; warp TY -> halo row r = 0 (j = j0-1); warp TY+1 -> halo
+    // column: lane r <= TY computes the pair at k0-2, k0-1 of row r (only the
+    // k0-1 value is used).  H phase: warps 0..TY-1, own pairs.
+    const bool col_warp = warp == TY + 1;
+    const bool e_active = !col_warp || lane <= TY;
+    const bool h_active = warp < TY;
+    const int er = warp < TY ? warp + 1 : (warp == TY ? 0 : lane);
+    const int eko = col_warp ? -2 : 2 * lane;  // pair start relative to k0
+    const bool own_row = warp < TY;
 
-    auto stage_ptr = [&](int st) { return smem + st * L::STAGE; };
+    auto stage_ptr = [&](int st) { return smem + st * p.stage_bytes; };
     auto sH = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + c * L::HBOXB); };
     auto sE = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + 3 * L::HBOXB + c * L::EBOXB); };
     auto sC = [&](int st, int c) {
         return reinterpret_cast<float *>(stage_ptr(st) + 3 * L::HBOXB + (3 + c) * L::EBOXB);
     };
-
-    int64_t issued[NS];  // plane last issued into each stage (meaningful on tid 0)
-    for (int s = 0; s < NS; s++) issued[s] = -1;
-    auto issue = [&](int64_t plane, int st) {
-        uint64_t *bar = &bars[st];
-        issued[st] = plane;
-        if (plane >= p.nx) {
-            // Past the last plane: H(nx) only feeds E components that are never
-            // updated at i = nx-1, so the stage content is irrelevant; complete
-            // the phase without a copy.
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-            return;
-        }
-        mbar_arrive_expect_tx(bar, L::TX);
-        const int kc = (int)(k0 - 4), jc = (int)(j0 - 1), xc = (int)plane;
-        for (int c = 0; c < 3; c++) tma_load_3d(sH(st, c), &maps.h[c], bar, kc, jc, xc);
-        for (int c = 0; c < 3; c++) tma_load_3d(sE(st, c), &maps.e[c], bar, kc, jc, xc);
-        for (int c = 0; c < 3; c++) tma_load_3d(sC(st, c), &maps.ce[c], bar, kc, jc, xc);
-    };
+    // z-psi boxes: 0,1 = E psi (exz, eyz) input; 2,3 = H psi (hxz, hyz); row r holds 2P values
+    auto sZ = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + L::STAGE + c * p.zbox); };
 
     if (tid == 0) {
         for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
@@ -215,238 +264,375 @@ k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
             prefetch_tmap(&maps.e[c]);
             prefetch_tmap(&maps.ce[c]);
         }
-        s_abort = 0;
-        // sources touching the extended region of this work item
-        int n = 0;
-        if (p.t >= 0 && p.t < p.namp) {
-            for (int s = 0; s < p.nsrc; s++) {
-                const int64_t si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
-                if (si >= i_start && si < x1 && sj >= j0 - 1 && sj < j0 + TY && sk >= k0 - 1 && sk < k0 + TZ) {
-                    if (n < MAX_LOCAL_SRC) {
-                        s_ls_i[n] = (int)si;
-                        s_ls_r[n] = (int)(sj - j0 + 1);
-                        s_ls_c[n] = (int)(sk - k0 + 1);
-                        s_ls_comp[n] = p.src_comp[s];
-                        s_ls_s[n] = s;
-                    }
-                    n++;
-                }
+        if (p.zpsi)
+            for (int c = 0; c < 2; c++) {
+                prefetch_tmap(&maps.zpe[c]);
+                prefetch_tmap(&maps.zph[c]);
             }
-            if (n > MAX_LOCAL_SRC) {  // the host rejects such layouts; never drop a source silently
-                atomicExch(p.status, FDTD_ERR_CAPACITY);
-                n = MAX_LOCAL_SRC;
+        s_abort = 0;
+    }
+    {
+        // stage the CPML coefficient tables (a few hundred floats) once per CTA
+        int off = 0;
+        for (int a = 0; a < 3; a++) {
+            const int n2 = 2 * p.P[a];
+            const float *src[6] = {p.tb_e[a], p.ta_e[a], p.tk_e[a], p.tb_h[a], p.ta_h[a], p.tk_h[a]};
+            for (int q = 0; q < 6; q++) {
+                for (int x = tid; x < n2; x += blockDim.x) tabs[off + x] = src[q][x];
+                off += n2;
             }
         }
-        s_nls = n;
     }
-    __syncthreads();
-    if (tid == 0)
-        for (int r = 0; r < NS; r++)
-            if (i_start + r <= last_plane) issue(i_start + r, r);
+    // offsets of each axis's six tables (b_e, a_e, km_e, b_h, a_h, km_h)
+    const int toff0 = 0, toff1 = 6 * 2 * p.P[0], toff2 = toff1 + 6 * 2 * p.P[1];
 
     const int64_t nx = p.nx, ny = p.ny, nz = p.nz;
     const int front0 = p.faces & 1, back0 = (p.faces >> 1) & 1;
     const int front1 = (p.faces >> 2) & 1, back1 = (p.faces >> 3) & 1;
     const int front2 = (p.faces >> 4) & 1, back2 = (p.faces >> 5) & 1;
-    const float *amp = p.src_amp;
+    const int P0 = p.P[0], P1 = p.P[1], P2 = p.P[2];
 
-    float prev_ey = 0.f, prev_ez = 0.f;
+    uint32_t g0 = 0;          // planes this CTA has issued before the current item
+    int64_t issued_hi = -1;   // highest plane index (relative) issued in the current item (tid 0)
+    int64_t q_abort = 0, i_start_abort = 0;
+    bool aborted = false;
+    const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
 
-    // E_new of one cell at smem row r (j = j0-1+r) and column c (k = k0-1+c).
-    // own: the cell belongs to this tile (psi_e_out is written only then).
-    auto compute_e = [&](int st, int st1, int64_t i, int r, int c, bool own, float &oex, float &oey, float &oez) {
-        const int64_t j = j0 - 1 + r, k = k0 - 1 + c;
-        const int hr = r, hc = c + 3;
-        const float *hx = sH(st, 0), *hy = sH(st, 1), *hz = sH(st, 2);
-        const float *hy1 = sH(st1, 1), *hz1 = sH(st1, 2);
-        const int hi = hr * HC + hc, ei = r * EC + hc;
-        const float hx0 = hx[hi], hy0 = hy[hi], hz0 = hz[hi];
-        float ex = sE(st, 0)[ei], ey = sE(st, 1)[ei], ez = sE(st, 2)[ei];
-        const float cex = sC(st, 0)[ei], cey = sC(st, 1)[ei], cez = sC(st, 2)[ei];
-        const bool in = j >= 0 && k >= 0 && j < ny && k < nz;
-        if (in) {
-            if (j < ny - 1 && k < nz - 1) ex = fadd(ex, fmul(cex, curl4(hz[hi + HC], hz0, hy[hi + 1], hy0)));
-            if (i < nx - 1 && k < nz - 1) ey = fadd(ey, fmul(cey, curl4(hx[hi + 1], hx0, hz1[hi], hz0)));
-            if (i < nx - 1 && j < ny - 1) ez = fadd(ez, fmul(cez, curl4(hy1[hi], hy0, hx[hi + HC], hx0)));
-            // CPML, x axis (plane-uniform branch)
-            const int sxs = slab_e(i, p.P[0], nx, front0, back0);
-            if (sxs >= 0) {
-                const float b = __ldg(&p.tb_e[0][sxs]), a = __ldg(&p.ta_e[0][sxs]), km = __ldg(&p.tk_e[0][sxs]);
-                const int64_t q = ((int64_t)sxs * ny + j) * nz + k;
-                if (k < nz - 1) {
-                    float psi = p.psi_e_in[0][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hz1[hi], hz0));
-                    if (own) p.psi_e_out[0][q] = psi;
-                    ey = fsub(ey, fmul(cey, tcorr));
+    for (int64_t item = blockIdx.x; item < nitems && !aborted; item += gridDim.x) {
+        const int64_t tzi = item % p.ntz, tyi = (item / p.ntz) % p.nty, xci = item / ((int64_t)p.ntz * p.nty);
+        const int64_t k0 = tzi * TZ, j0 = tyi * TY;
+        const int64_t x0 = xci * p.x_chunk;
+        const int64_t x1 = min(x0 + (int64_t)p.x_chunk, nx);
+        const int64_t i_start = x0 > 0 ? x0 - 1 : 0;
+        const int64_t nplanes = x1 - i_start + 1;  // planes i_start .. x1 (H(x1) feeds E(x1-1))
+        // Tile-uniform: no grid edge and no y/z CPML slab inside the tile's E/H region.
+        // tile's E (k0-1..k0+TZ-1) or H (k0..k0+TZ-1) columns touch a z slab
+        const bool ztile = P2 > 0 && ((front2 && k0 - 1 <= P2) || (back2 && k0 + TZ - 1 >= nz - P2 - 1));
+        const bool zstage = ztile && p.zpsi;
+        const bool yz_plain = j0 >= 1 && j0 + TY <= ny - 1 && k0 >= 1 && k0 + TZ <= nz - 1 &&
+                              (P1 == 0 || ((j0 - 1 > P1 || !front1) && (j0 + TY - 1 < ny - P1 - 1 || !back1))) &&
+                              (P2 == 0 || ((k0 - 1 > P2 || !front2) && (k0 + TZ - 1 < nz - P2 - 1 || !back2)));
+
+        // ---- per-item, per-thread cell description (pair at row j, columns k, k+1) ----
+        const int64_t jj = j0 - 1 + er, kk = k0 + eko;
+        const bool row_in = jj >= 0 && jj < ny;
+        const bool in0 = row_in && kk >= 0 && kk < nz, in1 = row_in && kk + 1 >= 0 && kk + 1 < nz;
+        const bool j_lt = jj < ny - 1, j_gt = jj > 0;
+        const bool k0_lt = kk < nz - 1, k1_lt = kk + 1 < nz - 1, k0_gt = kk > 0, k1_gt = kk + 1 > 0;
+        const int sye = row_in ? slab_e(jj, P1, ny, front1, back1) : -1;
+        const int syh = row_in ? slab_h(jj, P1, ny, front1, back1) : -1;
+        const int sze0 = in0 ? slab_e(kk, P2, nz, front2, back2) : -1;
+        const int sze1 = in1 ? slab_e(kk + 1, P2, nz, front2, back2) : -1;
+        const int szh0 = in0 ? slab_h(kk, P2, nz, front2, back2) : -1;
+        const int szh1 = in1 ? slab_h(kk + 1, P2, nz, front2, back2) : -1;
+
+        auto issue = [&](int64_t q) {
+            const int64_t plane = i_start + q;
+            const int st = (int)((g0 + q) % NS);
+            uint64_t *bar = &bars[st];
+            issued_hi = q;
+            if (plane >= nx) {
+                // Past the last plane: H(nx) only feeds E components that are
+                // never updated at i = nx-1; complete the phase without a copy.
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+                return;
+            }
+            mbar_arrive_expect_tx(bar, L::TX + (zstage ? p.tx_z : 0u));
+            const int kc = (int)(k0 - 4), jc = (int)(j0 - 1), xc = (int)plane;
+            for (int c = 0; c < 3; c++) tma_load_3d(sH(st, c), &maps.h[c], bar, kc, jc, xc);
+            for (int c = 0; c < 3; c++) tma_load_3d(sE(st, c), &maps.e[c], bar, kc, jc, xc);
+            for (int c = 0; c < 3; c++) tma_load_3d(sC(st, c), &maps.ce[c], bar, kc, jc, xc);
+            if (zstage) {
+                tma_load_3d(sZ(st, 0), &maps.zpe[0], bar, 0, jc, xc);
+                tma_load_3d(sZ(st, 1), &maps.zpe[1], bar, 0, jc, xc);
+                tma_load_3d(sZ(st, 2), &maps.zph[0], bar, 0, jc, xc);
+                tma_load_3d(sZ(st, 3), &maps.zph[1], bar, 0, jc, xc);
+            }
+        };
+
+        if (tid == 0) {
+            // sources inside the extended region of this work item
+            int n = 0;
+            if (p.t >= 0 && p.t < p.namp) {
+                for (int s = 0; s < p.nsrc; s++) {
+                    const int64_t si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
+                    if (si >= i_start && si < x1 && sj >= j0 - 1 && sj < j0 + TY && sk >= k0 - 1 && sk < k0 + TZ) {
+                        if (n < MAX_LOCAL_SRC) {
+                            s_ls_i[n] = (int)si;
+                            s_ls_j[n] = (int)sj;
+                            s_ls_k[n] = (int)sk;
+                            s_ls_comp[n] = p.src_comp[s];
+                            s_ls_s[n] = s;
+                        }
+                        n++;
+                    }
                 }
-                if (j < ny - 1) {
-                    float psi = p.psi_e_in[1][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hy1[hi], hy0));
-                    if (own) p.psi_e_out[1][q] = psi;
-                    ez = fadd(ez, fmul(cez, tcorr));
+                if (n > MAX_LOCAL_SRC) {  // the host rejects such layouts; never drop a source silently
+                    atomicExch(p.status, FDTD_ERR_CAPACITY);
+                    n = MAX_LOCAL_SRC;
                 }
             }
-            const int sys = slab_e(j, p.P[1], ny, front1, back1);
-            if (sys >= 0) {
-                const float b = __ldg(&p.tb_e[1][sys]), a = __ldg(&p.ta_e[1][sys]), km = __ldg(&p.tk_e[1][sys]);
-                const int64_t q = (i * 2 * p.P[1] + sys) * nz + k;
-                if (i < nx - 1) {
-                    float psi = p.psi_e_in[2][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hx[hi + HC], hx0));
-                    if (own) p.psi_e_out[2][q] = psi;
-                    ez = fsub(ez, fmul(cez, tcorr));
-                }
-                if (k < nz - 1) {
-                    float psi = p.psi_e_in[3][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hz[hi + HC], hz0));
-                    if (own) p.psi_e_out[3][q] = psi;
-                    ex = fadd(ex, fmul(cex, tcorr));
-                }
+            s_nls = n;
+        }
+        __syncthreads();  // previous item finished by every thread; source list ready
+        if (tid == 0)
+            for (int64_t q = 0; q < NS && q < nplanes; q++) issue(q);
+        const int nls = s_nls;
+        const bool tile_plain = yz_plain && nls == 0;
+
+        float2 prev_ey = make_float2(0.f, 0.f), prev_ez = make_float2(0.f, 0.f);
+        float2 oex = prev_ey, oey = prev_ey, oez = prev_ey;  // own E_new pair
+        for (int64_t q = 0; q + 1 < nplanes; q++) {
+            const int64_t i = i_start + q;
+            const uint32_t G = g0 + (uint32_t)q;
+            const int st = (int)(G % NS), st1 = (int)((G + 1) % NS);
+            const uint32_t par = (G / NS) & 1, par1 = ((G + 1) / NS) & 1;
+            // One thread waits for the copies; the barrier then releases the CTA
+            // (the mbarrier acquire by tid 0 plus bar.sync order the TMA writes
+            // before every thread's reads).
+            if (tid == 0 &&
+                (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status)))
+                s_abort = 1;
+            __syncthreads();  // (A) planes q, q+1 visible; iteration q-1 finished everywhere
+            if (s_abort) {
+                aborted = true;
+                q_abort = q;
+                i_start_abort = i_start;
+                break;
             }
-            const int szs = slab_e(k, p.P[2], nz, front2, back2);
-            if (szs >= 0) {
-                const float b = __ldg(&p.tb_e[2][szs]), a = __ldg(&p.ta_e[2][szs]), km = __ldg(&p.tk_e[2][szs]);
-                const int64_t q = (i * ny + j) * 2 * p.P[2] + szs;
-                if (j < ny - 1) {
-                    float psi = p.psi_e_in[4][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hy[hi + 1], hy0));
-                    if (own) p.psi_e_out[4][q] = psi;
-                    ex = fsub(ex, fmul(cex, tcorr));
+            if (tid == 0 && q >= 1 && q - 1 + NS < nplanes) issue(q - 1 + NS);  // reuse plane q-1's stage
+
+            // plane-uniform CPML (x) and masks
+            const int sxe = slab_e(i, P0, nx, front0, back0), sxh = slab_h(i, P0, nx, front0, back0);
+            const bool i_lt = i < nx - 1, i_gt = i > 0;
+            const bool e_plain = tile_plain && i_lt && sxe < 0;
+            const bool h_plain = tile_plain && i_gt && sxh < 0;
+
+            // ---- E phase ----
+            if (e_active) {
+                const int hc = 4 + eko;
+                const float *HX = sH(st, 0) + er * HC + hc, *HY = sH(st, 1) + er * HC + hc,
+                            *HZ = sH(st, 2) + er * HC + hc;
+                const float2 hx = ld2(HX), hy = ld2(HY), hz = ld2(HZ);
+                const float2 hxj1 = ld2(HX + HC), hzj1 = ld2(HZ + HC);
+                const float2 hxk1 = make_float2(HX[1], HX[2]), hyk1 = make_float2(HY[1], HY[2]);
+                const float2 hy1 = ld2(sH(st1, 1) + er * HC + hc), hz1 = ld2(sH(st1, 2) + er * HC + hc);
+                const int ei = er * EC + hc;
+                const float2 ex0 = ld2(sE(st, 0) + ei), ey0 = ld2(sE(st, 1) + ei), ez0 = ld2(sE(st, 2) + ei);
+                const float2 cex = ld2(sC(st, 0) + ei), cey = ld2(sC(st, 1) + ei), cez = ld2(sC(st, 2) + ei);
+                float2 ex = add2(ex0, mul2(cex, curl4x2(hzj1, hz, hyk1, hy)));
+                float2 ey = add2(ey0, mul2(cey, curl4x2(hxk1, hx, hz1, hz)));
+                float2 ez = add2(ez0, mul2(cez, curl4x2(hy1, hy, hxj1, hx)));
+                if (!e_plain) {
+                    // component masks (cells the reference does not update keep their value)
+                    if (!(j_lt && k0_lt)) ex.x = ex0.x;
+                    if (!(j_lt && k1_lt)) ex.y = ex0.y;
+                    if (!(i_lt && k0_lt)) ey.x = ey0.x;
+                    if (!(i_lt && k1_lt)) ey.y = ey0.y;
+                    if (!(i_lt && j_lt)) {
+                        ez.x = ez0.x;
+                        ez.y = ez0.y;
+                    }
+                    const bool own = own_row && i >= x0;
+                    if (sxe >= 0) {  // x slab: ey -= cey (..dHz/dx..), ez += cez (..dHy/dx..)
+                        const Coef c = tab_coef(tabs, toff0, 2 * P0, 0, sxe);
+                        const int64_t qb = ((int64_t)sxe * ny + jj) * nz + kk;
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (!(e ? in1 : in0)) continue;
+                            if (e ? k1_lt : k0_lt) {
+                                float psi = p.psi_e_in[0][qb + e];
+                                const float tc = corr(psi, c, fsub(get(hz1, e), get(hz, e)));
+                                if (own) p.psi_e_out[0][qb + e] = psi;
+                                set(ey, e, fsub(get(ey, e), fmul(get(cey, e), tc)));
+                            }
+                            if (j_lt) {
+                                float psi = p.psi_e_in[1][qb + e];
+                                const float tc = corr(psi, c, fsub(get(hy1, e), get(hy, e)));
+                                if (own) p.psi_e_out[1][qb + e] = psi;
+                                set(ez, e, fadd(get(ez, e), fmul(get(cez, e), tc)));
+                            }
+                        }
+                    }
+                    if (sye >= 0) {  // y slab: ez -= cez (..dHx/dy..), ex += cex (..dHz/dy..)
+                        const Coef cye = tab_coef(tabs, toff1, 2 * P1, 0, sye);
+                        const int64_t qb = (i * 2 * P1 + sye) * nz + kk;
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (!(e ? in1 : in0)) continue;
+                            if (i_lt) {
+                                float psi = p.psi_e_in[2][qb + e];
+                                const float tc = corr(psi, cye, fsub(get(hxj1, e), get(hx, e)));
+                                if (own) p.psi_e_out[2][qb + e] = psi;
+                                set(ez, e, fsub(get(ez, e), fmul(get(cez, e), tc)));
+                            }
+                            if (e ? k1_lt : k0_lt) {
+                                float psi = p.psi_e_in[3][qb + e];
+                                const float tc = corr(psi, cye, fsub(get(hzj1, e), get(hz, e)));
+                                if (own) p.psi_e_out[3][qb + e] = psi;
+                                set(ex, e, fadd(get(ex, e), fmul(get(cex, e), tc)));
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {  // z slab: ex -= cex (..dHy/dz..), ey += cey (..dHx/dz..)
+                        const int sz = e ? sze1 : sze0;
+                        if (sz < 0) continue;
+                        const Coef c = tab_coef(tabs, toff2, 2 * P2, 0, sz);
+                        const int64_t qz = (i * ny + jj) * 2 * P2 + sz;
+                        const int zs = er * 2 * P2 + sz;  // position in the staged z-psi box
+                        if (j_lt) {
+                            float psi = zstage ? sZ(st, 0)[zs] : p.psi_e_in[4][qz];
+                            const float tc = corr(psi, c, fsub(get(hyk1, e), get(hy, e)));
+                            if (own) p.psi_e_out[4][qz] = psi;
+                            set(ex, e, fsub(get(ex, e), fmul(get(cex, e), tc)));
+                        }
+                        if (i_lt) {
+                            float psi = zstage ? sZ(st, 1)[zs] : p.psi_e_in[5][qz];
+                            const float tc = corr(psi, c, fsub(get(hxk1, e), get(hx, e)));
+                            if (own) p.psi_e_out[5][qz] = psi;
+                            set(ey, e, fadd(get(ey, e), fmul(get(cey, e), tc)));
+                        }
+                    }
+                    for (int s = 0; s < nls; s++) {  // soft sources, list order
+                        if (s_ls_i[s] != i || s_ls_j[s] != jj) continue;
+                        const int64_t sk = s_ls_k[s];
+                        if (sk != kk && sk != kk + 1) continue;
+                        const int e = (int)(sk - kk);
+                        const float v = p.src_amp[(int64_t)s_ls_s[s] * p.namp + p.t];
+                        if (s_ls_comp[s] == 0) set(ex, e, fadd(get(ex, e), v));
+                        else if (s_ls_comp[s] == 1) set(ey, e, fadd(get(ey, e), v));
+                        else set(ez, e, fadd(get(ez, e), v));
+                    }
                 }
-                if (i < nx - 1) {
-                    float psi = p.psi_e_in[5][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(hx[hi + 1], hx0));
-                    if (own) p.psi_e_out[5][q] = psi;
-                    ey = fadd(ey, fmul(cey, tcorr));
-                }
+                const int o = er * NCW + 2 + eko;
+                st2(Nx + o, ex);
+                st2(Ny + o, ey);
+                st2(Nz + o, ez);
+                oex = ex;
+                oey = ey;
+                oez = ez;
             }
-            for (int q = 0; q < s_nls; q++) {
-                if (s_ls_i[q] == i && s_ls_r[q] == r && s_ls_c[q] == c) {
-                    const float v = amp[(int64_t)s_ls_s[q] * p.namp + p.t];
-                    if (s_ls_comp[q] == 0) ex = fadd(ex, v);
-                    else if (s_ls_comp[q] == 1) ey = fadd(ey, v);
-                    else ez = fadd(ez, v);
+            __syncthreads();  // (B) E_new of plane i visible
+
+            // ---- H phase: own rows ----
+            if (h_active) {
+                if (i >= x0) {
+                    const int o = er * NCW + 2 + eko;
+                    const float2 ez_jm = ld2(Nz + o - NCW), ex_jm = ld2(Nx + o - NCW);
+                    const float2 ey_km = make_float2(Ny[o - 1], oey.x), ex_km = make_float2(Nx[o - 1], oex.x);
+                    const int hi = er * HC + 4 + eko;
+                    const float2 hx0 = ld2(sH(st, 0) + hi), hy0 = ld2(sH(st, 1) + hi), hz0 = ld2(sH(st, 2) + hi);
+                    const float2 half = make_float2(0.5f, 0.5f);
+                    float2 hx = sub2(hx0, mul2(half, curl4x2(oez, ez_jm, oey, ey_km)));
+                    float2 hy = sub2(hy0, mul2(half, curl4x2(oex, ex_km, oez, prev_ez)));
+                    float2 hz = sub2(hz0, mul2(half, curl4x2(oey, prev_ey, oex, ex_jm)));
+                    if (!h_plain) {
+                        if (!(j_gt && k0_gt)) hx.x = hx0.x;
+                        if (!(j_gt && k1_gt)) hx.y = hx0.y;
+                        if (!(i_gt && k0_gt)) hy.x = hy0.x;
+                        if (!(i_gt && k1_gt)) hy.y = hy0.y;
+                        if (!(i_gt && j_gt)) {
+                            hz.x = hz0.x;
+                            hz.y = hz0.y;
+                        }
+                        if (sxh >= 0) {  // x slab: hy += (..dEz/dx..), hz -= (..dEy/dx..)
+                            const Coef c = tab_coef(tabs, toff0, 2 * P0, 1, sxh);
+                            const int64_t qb = ((int64_t)sxh * ny + jj) * nz + kk;
+#pragma unroll
+                            for (int e = 0; e < 2; e++) {
+                                if (!(e ? in1 : in0)) continue;
+                                if (e ? k1_gt : k0_gt) {
+                                    float psi = p.psi_h[0][qb + e];
+                                    const float tc = corr(psi, c, fsub(get(oez, e), get(prev_ez, e)));
+                                    p.psi_h[0][qb + e] = psi;
+                                    set(hy, e, fadd(get(hy, e), fmul(0.5f, tc)));
+                                }
+                                if (j_gt) {
+                                    float psi = p.psi_h[1][qb + e];
+                                    const float tc = corr(psi, c, fsub(get(oey, e), get(prev_ey, e)));
+                                    p.psi_h[1][qb + e] = psi;
+                                    set(hz, e, fsub(get(hz, e), fmul(0.5f, tc)));
+                                }
+                            }
+                        }
+                        if (syh >= 0) {  // y slab: hz += (..dEx/dy..), hx -= (..dEz/dy..)
+                            const Coef cyh = tab_coef(tabs, toff1, 2 * P1, 1, syh);
+                            const int64_t qb = (i * 2 * P1 + syh) * nz + kk;
+#pragma unroll
+                            for (int e = 0; e < 2; e++) {
+                                if (!(e ? in1 : in0)) continue;
+                                if (i_gt) {
+                                    float psi = p.psi_h[2][qb + e];
+                                    const float tc = corr(psi, cyh, fsub(get(oex, e), get(ex_jm, e)));
+                                    p.psi_h[2][qb + e] = psi;
+                                    set(hz, e, fadd(get(hz, e), fmul(0.5f, tc)));
+                                }
+                                if (e ? k1_gt : k0_gt) {
+                                    float psi = p.psi_h[3][qb + e];
+                                    const float tc = corr(psi, cyh, fsub(get(oez, e), get(ez_jm, e)));
+                                    p.psi_h[3][qb + e] = psi;
+                                    set(hx, e, fsub(get(hx, e), fmul(0.5f, tc)));
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {  // z slab: hx += (..dEy/dz..), hy -= (..dEx/dz..)
+                            const int sz = e ? szh1 : szh0;
+                            if (sz < 0) continue;
+                            const Coef c = tab_coef(tabs, toff2, 2 * P2, 1, sz);
+                            const int64_t qz = (i * ny + jj) * 2 * P2 + sz;
+                            const int zs = er * 2 * P2 + sz;
+                            if (j_gt) {
+                                float psi = zstage ? sZ(st, 2)[zs] : p.psi_h[4][qz];
+                                const float tc = corr(psi, c, fsub(get(oey, e), get(ey_km, e)));
+                                p.psi_h[4][qz] = psi;
+                                set(hx, e, fadd(get(hx, e), fmul(0.5f, tc)));
+                            }
+                            if (i_gt) {
+                                float psi = zstage ? sZ(st, 3)[zs] : p.psi_h[5][qz];
+                                const float tc = corr(psi, c, fsub(get(oex, e), get(ex_km, e)));
+                                p.psi_h[5][qz] = psi;
+                                set(hy, e, fsub(get(hy, e), fmul(0.5f, tc)));
+                            }
+                        }
+                    }
+                    const int64_t gi = i * p.sx + jj * p.sy + kk;
+                    if (in1) {
+                        st2(p.out[0] + gi, oex);
+                        st2(p.out[1] + gi, oey);
+                        st2(p.out[2] + gi, oez);
+                        st2(p.out[3] + gi, hx);
+                        st2(p.out[4] + gi, hy);
+                        st2(p.out[5] + gi, hz);
+                    } else if (in0) {
+                        p.out[0][gi] = oex.x;
+                        p.out[1][gi] = oey.x;
+                        p.out[2][gi] = oez.x;
+                        p.out[3][gi] = hx.x;
+                        p.out[4][gi] = hy.x;
+                        p.out[5][gi] = hz.x;
+                    }
                 }
+                prev_ey = oey;
+                prev_ez = oez;
             }
         }
-        oex = ex;
-        oey = ey;
-        oez = ez;
-    };
-
-    constexpr int NRC = L::NR * L::NC;
-    for (int64_t i = i_start; i < x1; i++) {
-        const int64_t rel = i - i_start;
-        const int st = (int)(rel % NS), st1 = (int)((rel + 1) % NS);
-        const uint32_t par = (uint32_t)((rel / NS) & 1), par1 = (uint32_t)(((rel + 1) / NS) & 1);
-        if (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status))
-            s_abort = 1;
-        __syncthreads();
-        if (s_abort) break;
-
-        // ---- E_new on the tile (own cells) and the j0-1 / k0-1 halo ----
-        float ex_o, ey_o, ez_o;
-        compute_e(st, st1, i, w + 1, lane + 1, i >= x0, ex_o, ey_o, ez_o);
-        {
-            const int o = (w + 1) * L::NC + lane + 1;
-            enew[o] = ex_o;
-            enew[NRC + o] = ey_o;
-            enew[2 * NRC + o] = ez_o;
+        if (!aborted) {
+            g0 += (uint32_t)nplanes;
+            issued_hi = -1;
         }
-        for (int x = tid; x < TZ + TY + 1; x += TY * 32) {
-            const int r = x < TZ ? 0 : x - TZ, c = x < TZ ? x + 1 : 0;
-            float a, b, d;
-            compute_e(st, st1, i, r, c, false, a, b, d);
-            const int o = r * L::NC + c;
-            enew[o] = a;
-            enew[NRC + o] = b;
-            enew[2 * NRC + o] = d;
-        }
-        __syncthreads();
-
-        const int64_t j = j0 + w, k = k0 + lane;
-        if (i >= x0 && j < ny && k < nz) {
-            const int o = (w + 1) * L::NC + lane + 1;
-            const float *Ex = enew, *Ey = enew + NRC, *Ez = enew + 2 * NRC;
-            const int hi = (w + 1) * HC + lane + 4;
-            float hx = sH(st, 0)[hi], hy = sH(st, 1)[hi], hz = sH(st, 2)[hi];
-            if (j > 0 && k > 0) hx = fsub(hx, fmul(0.5f, curl4(ez_o, Ez[o - L::NC], ey_o, Ey[o - 1])));
-            if (i > 0 && k > 0) hy = fsub(hy, fmul(0.5f, curl4(ex_o, Ex[o - 1], ez_o, prev_ez)));
-            if (i > 0 && j > 0) hz = fsub(hz, fmul(0.5f, curl4(ey_o, prev_ey, ex_o, Ex[o - L::NC])));
-            const int sxs = slab_h(i, p.P[0], nx, front0, back0);
-            if (sxs >= 0) {
-                const float b = __ldg(&p.tb_h[0][sxs]), a = __ldg(&p.ta_h[0][sxs]), km = __ldg(&p.tk_h[0][sxs]);
-                const int64_t q = ((int64_t)sxs * ny + j) * nz + k;
-                if (k > 0) {
-                    float psi = p.psi_h[0][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ez_o, prev_ez));
-                    p.psi_h[0][q] = psi;
-                    hy = fadd(hy, fmul(0.5f, tcorr));
-                }
-                if (j > 0) {
-                    float psi = p.psi_h[1][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ey_o, prev_ey));
-                    p.psi_h[1][q] = psi;
-                    hz = fsub(hz, fmul(0.5f, tcorr));
-                }
-            }
-            const int sys = slab_h(j, p.P[1], ny, front1, back1);
-            if (sys >= 0) {
-                const float b = __ldg(&p.tb_h[1][sys]), a = __ldg(&p.ta_h[1][sys]), km = __ldg(&p.tk_h[1][sys]);
-                const int64_t q = (i * 2 * p.P[1] + sys) * nz + k;
-                if (i > 0) {
-                    float psi = p.psi_h[2][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ex_o, Ex[o - L::NC]));
-                    p.psi_h[2][q] = psi;
-                    hz = fadd(hz, fmul(0.5f, tcorr));
-                }
-                if (k > 0) {
-                    float psi = p.psi_h[3][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ez_o, Ez[o - L::NC]));
-                    p.psi_h[3][q] = psi;
-                    hx = fsub(hx, fmul(0.5f, tcorr));
-                }
-            }
-            const int szs = slab_h(k, p.P[2], nz, front2, back2);
-            if (szs >= 0) {
-                const float b = __ldg(&p.tb_h[2][szs]), a = __ldg(&p.ta_h[2][szs]), km = __ldg(&p.tk_h[2][szs]);
-                const int64_t q = (i * ny + j) * 2 * p.P[2] + szs;
-                if (j > 0) {
-                    float psi = p.psi_h[4][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ey_o, Ey[o - 1]));
-                    p.psi_h[4][q] = psi;
-                    hx = fadd(hx, fmul(0.5f, tcorr));
-                }
-                if (i > 0) {
-                    float psi = p.psi_h[5][q];
-                    const float tcorr = cpml_corr(psi, b, a, km, fsub(ex_o, Ex[o - 1]));
-                    p.psi_h[5][q] = psi;
-                    hy = fsub(hy, fmul(0.5f, tcorr));
-                }
-            }
-            const int64_t g = i * p.sx + j * p.sy + k;
-            p.out[0][g] = ex_o;
-            p.out[1][g] = ey_o;
-            p.out[2][g] = ez_o;
-            p.out[3][g] = hx;
-            p.out[4][g] = hy;
-            p.out[5][g] = hz;
-        }
-        prev_ey = ey_o;
-        prev_ez = ez_o;
-        __syncthreads();  // stage st and enew are free again
-        if (tid == 0 && i + NS <= last_plane) issue(i + NS, st);
     }
 
-    if (s_abort) {
+    if (aborted) {
         if (tid == 0) {
             atomicExch(p.status, FDTD_ERR_TIMEOUT);
             // Let the copies still in flight land before the CTA's shared
             // memory is released (each wait bounded).
-            for (int s = 0; s < NS; s++) {
-                if (issued[s] < 0 || issued[s] >= p.nx) continue;
-                const int64_t rel = issued[s] - i_start;
-                mbar_wait_bounded(&bars[s], (uint32_t)((rel / NS) & 1), nullptr);
+            for (int64_t q = q_abort; q <= issued_hi; q++) {
+                if (i_start_abort + q >= nx) continue;
+                const uint32_t G = g0 + (uint32_t)q;
+                mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr);
             }
         }
         __syncthreads();
@@ -480,12 +666,35 @@ static EncodeTiledFn get_encode_fn() {
     return fn;
 }
 
+typedef void (*FusedKernel)(const TMaps, const Params);
+
+struct KernelEntry {
+    int ty, ns, threads, stage, enew;
+    FusedKernel fn;
+};
+
+template <int TY, int NS>
+static KernelEntry entry() {
+    return KernelEntry{TY, NS, Layout<TY, NS>::THREADS, Layout<TY, NS>::STAGE, Layout<TY, NS>::ENEW,
+                       k_yee_fused<TY, NS>};
+}
+
+// Tile heights and pipeline depths compiled in (the autotuner picks among them).
+static const KernelEntry *find_kernel(int ty, int ns) {
+    static const KernelEntry table[] = {entry<4, 4>(), entry<4, 6>(), entry<8, 3>(), entry<8, 4>(),
+                                        entry<16, 3>()};
+    for (const KernelEntry &e : table)
+        if (e.ty == ty && e.ns == ns) return &e;
+    return nullptr;
+}
+
 struct fdtd_yee_plan {
     Grid g;
-    int ty;
-    int x_chunk;
-    int nitems;
+    const KernelEntry *k;
     int smem;
+    int x_chunk;
+    int64_t nitems;
+    int nblocks;
     int cur;
     TMaps maps[2];
     Params base;
@@ -493,32 +702,23 @@ struct fdtd_yee_plan {
     float *psi_e[2][6];
 };
 
-static int encode_map(EncodeTiledFn enc, CUtensorMap *m, const float *ptr, const Grid &g, int box_z, int box_y) {
-    cuuint64_t dims[3] = {(cuuint64_t)g.nz, (cuuint64_t)g.ny, (cuuint64_t)g.nx};
-    cuuint64_t strides[2] = {(cuuint64_t)g.sy * 4, (cuuint64_t)g.sx * 4};
-    cuuint32_t box[3] = {(cuuint32_t)box_z, (cuuint32_t)box_y, 1};
+// 3-D FP32 tensor map: dims (n0 fastest, n1, n2), element strides s1, s2,
+// box (b0, b1, 1); out-of-range elements read as zero.
+static int encode_map3(EncodeTiledFn enc, CUtensorMap *m, const float *ptr, int64_t n0, int64_t n1, int64_t n2,
+                       int64_t s1, int64_t s2, int b0, int b1, CUtensorMapL2promotion promo) {
+    cuuint64_t dims[3] = {(cuuint64_t)n0, (cuuint64_t)n1, (cuuint64_t)n2};
+    cuuint64_t strides[2] = {(cuuint64_t)s1 * 4, (cuuint64_t)s2 * 4};
+    cuuint32_t box[3] = {(cuuint32_t)b0, (cuuint32_t)b1, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(ptr), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, promo,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? FDTD_OK : FDTD_ERR_CUDA;
 }
 
-template <int TY>
-static int configure(fdtd_yee_plan *pl) {
-    pl->smem = Layout<TY>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_yee_fused<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, pl->smem);
-    if (e != cudaSuccess) {
-        set_cuda_error(e);
-        return FDTD_ERR_CUDA;
-    }
-    return FDTD_OK;
-}
-
-template <int TY>
-static int launch(const fdtd_yee_plan *pl, const TMaps &m, const Params &p, cudaStream_t st) {
-    k_yee_fused<TY><<<pl->nitems, TY * 32, pl->smem, st>>>(m, p);
-    return check_launch();
+static int encode_map(EncodeTiledFn enc, CUtensorMap *m, const float *ptr, const Grid &g, int box_z, int box_y,
+                      CUtensorMapL2promotion promo) {
+    return encode_map3(enc, m, ptr, g.nz, g.ny, g.nx, g.sy, g.sx, box_z, box_y, promo);
 }
 
 static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
@@ -544,14 +744,16 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         if (!s->ce[q]) return FDTD_ERR_ARG;
         if (!aligned16(s->ce[q])) return FDTD_ERR_ALIGN;
     }
-    int ty = tile && tile->tile_y ? tile->tile_y : 8;
-    if (ty != 4 && ty != 8 && ty != 16) return FDTD_ERR_UNSUPPORTED;
-    int xch = tile && tile->x_chunk ? tile->x_chunk : 64;
+    const int ty = tile && tile->tile_y ? tile->tile_y : 8;
+    const int ns = tile && tile->stages ? tile->stages : 3;
+    const KernelEntry *ke = find_kernel(ty, ns);
+    if (!ke) return FDTD_ERR_UNSUPPORTED;
+    const int xch = tile && tile->x_chunk ? tile->x_chunk : 128;
     if (xch < 1) return FDTD_ERR_ARG;
 
     fdtd_yee_plan *pl = new fdtd_yee_plan();
     pl->g = g;
-    pl->ty = ty;
+    pl->k = ke;
     pl->x_chunk = (int)std::min<int64_t>(xch, g.nx);
     pl->cur = cur;
     Params &p = pl->base;
@@ -559,11 +761,9 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     p.nx = g.nx; p.ny = g.ny; p.nz = g.nz; p.sx = g.sx; p.sy = g.sy;
     p.ntz = (int)((g.nz + TZ - 1) / TZ);
     p.nty = (int)((g.ny + ty - 1) / ty);
+    p.nxc = (int)((g.nx + pl->x_chunk - 1) / pl->x_chunk);
     p.x_chunk = pl->x_chunk;
-    const int64_t nxc = (g.nx + pl->x_chunk - 1) / pl->x_chunk;
-    const int64_t nitems = (int64_t)p.ntz * p.nty * nxc;
-    if (nitems > 0x7fffffff) { delete pl; return FDTD_ERR_SHAPE; }
-    pl->nitems = (int)nitems;
+    pl->nitems = (int64_t)p.ntz * p.nty * p.nxc;
     p.status = status_dev;
 
     const bool pml = c && (c->npml[0] > 0 || c->npml[1] > 0 || c->npml[2] > 0);
@@ -589,25 +789,25 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     if (src && src->nsrc > 0) {
         if (!all_nonnull(src->ijk, src->comp, src->amp) || src->namp < 0) { delete pl; return FDTD_ERR_ARG; }
         p.nsrc = src->nsrc; p.src_ijk = src->ijk; p.src_comp = src->comp; p.src_amp = src->amp; p.namp = src->namp;
-        // capacity: sources per work item's extended region
+        // capacity: sources per work item's extended region (checked on the host)
         int32_t *hijk = new int32_t[3 * (size_t)src->nsrc];
         if (cudaMemcpy(hijk, src->ijk, sizeof(int32_t) * 3 * src->nsrc, cudaMemcpyDeviceToHost) != cudaSuccess) {
             delete[] hijk; delete pl; return FDTD_ERR_CUDA;
         }
         for (int a = 0; a < src->nsrc; a++) {
+            if (hijk[3 * a] < 0 || hijk[3 * a] >= g.nx || hijk[3 * a + 1] < 0 || hijk[3 * a + 1] >= g.ny ||
+                hijk[3 * a + 2] < 0 || hijk[3 * a + 2] >= g.nz) {
+                delete[] hijk; delete pl; return FDTD_ERR_ARG;
+            }
             int cnt = 0;
             for (int b = 0; b < src->nsrc; b++) {
-                // conservative: same tile neighbourhood (one tile + halo in y/z, one chunk + 1 in x)
+                // conservative: neighbouring tile in y/z, neighbouring chunk in x
                 if (std::abs(hijk[3 * a + 1] / ty - hijk[3 * b + 1] / ty) <= 1 &&
                     std::abs(hijk[3 * a + 2] / TZ - hijk[3 * b + 2] / TZ) <= 1 &&
                     std::abs(hijk[3 * a] / pl->x_chunk - hijk[3 * b] / pl->x_chunk) <= 1)
                     cnt++;
             }
             if (cnt > MAX_LOCAL_SRC) { delete[] hijk; delete pl; return FDTD_ERR_CAPACITY; }
-            if (hijk[3 * a] < 0 || hijk[3 * a] >= g.nx || hijk[3 * a + 1] < 0 || hijk[3 * a + 1] >= g.ny ||
-                hijk[3 * a + 2] < 0 || hijk[3 * a + 2] >= g.nz) {
-                delete[] hijk; delete pl; return FDTD_ERR_ARG;
-            }
         }
         delete[] hijk;
     }
@@ -619,16 +819,63 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
             pl->f[b][q] = s->f[b][q];
             pl->psi_e[b][q] = s->psi_e[b][q];
         }
+        const int pm = tile ? tile->l2_promotion : 0;
+        const CUtensorMapL2promotion promo = pm == 1   ? CU_TENSOR_MAP_L2_PROMOTION_NONE
+                                             : pm == 2 ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
+                                             : pm == 3 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B
+                                                       : CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
         int st = FDTD_OK;
         for (int q = 0; q < 3 && st == FDTD_OK; q++) {
-            st = encode_map(enc, &pl->maps[b].h[q], s->f[b][3 + q], g, HC, ty + 2);
-            if (st == FDTD_OK) st = encode_map(enc, &pl->maps[b].e[q], s->f[b][q], g, EC, ty + 1);
-            if (st == FDTD_OK) st = encode_map(enc, &pl->maps[b].ce[q], s->ce[q], g, EC, ty + 1);
+            st = encode_map(enc, &pl->maps[b].h[q], s->f[b][3 + q], g, HC, ty + 2, promo);
+            if (st == FDTD_OK) st = encode_map(enc, &pl->maps[b].e[q], s->f[b][q], g, EC, ty + 1, promo);
+            if (st == FDTD_OK) st = encode_map(enc, &pl->maps[b].ce[q], s->ce[q], g, EC, ty + 1, promo);
         }
         if (st != FDTD_OK) { delete pl; return st; }
     }
-    int st = ty == 4 ? configure<4>(pl) : ty == 8 ? configure<8>(pl) : configure<16>(pl);
-    if (st != FDTD_OK) { delete pl; return st; }
+    // z-slab psi staged by TMA: needs rows of 2P floats that are 16-byte multiples
+    const int P2 = p.P[2];
+    const bool zpsi = P2 > 0 && (2 * P2 * 4) % 16 == 0 && 2 * P2 <= 256 && g.ny <= 0x7fffffff;
+    int zbox = 0;
+    if (zpsi) {
+        const int box_bytes = (ty + 1) * 2 * P2 * 4;
+        zbox = (box_bytes + 127) / 128 * 128;
+        p.tx_z = 4u * (uint32_t)box_bytes;
+        int st = FDTD_OK;
+        for (int b = 0; b < 2 && st == FDTD_OK; b++)
+            for (int q = 0; q < 2 && st == FDTD_OK; q++) {
+                st = encode_map3(enc, &pl->maps[b].zpe[q], s->psi_e[b][4 + q], 2 * P2, g.ny, g.nx, 2 * P2,
+                                 g.ny * 2 * P2, 2 * P2, ty + 1, CU_TENSOR_MAP_L2_PROMOTION_NONE);
+                if (st == FDTD_OK)
+                    st = encode_map3(enc, &pl->maps[b].zph[q], s->psi_h[4 + q], 2 * P2, g.ny, g.nx, 2 * P2,
+                                     g.ny * 2 * P2, 2 * P2, ty + 1, CU_TENSOR_MAP_L2_PROMOTION_NONE);
+            }
+        if (st != FDTD_OK) { delete pl; return st; }
+        for (int q = 0; q < 2; q++)
+            if (!aligned16(s->psi_h[4 + q]) || !aligned16(s->psi_e[0][4 + q]) || !aligned16(s->psi_e[1][4 + q])) {
+                delete pl; return FDTD_ERR_ALIGN;
+            }
+    }
+    p.zpsi = zpsi ? 1 : 0;
+    p.zbox = zbox;
+    p.stage_bytes = ke->stage + 4 * zbox;
+    const int tab_bytes = 6 * 2 * (p.P[0] + p.P[1] + p.P[2]) * 4;
+    pl->smem = ns * p.stage_bytes + ke->enew + 128 /*barriers*/ + tab_bytes + 128 /*align slack*/;
+    int dev = 0, nsm = 0, occ = 0, optin = 0;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)ke->fn);
+    if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
+    const int max_dyn = optin - (int)fa.sharedSizeBytes;
+    if (pl->smem > max_dyn) { delete pl; return FDTD_ERR_UNSUPPORTED; }
+    // the attribute is an upper bound; every plan of this kernel fits under it
+    e = cudaFuncSetAttribute((const void *)ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)ke->fn, ke->threads, pl->smem);
+    if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
+    if (occ < 1) { delete pl; return FDTD_ERR_UNSUPPORTED; }
+    if (tile && tile->ctas_per_sm > 0) occ = std::min(occ, (int)tile->ctas_per_sm);
+    pl->nblocks = (int)std::min<int64_t>(pl->nitems, (int64_t)nsm * occ);
     *out = pl;
     return FDTD_OK;
 }
@@ -645,9 +892,8 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
             p.psi_e_out[q] = pl->psi_e[outb][q];
         }
         p.t = t0 + n;
-        int r = pl->ty == 4 ? launch<4>(pl, pl->maps[in], p, st)
-                            : pl->ty == 8 ? launch<8>(pl, pl->maps[in], p, st) : launch<16>(pl, pl->maps[in], p, st);
-        if (r != FDTD_OK) return r;
+        pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p);
+        FDTD_TRY(check_launch());
         pl->cur = outb;
     }
     return FDTD_OK;
@@ -658,6 +904,17 @@ int fdtd_yee_plan_current(const fdtd_yee_plan *pl) { return pl ? pl->cur : -1; }
 int fdtd_yee_plan_set_current(fdtd_yee_plan *pl, int32_t cur) {
     if (!pl || (cur != 0 && cur != 1)) return FDTD_ERR_ARG;
     pl->cur = cur;
+    return FDTD_OK;
+}
+
+int fdtd_yee_plan_info(const fdtd_yee_plan *pl, int32_t *info, int32_t n) {
+    if (!pl || !info || n < 6) return FDTD_ERR_ARG;
+    info[0] = pl->k->ty;
+    info[1] = pl->k->ns;
+    info[2] = pl->x_chunk;
+    info[3] = pl->nblocks;
+    info[4] = pl->k->threads;
+    info[5] = pl->smem;
     return FDTD_OK;
 }
 

@@ -115,13 +115,19 @@ class YeeSolver:
             st = self._state_struct()
             cp = self.cpml.struct()
             src = self.sources.struct()
-            tile = N.Tile(*(self.tile or (0, 0, 0)))
+            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             h = C.c_void_p()
             with torch.cuda.device(self.device):
                 N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
                        C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), self.cur)
             self._plan = h
         return self._plan
+
+    def plan_info(self):
+        """Launch shape chosen for the fused kernel."""
+        info = (C.c_int32 * 6)()
+        N.call("fdtd_yee_plan_info", self.plan(), info, 6)
+        return dict(zip(("tile_y", "stages", "x_chunk", "ctas", "threads", "smem_bytes"), list(info)))
 
     def step(self, n=1):
         """Advance n steps with the fused kernel (one launch per step)."""

@@ -136,10 +136,17 @@ typedef struct {
     const float *ce[3];
 } fdtd_yee_state;
 
+/* Launch shape of the fused kernel (0 = default): tile height in y (4, 8
+ * or 16 cells; the tile is 64 cells wide in z), x planes per work item,
+ * resident CTAs per SM (persistent grid), pipeline stages (planes staged in
+ * shared memory), L2 promotion of the tile loads (0 = 256 B, 1 = none,
+ * 2 = 64 B, 3 = 128 B). */
 typedef struct {
-    int32_t tile_y;       /* 0 = default */
-    int32_t x_chunk;      /* planes per work item, 0 = default */
-    int32_t ctas_per_sm;  /* 0 = default */
+    int32_t tile_y;
+    int32_t x_chunk;
+    int32_t ctas_per_sm;
+    int32_t stages;
+    int32_t l2_promotion;
 } fdtd_tile;
 
 typedef struct fdtd_yee_plan fdtd_yee_plan;
@@ -152,6 +159,8 @@ int fdtd_yee_plan_create(fdtd_yee_plan **plan, const fdtd_grid *g, const fdtd_ye
 int fdtd_yee_plan_run(fdtd_yee_plan *plan, int64_t t0, int64_t nsteps, void *stream);
 int fdtd_yee_plan_current(const fdtd_yee_plan *plan);
 int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
+/* info[0..5] = tile_y, stages, x_chunk, CTAs launched, threads/CTA, shared bytes/CTA */
+int fdtd_yee_plan_info(const fdtd_yee_plan *plan, int32_t *info, int32_t n);
 int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 
 /* ---- 4th-order symplectic stages (in place) --------------------------- */

@@ -159,10 +159,16 @@ def _oracle_sim(work_shape, ce, npml, faces, sources, init):
 
 @pytest.mark.parametrize("shape,npml,tile", [
     ((37, 29, 45), 5, None),
-    ((37, 29, 45), 5, (4, 7, 0)),
-    ((40, 33, 64), 6, (16, 16, 0)),
-    ((24, 20, 36), 0, (8, 5, 0)),
-    ((70, 9, 100), 3, (8, 64, 0)),
+    ((37, 29, 45), 5, (4, 7, 0, 6)),
+    ((40, 33, 64), 6, (16, 16, 0, 3)),
+    ((24, 20, 36), 0, (8, 5, 0, 3)),
+    ((70, 9, 100), 3, (8, 64, 0, 4)),
+    ((41, 35, 70), 4, (16, 8, 1, 3)),    # persistent: many work items per CTA
+    ((41, 35, 70), 4, (8, 3, 1, 3)),
+    ((19, 66, 33), 4, (16, 2, 1, 3)),
+    ((40, 40, 200), 4, (8, 16, 0, 4)),   # interior tiles take the packed fast path
+    ((30, 44, 260), 3, None),
+    ((24, 40, 200), 0, (4, 8, 0, 4)),
 ])
 def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     from fdtd_accelerate_gb300 import configs

@@ -57,7 +57,7 @@ struct Layout {
     static constexpr int ENEW = al128(3 * ENEWC * 4);
     static constexpr int SMEM = NS * STAGE + ENEW + 128 /*barriers*/ + 128 /*align slack*/;
     // CTAs per SM the register budget is sized for (shared memory may allow fewer)
-    static constexpr int MINB = TY == 4 ? 3 : (TY == 8 ? 2 : 1);
+    static constexpr int MINB = TY == 4 ? 4 : (TY == 8 ? 2 : 1);
 };
 
 struct TMaps {
@@ -681,8 +681,8 @@ static KernelEntry entry() {
 
 // Tile heights and pipeline depths compiled in (the autotuner picks among them).
 static const KernelEntry *find_kernel(int ty, int ns) {
-    static const KernelEntry table[] = {entry<4, 4>(), entry<4, 6>(), entry<8, 3>(), entry<8, 4>(),
-                                        entry<16, 3>()};
+    static const KernelEntry table[] = {entry<4, 3>(), entry<4, 4>(), entry<4, 6>(), entry<8, 3>(),
+                                        entry<8, 4>(),  entry<16, 3>()};
     for (const KernelEntry &e : table)
         if (e.ty == ty && e.ns == ns) return &e;
     return nullptr;

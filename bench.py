@@ -38,8 +38,9 @@ NPML = 12
 FALLBACK_HBM_GBS = 6790.7
 # DRAM bytes per cell-step of the fused kernel from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum over one launch / cells);
-# see profiles/k_yee_fused_cpml1024.md.  None until captured.
-NCU_DRAM_BYTES_PER_CELL = None
+# see profiles/k_yee_fused_cpml1024.md (512x512x256 capture of the same workload,
+# scaled by cells: an upper bound at full size, where the CPML fraction is smaller).
+NCU_DRAM_BYTES_PER_CELL = 81.4
 
 
 def algorithmic_bytes_per_step(shape, npml):
@@ -130,7 +131,7 @@ def cpu_oracle_sample(seconds=12.0, sample_shape=(256, 1024, 512)):
         sim.step(1)
         steps += 1
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 50:
+        if el >= seconds or steps >= 2000:
             break
     cells = int(np.prod(sample_shape))
     return {"value": cells * steps / el / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -251,7 +252,7 @@ def run_ours(args, rank, world):
                                "200 spheres eps_r U[1,12], 6 Gaussian dipoles" % tuple(shape),
                    "cells": cells, "l2": "state 33 GB >> L2 (no flush needed)",
                    "kernel": "k_yee_fused (TMA 3-D boxes, ping-pong state)",
-                   "tile": list(args.tile) if args.tile else "default (32x8, x_chunk 64)",
+                   "tile": solver.plan_info(),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,

@@ -16,5 +16,5 @@ __all__ = ["update_e", "update_h", "update_pbc_e", "update_pbc_h", "CpmlLayer", 
 
 
 def build(force=False, verbose=False):
-    from .build import build as _b
+    from .buildlib import build as _b
     return _b(force=force, verbose=verbose)

@@ -70,6 +70,11 @@ _SIGS = {
                                         C.POINTER(Sources), I64, P]),
     "fdtd_symplectic_h_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),
     "fdtd_symplectic_e_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),
+    "fdtd_symplectic_h_scalar_f32": (C.c_int, [C.POINTER(Grid), F32, F32] + [P] * 6 + [P]),
+    "fdtd_symplectic_cpml_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), F32] + [P] * 9
+                                   + [C.POINTER(Psi), P]),
+    "fdtd_symplectic_cpml_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), F32, F32] + [P] * 9
+                                   + [C.POINTER(Psi), P]),
     "fdtd_yee_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
                                        C.POINTER(Sources), C.POINTER(Tile), P, I32]),
     "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),
@@ -89,7 +94,7 @@ def lib():
         if not os.path.exists(LIB_PATH):
             raise ImportError("libfdtd_gb300.so not built: run "
                               "`python -c 'import __graft_entry__ as g; g.build()'` "
-                              "or `python fdtd_accelerate_gb300/build.py`")
+                              "or `python fdtd_accelerate_gb300/buildlib.py`")
         L = C.CDLL(LIB_PATH)
         for name, (res, args) in _SIGS.items():
             fn = getattr(L, name, None)

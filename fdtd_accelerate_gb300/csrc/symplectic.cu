@@ -65,6 +65,159 @@ k_symp_e(Grid g, float dl, float *__restrict__ ex, float *__restrict__ ey, float
     }
 }
 
+// H stage with a uniform ch (the 4th-order workload's ch = S/24): same
+// arithmetic as k_symp_h with (cl * ch) formed once.
+__global__ void __launch_bounds__(kSympBlock)
+k_symp_h_scalar(Grid g, float clch, const float *__restrict__ ex, const float *__restrict__ ey,
+                const float *__restrict__ ez, float *__restrict__ hx, float *__restrict__ hy, float *__restrict__ hz) {
+    const int64_t k = (int64_t)blockIdx.x * kSympBlock + threadIdx.x;
+    const int64_t j = blockIdx.y, i = blockIdx.z;
+    if (k >= g.nz) return;
+    const int64_t c = i * g.sx + j * g.sy + k, X = g.sx, Y = g.sy;
+    const bool jin = j > 1 && j < g.ny - 1, kin = k > 1 && k < g.nz - 1, iin = i > 1 && i < g.nx - 1;
+    if (jin && kin) {
+        float n = curl4(ez[c], ez[c - Y], ey[c], ey[c - 1]);
+        float f = curl4(ez[c + Y], ez[c - 2 * Y], ey[c + 1], ey[c - 2]);
+        hx[c] = fsub(hx[c], fmul(clch, fsub(fmul(27.0f, n), f)));
+    }
+    if (iin && kin) {
+        float n = curl4(ex[c], ex[c - 1], ez[c], ez[c - X]);
+        float f = curl4(ex[c + 1], ex[c - 2], ez[c + X], ez[c - 2 * X]);
+        hy[c] = fsub(hy[c], fmul(clch, fsub(fmul(27.0f, n), f)));
+    }
+    if (iin && jin) {
+        float n = curl4(ey[c], ey[c - X], ex[c], ex[c - Y]);
+        float f = curl4(ey[c + X], ey[c - 2 * X], ex[c + Y], ex[c - 2 * Y]);
+        hz[c] = fsub(hz[c], fmul(clch, fsub(fmul(27.0f, n), f)));
+    }
+}
+
+// 4th-order CPML (no reference counterpart: the reference's 4th-order code
+// has no absorbing boundary).  Same slab geometry as the 2nd-order CPML; the
+// derivative along the slab axis is the stage stencil's
+//   E nodes: d = 27*(F[i+1]-F[i]) - (F[i+2]-F[i-1])
+//   H nodes: d = 27*(F[i]-F[i-1]) - (F[i+1]-F[i-2])
+// psi = b*psi + a*d with the stage's b, a; F -/+= (coef*c)*(km1*d + psi)
+// only where the stage updates F.
+struct SympCpmlArgs {
+    int64_t P;
+    int front, back;
+    const float *b, *a, *km1;
+    float *psi1, *psi2;
+    float *f1, *f2;         // updated components
+    const float *g1, *g2;   // differentiated components
+    const float *c1, *c2;   // coefficient arrays (NULL -> scalar)
+    float coef, cscalar;    // stage coefficient, uniform coefficient
+};
+
+template <int AX, bool E>
+__global__ void k_symp_cpml(Grid g, SympCpmlArgs A) {
+    int64_t i, j, k, s;
+    const int64_t twoP = 2 * A.P;
+    if (AX == 0) {
+        k = (int64_t)blockIdx.x * kSympBlock + threadIdx.x;
+        j = blockIdx.y;
+        s = blockIdx.z;
+        if (k >= g.nz) return;
+    } else if (AX == 1) {
+        k = (int64_t)blockIdx.x * kSympBlock + threadIdx.x;
+        s = blockIdx.y;
+        i = blockIdx.z;
+        if (k >= g.nz) return;
+    } else {
+        const int64_t t = (int64_t)blockIdx.x * kSympBlock + threadIdx.x;
+        if (t >= g.nx * g.ny * twoP) return;
+        s = t % twoP;
+        j = (t / twoP) % g.ny;
+        i = t / (twoP * g.ny);
+    }
+    if (!(s < A.P ? A.front : A.back)) return;
+    const int64_t n_ax = AX == 0 ? g.nx : (AX == 1 ? g.ny : g.nz);
+    const int64_t node = E ? slab_node_e(s, A.P, n_ax) : slab_node_h(s, A.P, n_ax);
+    if (AX == 0) i = node;
+    else if (AX == 1) j = node;
+    else k = node;
+    const int64_t st = AX == 0 ? g.sx : (AX == 1 ? g.sy : 1);
+    const int64_t c = i * g.sx + j * g.sy + k;
+    const int64_t q = AX == 0 ? (s * g.ny + j) * g.nz + k : (AX == 1 ? (i * twoP + s) * g.nz + k : (i * g.ny + j) * twoP + s);
+    // update ranges of the stage: E in [1, n-3], H in [2, n-2] along the two
+    // axes the component differentiates
+    auto in_e = [&](int64_t x, int64_t n) { return x >= 1 && x <= n - 3; };
+    auto in_h = [&](int64_t x, int64_t n) { return x >= 2 && x <= n - 2; };
+    bool ok_i, ok_j, ok_k;
+    if (E) { ok_i = in_e(i, g.nx); ok_j = in_e(j, g.ny); ok_k = in_e(k, g.nz); }
+    else { ok_i = in_h(i, g.nx); ok_j = in_h(j, g.ny); ok_k = in_h(k, g.nz); }
+    // component 1 (sign -1 for E, +1 for H) and component 2 (opposite sign)
+    bool ok1, ok2;
+    if (AX == 0) { ok1 = ok_i && ok_k; ok2 = ok_i && ok_j; }
+    else if (AX == 1) { ok1 = ok_i && ok_j; ok2 = ok_j && ok_k; }
+    else { ok1 = ok_j && ok_k; ok2 = ok_i && ok_k; }
+    const float b = A.b[s], a = A.a[s], km1 = A.km1[s];
+    auto deriv = [&](const float *F) {
+        return E ? fsub(fmul(27.0f, fsub(F[c + st], F[c])), fsub(F[c + 2 * st], F[c - st]))
+                 : fsub(fmul(27.0f, fsub(F[c], F[c - st])), fsub(F[c + st], F[c - 2 * st]));
+    };
+    if (ok1) {
+        const float d = deriv(A.g1);
+        const float psi = fadd(fmul(b, A.psi1[q]), fmul(a, d));
+        A.psi1[q] = psi;
+        const float t = fmul(fmul(A.coef, A.c1 ? A.c1[c] : A.cscalar), fadd(fmul(km1, d), psi));
+        A.f1[c] = E ? fsub(A.f1[c], t) : fadd(A.f1[c], t);
+    }
+    if (ok2) {
+        const float d = deriv(A.g2);
+        const float psi = fadd(fmul(b, A.psi2[q]), fmul(a, d));
+        A.psi2[q] = psi;
+        const float t = fmul(fmul(A.coef, A.c2 ? A.c2[c] : A.cscalar), fadd(fmul(km1, d), psi));
+        A.f2[c] = E ? fadd(A.f2[c], t) : fsub(A.f2[c], t);
+    }
+}
+
+template <bool E>
+static int launch_symp_cpml(const Grid &g, const fdtd_cpml *cp, const fdtd_psi *psi, float coef, float cscalar,
+                            float *const F[3], const float *const G[3], const float *const Cf[3], cudaStream_t st) {
+    for (int ax = 0; ax < 3; ax++) {
+        const int64_t P = cp->npml[ax];
+        if (P <= 0) continue;
+        const int64_t n_ax = ax == 0 ? g.nx : (ax == 1 ? g.ny : g.nz);
+        if (n_ax < 2 * P + 2) return FDTD_ERR_SHAPE;
+        SympCpmlArgs A;
+        A.P = P;
+        A.front = (cp->faces >> (2 * ax)) & 1;
+        A.back = (cp->faces >> (2 * ax + 1)) & 1;
+        A.b = E ? cp->b_e[ax] : cp->b_h[ax];
+        A.a = E ? cp->a_e[ax] : cp->a_h[ax];
+        A.km1 = E ? cp->km1_e[ax] : cp->km1_h[ax];
+        A.psi1 = E ? psi->e[2 * ax] : psi->h[2 * ax];
+        A.psi2 = E ? psi->e[2 * ax + 1] : psi->h[2 * ax + 1];
+        if (!all_nonnull(A.b, A.a, A.km1, A.psi1, A.psi2)) return FDTD_ERR_ARG;
+        // (updated, differentiated) pairs: E: x (ey,hz),(ez,hy); y (ez,hx),(ex,hz); z (ex,hy),(ey,hx)
+        //                                  H: x (hy,ez),(hz,ey); y (hz,ex),(hx,ez); z (hx,ey),(hy,ex)
+        static const int u1[3] = {1, 2, 0}, u2[3] = {2, 0, 1};
+        static const int ge1[3] = {2, 0, 1}, ge2[3] = {1, 2, 0};
+        A.f1 = F[u1[ax]];
+        A.f2 = F[u2[ax]];
+        A.g1 = G[ge1[ax]];
+        A.g2 = G[ge2[ax]];
+        A.c1 = Cf ? Cf[u1[ax]] : nullptr;
+        A.c2 = Cf ? Cf[u2[ax]] : nullptr;
+        A.coef = coef;
+        A.cscalar = cscalar;
+        if (ax == 0) {
+            dim3 grid((unsigned)((g.nz + kSympBlock - 1) / kSympBlock), (unsigned)g.ny, (unsigned)(2 * P));
+            k_symp_cpml<0, E><<<grid, kSympBlock, 0, st>>>(g, A);
+        } else if (ax == 1) {
+            dim3 grid((unsigned)((g.nz + kSympBlock - 1) / kSympBlock), (unsigned)(2 * P), (unsigned)g.nx);
+            k_symp_cpml<1, E><<<grid, kSympBlock, 0, st>>>(g, A);
+        } else {
+            const int64_t n = g.nx * g.ny * 2 * P;
+            k_symp_cpml<2, E><<<(unsigned)((n + kSympBlock - 1) / kSympBlock), kSympBlock, 0, st>>>(g, A);
+        }
+        FDTD_TRY(check_launch());
+    }
+    return FDTD_OK;
+}
+
 }  // namespace fdtd
 
 using namespace fdtd;
@@ -91,6 +244,41 @@ int fdtd_symplectic_e_f32(const fdtd_grid *gp, float dl, float *ex, float *ey, f
     dim3 grid((unsigned)((g.nz + kSympBlock - 1) / kSympBlock), (unsigned)g.ny, (unsigned)g.nx);
     k_symp_e<<<grid, kSympBlock, 0, as_stream(stream)>>>(g, dl, ex, ey, ez, hx, hy, hz, cex, cey, cez);
     return check_launch();
+}
+
+int fdtd_symplectic_h_scalar_f32(const fdtd_grid *gp, float cl, float ch, const float *ex, const float *ey,
+                                 const float *ez, float *hx, float *hy, float *hz, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!all_nonnull(ex, ey, ez, hx, hy, hz)) return FDTD_ERR_ARG;
+    dim3 grid((unsigned)((g.nz + kSympBlock - 1) / kSympBlock), (unsigned)g.ny, (unsigned)g.nx);
+    const float clch = cl * ch;  // one IEEE single-precision product, as the reference's (cl*ch[c])
+    k_symp_h_scalar<<<grid, kSympBlock, 0, as_stream(stream)>>>(g, clch, ex, ey, ez, hx, hy, hz);
+    return check_launch();
+}
+
+int fdtd_symplectic_cpml_e_f32(const fdtd_grid *gp, const fdtd_cpml *c, float dl, float *ex, float *ey, float *ez,
+                               const float *hx, const float *hy, const float *hz, const float *cex,
+                               const float *cey, const float *cez, const fdtd_psi *psi, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!c || !psi || !all_nonnull(ex, ey, ez, hx, hy, hz, cex, cey, cez)) return FDTD_ERR_ARG;
+    float *const F[3] = {ex, ey, ez};
+    const float *const G[3] = {hx, hy, hz};
+    const float *const Cf[3] = {cex, cey, cez};
+    return launch_symp_cpml<true>(g, c, psi, dl, 0.f, F, G, Cf, as_stream(stream));
+}
+
+int fdtd_symplectic_cpml_h_f32(const fdtd_grid *gp, const fdtd_cpml *c, float cl, float ch, const float *ex,
+                               const float *ey, const float *ez, float *hx, float *hy, float *hz, const float *chx,
+                               const float *chy, const float *chz, const fdtd_psi *psi, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!c || !psi || !all_nonnull(ex, ey, ez, hx, hy, hz)) return FDTD_ERR_ARG;
+    float *const F[3] = {hx, hy, hz};
+    const float *const G[3] = {ex, ey, ez};
+    const float *const Cf[3] = {chx, chy, chz};
+    return launch_symp_cpml<false>(g, c, psi, cl, ch, F, G, chx ? Cf : nullptr, as_stream(stream));
 }
 
 }  // extern "C"

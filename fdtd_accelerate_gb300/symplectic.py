@@ -1,0 +1,233 @@
+"""4th-order spatial / 4-stage symplectic FDTD on CUDA float32 tensors.
+
+Reference: 4th_order-Symplectic/PyCUDA/100-base.py (kernels :10-44, integrator
+:58-63 and :124-141) and 4th_order-Symplectic/Python-C/dielectric.c:5-96.
+One step is
+
+    for sn in 0..3:  H stage (cl[sn]);  E stage (dl[sn]);  sources at t = tn + sn/5
+    H stage (cl[4])
+
+with cl = [c1, c2, c3, c2, c1], dl = [d1, d2, d2, d1, 0] (the closing H stage
+uses cl[4]; the C driver's cl[sn] at Python-C/100-base.py:69-72 is not
+followed).  Coefficients ce = (S/24)/eps_r, ch = S/24, S = 0.743
+(Python-C/100-base.py:11,28).
+
+CPML: the reference has none for this scheme; here each stage applies the
+kappa CPML of the 2nd-order scheme with the stage's sub-step: b = exp(-(sigma/
+kappa + alpha) * c * S), a = sigma/(sigma kappa + alpha kappa^2) (b - 1), and the
+stage stencil's 4th-order derivative (fdtd_symplectic_cpml_{e,h}_f32).
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .api import check_field_tensors, grid_of, stream_of
+from .cpml import parse_faces, sigma_max_from_reflection
+from .sources import PointSources
+
+__all__ = ["C1", "C2", "C3", "D1", "D2", "CL", "DL", "COURANT", "update_h", "update_e",
+           "stage_tables", "SymplecticCpml", "SymplecticSolver"]
+
+C1, C2, C3 = 0.17399689146541, -0.12038504121430, 0.89277629949778
+D1, D2 = 0.62337932451322, -0.12337932451322
+CL = (C1, C2, C3, C2, C1)
+DL = (D1, D2, D2, D1, 0.0)
+COURANT = 0.743
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _check_dims(nx, ny, nz, ref):
+    if (nx, ny, nz) != tuple(ref.shape):
+        raise ValueError("nx, ny, nz = %s do not match the arrays %s" % ((nx, ny, nz), tuple(ref.shape)))
+
+
+def update_h(nx, ny, nz, cl, ex, ey, ez, hx, hy, hz, chx, chy=None, chz=None):
+    """H stage, signature of dielectric.update_h (Python-C/dielectric.c:5-14).
+    chx may be a float (uniform ch) with chy = chz = None."""
+    names = ["ex", "ey", "ez", "hx", "hy", "hz"]
+    ts = [ex, ey, ez, hx, hy, hz]
+    scalar = isinstance(chx, (int, float))
+    if not scalar:
+        names += ["chx", "chy", "chz"]
+        ts += [chx, chy, chz]
+    ref = check_field_tensors(names, ts)
+    _check_dims(nx, ny, nz, ref)
+    g = grid_of(ref)
+    with torch.cuda.device(ref.device):
+        if scalar:
+            N.call("fdtd_symplectic_h_scalar_f32", C.byref(g), float(cl), float(chx),
+                   *map(_p, (ex, ey, ez, hx, hy, hz)), stream_of(ref))
+        else:
+            N.call("fdtd_symplectic_h_f32", C.byref(g), float(cl), *map(_p, ts), stream_of(ref))
+
+
+def update_e(nx, ny, nz, dl, ex, ey, ez, hx, hy, hz, cex, cey, cez):
+    """E stage, signature of dielectric.update_e (Python-C/dielectric.c:52-61)."""
+    ts = (ex, ey, ez, hx, hy, hz, cex, cey, cez)
+    ref = check_field_tensors(("ex", "ey", "ez", "hx", "hy", "hz", "cex", "cey", "cez"), ts)
+    _check_dims(nx, ny, nz, ref)
+    g = grid_of(ref)
+    with torch.cuda.device(ref.device):
+        N.call("fdtd_symplectic_e_f32", C.byref(g), float(dl), *map(_p, ts), stream_of(ref))
+
+
+def stage_tables(npml, coef, S=COURANT, m=4, R=1e-8, kappa_max=5.0, alpha_max=0.05, m_alpha=1):
+    """FP64 CPML tables of one stage (sub-step coef*S): b_e, a_e, b_h, a_h, km1_e, km1_h."""
+    P = int(npml)
+    smax = sigma_max_from_reflection(P, m, R)
+    s = np.arange(P, dtype=np.float64)
+    out = {}
+    for tag, d in (("e", np.concatenate([P - s - 0.5, s + 0.5])), ("h", np.concatenate([P - s, s + 1.0]))):
+        x = d / P
+        sig = smax * x ** m
+        kap = 1.0 + (kappa_max - 1.0) * x ** m
+        alp = alpha_max * (1.0 - x) ** m_alpha
+        b = np.exp(-(sig / kap + alp) * (coef * S))
+        den = sig * kap + alp * kap * kap
+        out["b_" + tag] = b
+        out["a_" + tag] = np.where(den > 0, sig / np.where(den > 0, den, 1.0) * (b - 1.0), 0.0)
+        out["km1_" + tag] = 1.0 / kap - 1.0
+    return out
+
+
+class SymplecticCpml:
+    """Device tables for every distinct stage coefficient and psi slabs."""
+
+    def __init__(self, shape, npml, faces=0x3F, S=COURANT, device="cuda", **params):
+        nx, ny, nz = shape
+        if isinstance(npml, int):
+            npml = (npml,) * 3
+        faces = parse_faces(faces)
+        npml = [int(p) if (faces >> (2 * a)) & 3 else 0 for a, p in enumerate(npml)]
+        for a, (p, n) in enumerate(zip(npml, shape)):
+            if p and n < 2 * p + 2:
+                raise ValueError("axis %d: %d CPML cells need at least %d cells" % (a, p, 2 * p + 2))
+        self.npml, self.faces, self.S = tuple(npml), faces, S
+        self.device = torch.device(device)
+        f32 = lambda v: torch.tensor(v, dtype=torch.float32, device=self.device)
+        self.tables = {}
+        for coef in sorted(set(CL) | set(DL[:4])):
+            t = [stage_tables(p, coef, S, **params) if p else None for p in npml]
+            self.tables[coef] = [{k: f32(v) for k, v in ta.items()} if ta else None for ta in t]
+        pshapes = [(2 * npml[0], ny, nz), (nx, 2 * npml[1], nz), (nx, ny, 2 * npml[2])]
+        z = lambda a: torch.zeros(pshapes[a], dtype=torch.float32, device=self.device) if npml[a] else None
+        self.psi_e = [z(a) for a in range(3) for _ in range(2)]
+        self.psi_h = [z(a) for a in range(3) for _ in range(2)]
+        self._structs = {c: self._make_struct(c) for c in self.tables}
+        self._psi = N.Psi()
+        for q in range(6):
+            self._psi.e[q] = self.psi_e[q].data_ptr() if self.psi_e[q] is not None else None
+            self._psi.h[q] = self.psi_h[q].data_ptr() if self.psi_h[q] is not None else None
+
+    @property
+    def active(self):
+        return any(self.npml)
+
+    def _make_struct(self, coef):
+        c = N.Cpml()
+        for a in range(3):
+            c.npml[a] = self.npml[a]
+        c.faces = self.faces
+        for a in range(3):
+            t = self.tables[coef][a]
+            for key in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h"):
+                getattr(c, key)[a] = t[key].data_ptr() if t else None
+        return c
+
+    def update_h(self, cl, ch, f, stream):
+        """f = (ex, ey, ez, hx, hy, hz); ch a float or three arrays."""
+        g = grid_of(f[0])
+        chs = (None, None, None) if isinstance(ch, (int, float)) else ch
+        chv = float(ch) if isinstance(ch, (int, float)) else 0.0
+        N.call("fdtd_symplectic_cpml_h_f32", C.byref(g), C.byref(self._structs[cl]), float(cl), chv,
+               *map(_p, f), *map(_p, chs), C.byref(self._psi), stream)
+
+    def update_e(self, dl, f, ce, stream):
+        """f = (ex, ey, ez, hx, hy, hz); ce three arrays."""
+        g = grid_of(f[0])
+        N.call("fdtd_symplectic_cpml_e_f32", C.byref(g), C.byref(self._structs[dl]), float(dl),
+               *map(_p, f), *map(_p, ce), C.byref(self._psi), stream)
+
+
+class SymplecticSolver:
+    """4-stage symplectic 4th-order FDTD on one GPU.
+
+    ce: three eps-weighted E coefficient arrays ((S/24)/eps_r); ch: a float
+    (uniform, default S/24) or three arrays; sources: (component, (i, j, k),
+    amplitude) with amplitude a callable of continuous time t (FP64), added
+    after every E stage at t = tn + sn/5 (PyCUDA/100-base.py:136).
+    """
+
+    def __init__(self, shape, ce=None, ch=None, npml=0, faces=0x3F, sources=(), device="cuda",
+                 S=COURANT, cpml_params=None, max_steps=0):
+        self.shape = tuple(int(v) for v in shape)
+        self.device = torch.device(device)
+        dev = self.device
+        self.S = S
+        self.f = [torch.zeros(self.shape, dtype=torch.float32, device=dev) for _ in range(6)]
+        if ce is None:
+            ce = [np.full(self.shape, S / 24.0)] * 3
+        self.ce = [torch.as_tensor(c, dtype=torch.float32, device=dev).contiguous() for c in ce]
+        self.ch = float(S / 24.0) if ch is None else (
+            float(ch) if isinstance(ch, (int, float)) else
+            [torch.as_tensor(c, dtype=torch.float32, device=dev).contiguous() for c in ch])
+        self.cpml = SymplecticCpml(self.shape, npml, faces, S, device=dev, **(cpml_params or {}))
+        self.src_spec = list(sources)
+        self.max_steps = max_steps
+        self.tstep = 1
+        self._src = None
+        self._build_sources(max(max_steps, 1))
+
+    def _build_sources(self, nsteps):
+        tabs = []
+        for comp, ijk, amp in self.src_spec:
+            t = np.zeros(4 * (nsteps + 2), dtype=np.float64)
+            for tn in range(1, nsteps + 2):
+                for sn in range(4):
+                    t[4 * tn + sn] = amp(tn + sn / 5.0)
+            tabs.append((comp, ijk, t))
+        self._src = PointSources(self.shape, tabs, device=self.device)
+        self._src_steps = nsteps
+
+    @property
+    def fields(self):
+        return dict(zip(("ex", "ey", "ez", "hx", "hy", "hz"), self.f))
+
+    def set_fields(self, **arrays):
+        for k, v in arrays.items():
+            self.fields[k].copy_(torch.as_tensor(v, dtype=torch.float32, device=self.device))
+
+    def step(self, n=1):
+        nx, ny, nz = self.shape
+        f, ce, ch = self.f, self.ce, self.ch
+        if self.src_spec and self.tstep + n > self._src_steps:
+            self._build_sources(self.tstep + n)
+        with torch.cuda.device(self.device):
+            stream = stream_of(f[0])
+            for _ in range(n):
+                tn = self.tstep
+                for sn in range(4):
+                    self._h_stage(CL[sn], stream)
+                    update_e(nx, ny, nz, DL[sn], *f, *ce)
+                    if self.cpml.active:
+                        self.cpml.update_e(DL[sn], f, ce, stream)
+                    if self.src_spec:
+                        self._src.apply(4 * tn + sn, *f[:3])
+                self._h_stage(CL[4], stream)
+                self.tstep += 1
+
+    def _h_stage(self, cl, stream):
+        nx, ny, nz = self.shape
+        f, ch = self.f, self.ch
+        if isinstance(ch, float):
+            update_h(nx, ny, nz, cl, *f, ch)
+        else:
+            update_h(nx, ny, nz, cl, *f, *ch)
+        if self.cpml.active:
+            self.cpml.update_h(cl, ch, f, stream)

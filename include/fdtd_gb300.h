@@ -173,6 +173,27 @@ int fdtd_symplectic_e_f32(const fdtd_grid *g, float dl,
                           const float *hx, const float *hy, const float *hz,
                           const float *cex, const float *cey, const float *cez, void *stream);
 
+/* H stage with a uniform ch (4th-order workload: ch = S/24); same update as
+ * fdtd_symplectic_h_f32 with ch arrays filled with `ch`. */
+int fdtd_symplectic_h_scalar_f32(const fdtd_grid *g, float cl, float ch,
+                                 const float *ex, const float *ey, const float *ez,
+                                 float *hx, float *hy, float *hz, void *stream);
+/* 4th-order CPML stage corrections (no reference counterpart: the
+ * reference's 4th-order programs have no absorbing boundary).  c holds the
+ * stage's b/a tables (b = exp(-(sigma/kappa+alpha)*coef*S)) and km1; slab
+ * geometry and psi layout as fdtd_cpml_{e,h}_f32.  Call after the stage's
+ * main update.  ch arrays may be NULL: uniform ch. */
+int fdtd_symplectic_cpml_e_f32(const fdtd_grid *g, const fdtd_cpml *c, float dl,
+                               float *ex, float *ey, float *ez,
+                               const float *hx, const float *hy, const float *hz,
+                               const float *cex, const float *cey, const float *cez,
+                               const fdtd_psi *psi, void *stream);
+int fdtd_symplectic_cpml_h_f32(const fdtd_grid *g, const fdtd_cpml *c, float cl, float ch,
+                               const float *ex, const float *ey, const float *ez,
+                               float *hx, float *hy, float *hz,
+                               const float *chx, const float *chy, const float *chz,
+                               const fdtd_psi *psi, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -413,3 +413,169 @@ void FN(symp_e)(const int64_t *g, REAL dl, REAL *ex, REAL *ey, REAL *ez,
                 }
             }
 }
+
+/* ------------------------------------------------------------------------ */
+/* 4th-order CPML (builder-defined: the reference has none).  Same slab     */
+/* geometry and psi layout as the 2nd-order CPML; the derivative along the  */
+/* slab axis is the 4th-order combination d = 27*(near) - (far) of the      */
+/* stage stencil; per stage: psi = b*psi + a*d and                          */
+/* F -/+= (c*coef)*(km1*d + psi), only where the stage updates F.            */
+/* E nodes use d = 27*(F[i+1]-F[i]) - (F[i+2]-F[i-1]);                      */
+/* H nodes use d = 27*(F[i]-F[i-1]) - (F[i+1]-F[i-2]).                      */
+/* ------------------------------------------------------------------------ */
+static inline REAL d4e(const REAL *F, int64_t c, int64_t st)
+{
+    return (REAL)27 * (F[c + st] - F[c]) - (F[c + 2 * st] - F[c - st]);
+}
+static inline REAL d4h(const REAL *F, int64_t c, int64_t st)
+{
+    return (REAL)27 * (F[c] - F[c - st]) - (F[c + st] - F[c - 2 * st]);
+}
+
+/* coef: E stage coefficient dl; ce arrays. psi[6] as cpml_e. */
+void FN(symp_cpml_e)(const int64_t *g, const int32_t *npml, int faces, REAL dl,
+                     const REAL *const *b, const REAL *const *a, const REAL *const *km1,
+                     REAL *ex, REAL *ey, REAL *ez,
+                     const REAL *hx, const REAL *hy, const REAL *hz,
+                     const REAL *cex, const REAL *cey, const REAL *cez,
+                     REAL *const *psi)
+{
+    GRID;
+    for (int ax = 0; ax < 3; ax++) {
+        const int64_t P = npml[ax];
+        if (P <= 0) continue;
+        const int64_t n_ax = ax == 0 ? nx : (ax == 1 ? ny : nz);
+        const int64_t st_ax = ax == 0 ? sx : (ax == 1 ? sy : 1);
+        REAL *p1 = psi[2 * ax], *p2 = psi[2 * ax + 1];
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int64_t i = 0; i < nx; i++)
+            for (int64_t j = 0; j < ny; j++)
+                for (int64_t k = 0; k < nz; k++) {
+                    const int64_t idx = ax == 0 ? i : (ax == 1 ? j : k);
+                    int64_t s;
+                    if ((faces >> (2 * ax)) & 1 && idx >= 1 && idx <= P) s = idx - 1;
+                    else if ((faces >> (2 * ax + 1)) & 1 && idx >= n_ax - P - 1 && idx <= n_ax - 2)
+                        s = P + idx - (n_ax - P - 1);
+                    else continue;
+                    const int64_t c = i * sx + j * sy + k;
+                    const int64_t q = ax == 0 ? (s * ny + j) * nz + k
+                                    : ax == 1 ? (i * 2 * P + s) * nz + k
+                                              : (i * ny + j) * 2 * P + s;
+                    const REAL bb = b[ax][s], aa = a[ax][s], kk = km1[ax][s];
+                    /* update ranges: ex j,k in [1,n-3]; ey i,k; ez i,j */
+                    const int ok_i = i >= 1 && i <= nx - 3, ok_j = j >= 1 && j <= ny - 3,
+                              ok_k = k >= 1 && k <= nz - 3;
+                    REAL *f1, *f2;
+                    const REAL *g1, *g2, *c1, *c2;
+                    int ok1, ok2;
+                    REAL s1, s2;
+                    if (ax == 0) { f1 = ey; g1 = hz; c1 = cey; ok1 = ok_i && ok_k; s1 = -1;
+                                   f2 = ez; g2 = hy; c2 = cez; ok2 = ok_i && ok_j; s2 = +1; }
+                    else if (ax == 1) { f1 = ez; g1 = hx; c1 = cez; ok1 = ok_i && ok_j; s1 = -1;
+                                        f2 = ex; g2 = hz; c2 = cex; ok2 = ok_j && ok_k; s2 = +1; }
+                    else { f1 = ex; g1 = hy; c1 = cex; ok1 = ok_j && ok_k; s1 = -1;
+                           f2 = ey; g2 = hx; c2 = cey; ok2 = ok_i && ok_k; s2 = +1; }
+                    if (ok1) {
+                        REAL d = d4e(g1, c, st_ax);
+                        p1[q] = bb * p1[q] + aa * d;
+                        REAL t = (dl * c1[c]) * (kk * d + p1[q]);
+                        f1[c] = s1 > 0 ? f1[c] + t : f1[c] - t;
+                    }
+                    if (ok2) {
+                        REAL d = d4e(g2, c, st_ax);
+                        p2[q] = bb * p2[q] + aa * d;
+                        REAL t = (dl * c2[c]) * (kk * d + p2[q]);
+                        f2[c] = s2 > 0 ? f2[c] + t : f2[c] - t;
+                    }
+                }
+    }
+}
+
+/* coef: H stage coefficient cl; ch arrays or NULL -> ch_scalar. psi[6] as cpml_h. */
+void FN(symp_cpml_h)(const int64_t *g, const int32_t *npml, int faces, REAL cl, REAL ch_scalar,
+                     const REAL *const *b, const REAL *const *a, const REAL *const *km1,
+                     const REAL *ex, const REAL *ey, const REAL *ez,
+                     REAL *hx, REAL *hy, REAL *hz,
+                     const REAL *chx, const REAL *chy, const REAL *chz,
+                     REAL *const *psi)
+{
+    GRID;
+    for (int ax = 0; ax < 3; ax++) {
+        const int64_t P = npml[ax];
+        if (P <= 0) continue;
+        const int64_t n_ax = ax == 0 ? nx : (ax == 1 ? ny : nz);
+        const int64_t st_ax = ax == 0 ? sx : (ax == 1 ? sy : 1);
+        REAL *p1 = psi[2 * ax], *p2 = psi[2 * ax + 1];
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int64_t i = 0; i < nx; i++)
+            for (int64_t j = 0; j < ny; j++)
+                for (int64_t k = 0; k < nz; k++) {
+                    const int64_t idx = ax == 0 ? i : (ax == 1 ? j : k);
+                    int64_t s;
+                    if ((faces >> (2 * ax)) & 1 && idx >= 1 && idx <= P) s = idx - 1;
+                    else if ((faces >> (2 * ax + 1)) & 1 && idx >= n_ax - P && idx <= n_ax - 1)
+                        s = P + idx - (n_ax - P);
+                    else continue;
+                    const int64_t c = i * sx + j * sy + k;
+                    const int64_t q = ax == 0 ? (s * ny + j) * nz + k
+                                    : ax == 1 ? (i * 2 * P + s) * nz + k
+                                              : (i * ny + j) * 2 * P + s;
+                    const REAL bb = b[ax][s], aa = a[ax][s], kk = km1[ax][s];
+                    /* update ranges: hx j,k in [2,n-2]; hy i,k; hz i,j */
+                    const int ok_i = i >= 2 && i <= nx - 2, ok_j = j >= 2 && j <= ny - 2,
+                              ok_k = k >= 2 && k <= nz - 2;
+                    REAL *f1, *f2;
+                    const REAL *g1, *g2, *c1, *c2;
+                    int ok1, ok2;
+                    REAL s1, s2;
+                    if (ax == 0) { f1 = hy; g1 = ez; c1 = chy; ok1 = ok_i && ok_k; s1 = +1;
+                                   f2 = hz; g2 = ey; c2 = chz; ok2 = ok_i && ok_j; s2 = -1; }
+                    else if (ax == 1) { f1 = hz; g1 = ex; c1 = chz; ok1 = ok_i && ok_j; s1 = +1;
+                                        f2 = hx; g2 = ez; c2 = chx; ok2 = ok_j && ok_k; s2 = -1; }
+                    else { f1 = hx; g1 = ey; c1 = chx; ok1 = ok_j && ok_k; s1 = +1;
+                           f2 = hy; g2 = ex; c2 = chy; ok2 = ok_i && ok_k; s2 = -1; }
+                    if (ok1) {
+                        REAL d = d4h(g1, c, st_ax);
+                        p1[q] = bb * p1[q] + aa * d;
+                        REAL t = (cl * (c1 ? c1[c] : ch_scalar)) * (kk * d + p1[q]);
+                        f1[c] = s1 > 0 ? f1[c] + t : f1[c] - t;
+                    }
+                    if (ok2) {
+                        REAL d = d4h(g2, c, st_ax);
+                        p2[q] = bb * p2[q] + aa * d;
+                        REAL t = (cl * (c2 ? c2[c] : ch_scalar)) * (kk * d + p2[q]);
+                        f2[c] = s2 > 0 ? f2[c] + t : f2[c] - t;
+                    }
+                }
+    }
+}
+
+/* 4th-order H stage with a scalar ch (ch arrays NULL): same arithmetic as symp_h */
+void FN(symp_h_scalar)(const int64_t *g, REAL cl, REAL ch, const REAL *ex, const REAL *ey, const REAL *ez,
+                       REAL *hx, REAL *hy, REAL *hz)
+{
+    GRID;
+    const REAL c27 = (REAL)27;
+    const REAL cc = cl * ch;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int64_t i = 0; i < nx; i++)
+        for (int64_t j = 0; j < ny; j++)
+            for (int64_t k = 0; k < nz; k++) {
+                const int64_t c = i * sx + j * sy + k;
+                if (j > 1 && j < ny - 1 && k > 1 && k < nz - 1) {
+                    REAL n = ((ez[c] - ez[c - sy]) - ey[c]) + ey[c - 1];
+                    REAL f = ((ez[c + sy] - ez[c - 2 * sy]) - ey[c + 1]) + ey[c - 2];
+                    hx[c] = hx[c] - cc * (c27 * n - f);
+                }
+                if (i > 1 && i < nx - 1 && k > 1 && k < nz - 1) {
+                    REAL n = ((ex[c] - ex[c - 1]) - ez[c]) + ez[c - sx];
+                    REAL f = ((ex[c + 1] - ex[c - 2]) - ez[c + sx]) + ez[c - 2 * sx];
+                    hy[c] = hy[c] - cc * (c27 * n - f);
+                }
+                if (i > 1 && i < nx - 1 && j > 1 && j < ny - 1) {
+                    REAL n = ((ey[c] - ey[c - sx]) - ex[c]) + ex[c - sy];
+                    REAL f = ((ey[c + sx] - ey[c - 2 * sx]) - ex[c + sy]) + ex[c - 2 * sy];
+                    hz[c] = hz[c] - cc * (c27 * n - f);
+                }
+            }
+}

@@ -14,7 +14,7 @@ from . import build as _build
 
 __all__ = ["update_e", "update_h", "pbc_e", "pbc_h", "cpml_e", "cpml_h",
            "add_points", "symp_h", "symp_e", "cpml_tables", "pulse",
-           "OracleSim", "lib"]
+           "OracleSim", "lib", "symp_h_scalar", "symp_cpml_e", "symp_cpml_h", "symp_stage_tables"]
 
 _LIBS = {}
 
@@ -219,3 +219,39 @@ class OracleSim:
             if pml:
                 cpml_h(self.npml, self.faces, self.tables, *E, *H, self.psi_h, *CH)
             self.tstep += 1
+
+
+def symp_h_scalar(cl, ch, ex, ey, ez, hx, hy, hz):
+    _check(ex, ey, ez, hx, hy, hz)
+    k, ct = _kind(ex)
+    getattr(lib(k), "orc_symp_h_scalar_" + k)(_grid(ex), ct(cl), ct(ch), *map(_p, (ex, ey, ez, hx, hy, hz)))
+
+
+def _symp_cpml(fn, npml, faces, coef_args, tables, which, E, H, coef, psi):
+    ref = E[0]
+    k, ct = _kind(ref)
+    keep, ptrs = [], []
+    for name in ("b", "a", "km1"):
+        arrs, pp = _tables(tables, name + "_" + which, ref.dtype)
+        keep.append(arrs)
+        ptrs.append(pp)
+    psi_p = (C.c_void_p * 6)(*[(p.ctypes.data if p is not None else 0) for p in psi])
+    npml_c = (C.c_int32 * 3)(*npml)
+    getattr(lib(k), fn + k)(_grid(ref), npml_c, C.c_int(faces), *[ct(v) for v in coef_args],
+                            ptrs[0], ptrs[1], ptrs[2], *map(_p, E), *map(_p, H), *map(_p, coef), psi_p)
+
+
+def symp_cpml_e(npml, faces, dl, tables, ex, ey, ez, hx, hy, hz, cex, cey, cez, psi_e):
+    """4th-order CPML E-stage correction; tables: stage tables (b_e, a_e, km1_e per axis)."""
+    _symp_cpml("orc_symp_cpml_e_", npml, faces, (dl,), tables, "e", (ex, ey, ez), (hx, hy, hz),
+               (cex, cey, cez), psi_e)
+
+
+def symp_cpml_h(npml, faces, cl, ch_scalar, tables, ex, ey, ez, hx, hy, hz, psi_h, chx=None, chy=None, chz=None):
+    _symp_cpml("orc_symp_cpml_h_", npml, faces, (cl, ch_scalar), tables, "h", (ex, ey, ez), (hx, hy, hz),
+               (chx, chy, chz), psi_h)
+
+
+def symp_stage_tables(npml, coef, S=0.743, m=4, R=1e-8, kappa_max=5.0, alpha_max=0.05, m_alpha=1):
+    """Stage tables of the 4th-order CPML: cpml_tables with the sub-step coef*S."""
+    return cpml_tables(npml, m=m, R=R, kappa_max=kappa_max, alpha_max=alpha_max, m_alpha=m_alpha, dt=coef * S)

@@ -1,0 +1,157 @@
+"""GPU parity of the 4th-order symplectic path (stages, CPML, whole steps)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests.conftest import cuda_available
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not cuda_available(), reason="needs a CUDA GPU")]
+
+NAMES = ("ex", "ey", "ez", "hx", "hy", "hz")
+
+
+@pytest.fixture(scope="module")
+def S():
+    import fdtd_accelerate_gb300 as F
+    F.build()
+    from fdtd_accelerate_gb300 import symplectic
+    return symplectic
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host(t):
+    return t.detach().cpu().numpy()
+
+
+def test_golden_reference_c_stages_through_gpu(S, golden_dir):
+    """4th_order-Symplectic/Python-C/dielectric.c outputs, reproduced through
+    the reference signature update_h(nx, ny, nz, cl, ...)."""
+    g = np.load(os.path.join(golden_dir, "symp_c.npz"))
+    for n in range(int(g["ncases"])):
+        t = "c%d_" % n
+        which = int(g[t + "meta"][0])
+        f = [_dev(g[t + "in_" + k]) for k in NAMES]
+        c = [_dev(g[t + "in_" + k]) for k in ("c0", "c1", "c2")]
+        coef = float(g[t + "coef"][()])
+        nx, ny, nz = f[0].shape
+        if which == 0:
+            S.update_h(nx, ny, nz, coef, *f, *c)
+            comps = range(3, 6)
+        else:
+            S.update_e(nx, ny, nz, coef, *f, *c)
+            comps = range(0, 3)
+        torch.cuda.synchronize()
+        for q in comps:
+            np.testing.assert_array_equal(_host(f[q])[:-1, :-1, :-1], g[t + "out_" + NAMES[q]][:-1, :-1, :-1],
+                                          err_msg="case %d %s" % (n, NAMES[q]))
+
+
+@pytest.mark.parametrize("shape", [(12, 13, 14), (20, 9, 33)])
+def test_stages_bit_exact_vs_oracle(S, shape):
+    rng = np.random.default_rng(2)
+    f = {k: rng.standard_normal(shape).astype(np.float32) for k in NAMES}
+    c = [rng.random(shape, dtype=np.float32) for _ in range(3)]
+    d = {k: _dev(v) for k, v in f.items()}
+    dc = [_dev(x) for x in c]
+    nx, ny, nz = shape
+    ch = np.float32(S.COURANT / 24)
+    for cl, dl in zip(S.CL[:4], S.DL[:4]):
+        oracle.symp_h(np.float32(cl), *(f[k] for k in NAMES), *c)
+        S.update_h(nx, ny, nz, cl, *(d[k] for k in NAMES), *dc)
+        oracle.symp_h_scalar(np.float32(cl), ch, *(f[k] for k in NAMES))
+        S.update_h(nx, ny, nz, cl, *(d[k] for k in NAMES), float(ch))
+        oracle.symp_e(np.float32(dl), *(f[k] for k in NAMES), *c)
+        S.update_e(nx, ny, nz, dl, *(d[k] for k in NAMES), *dc)
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(d[k]), f[k], err_msg=k)
+
+
+class OracleSymplectic:
+    """The symplectic step of SymplecticSolver restated with oracle calls."""
+
+    def __init__(self, S, shape, ce, ch, npml, faces, sources, dtype=np.float32):
+        self.S, self.shape, self.dtype = S, shape, dtype
+        self.f = {k: np.zeros(shape, dtype) for k in NAMES}
+        self.ce = [np.asarray(c, dtype) for c in ce]
+        self.ch = dtype(ch)
+        self.npml, self.faces = npml, faces
+        self.tables = {}
+        for coef in set(S.CL) | set(S.DL[:4]):
+            t = [oracle.symp_stage_tables(p, coef, S.COURANT) if p else None for p in npml]
+            self.tables[coef] = {k: [x[k] if x is not None else None for x in t]
+                                 for k in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h")}
+        nx, ny, nz = shape
+        ps = [(2 * npml[0], ny, nz), (nx, 2 * npml[1], nz), (nx, ny, 2 * npml[2])]
+        self.psi_e = [np.zeros(ps[a], dtype) if npml[a] else None for a in range(3) for _ in range(2)]
+        self.psi_h = [np.zeros(ps[a], dtype) if npml[a] else None for a in range(3) for _ in range(2)]
+        self.sources = sources
+        self.tstep = 1
+
+    def _h(self, cl):
+        f = self.f
+        oracle.symp_h_scalar(self.dtype(cl), self.ch, *(f[k] for k in NAMES))
+        if any(self.npml):
+            oracle.symp_cpml_h(self.npml, self.faces, self.dtype(cl), self.ch, self.tables[cl],
+                               *(f[k] for k in NAMES), self.psi_h)
+
+    def step(self, n):
+        f, S = self.f, self.S
+        for _ in range(n):
+            tn = self.tstep
+            for sn in range(4):
+                self._h(S.CL[sn])
+                oracle.symp_e(self.dtype(S.DL[sn]), *(f[k] for k in NAMES), *self.ce)
+                if any(self.npml):
+                    oracle.symp_cpml_e(self.npml, self.faces, self.dtype(S.DL[sn]), self.tables[S.DL[sn]],
+                                       *(f[k] for k in NAMES), *self.ce, self.psi_e)
+                for comp, (i, j, k), amp in self.sources:
+                    f[comp][i, j, k] = f[comp][i, j, k] + self.dtype(np.float32(amp(tn + sn / 5.0)))
+            self._h(S.CL[4])
+            self.tstep += 1
+
+
+@pytest.mark.parametrize("shape,npml,faces", [((30, 26, 34), 5, 0x3F), ((24, 28, 20), 4, 0x15),
+                                              ((22, 22, 40), 0, 0x3F)])
+def test_symplectic_steps_bit_exact_vs_oracle(S, shape, npml, faces):
+    from fdtd_accelerate_gb300 import configs
+    rng = np.random.default_rng(4)
+    spheres = configs.random_spheres(rng, shape, 5, 2, 5, 1.0, 4.0)
+    ce = [(c.numpy() * np.float32(S.COURANT / 24 / 0.5)).astype(np.float32)
+          for c in configs.ce_from_spheres(shape, spheres)]
+    src = [("ez", (shape[0] // 2, shape[1] // 2, shape[2] // 2),
+            lambda t: np.sin(0.3 * t) * np.exp(-0.5 * ((t - 4.0) / 2.0) ** 2))]
+    solver = S.SymplecticSolver(shape, ce=ce, npml=npml, faces=faces, sources=src, max_steps=8)
+    orc = OracleSymplectic(S, shape, ce, S.COURANT / 24, solver.cpml.npml, solver.cpml.faces, src)
+    solver.step(6)
+    orc.step(6)
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(solver.fields[k]), orc.f[k], err_msg=k)
+    for q in range(6):
+        if orc.psi_e[q] is not None:
+            np.testing.assert_array_equal(_host(solver.cpml.psi_e[q]), orc.psi_e[q], err_msg="psi_e%d" % q)
+            np.testing.assert_array_equal(_host(solver.cpml.psi_h[q]), orc.psi_h[q], err_msg="psi_h%d" % q)
+
+
+def test_symplectic_cpml_absorbs(S):
+    """A pulse launched in a CPML box leaves: field energy falls well below the
+    PEC box's energy, which stays bounded (the scheme is stable)."""
+    shape = (48, 48, 48)
+    # derivative of a Gaussian: no DC part, so no static field stays behind
+    src = [("ez", (24, 24, 24), lambda t: -(t - 20.0) / 16.0 * np.exp(-0.5 * ((t - 20.0) / 4.0) ** 2))]
+    energies = {}
+    for npml in (0, 8):
+        s = S.SymplecticSolver(shape, npml=npml, sources=src, max_steps=300)
+        s.step(300)
+        torch.cuda.synchronize()
+        energies[npml] = sum(float((t.double() ** 2).sum()) for t in s.f)
+        assert np.isfinite(energies[npml])
+    assert energies[8] < 0.05 * energies[0], energies

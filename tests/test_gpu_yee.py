@@ -233,3 +233,20 @@ def test_api_errors(fdtd):
         fdtd.update_pbc_e("xw", a, a, a)
     with pytest.raises(ValueError):
         fdtd.YeeSolver((10, 10, 10), npml=5)   # 2P+2 > n
+
+
+def test_cpml_absorbs_outgoing_pulse(fdtd):
+    """A zero-mean pulse radiated from the centre leaves a CPML box: the field
+    energy that remains is a small fraction of the PEC box's (lossless) energy."""
+    shape = (64, 64, 64)
+    t = np.arange(402, dtype=np.float64)
+    amp = -(t - 30.0) / 36.0 * np.exp(-0.5 * ((t - 30.0) / 6.0) ** 2)
+    energies = {}
+    for npml in (0, 10):
+        s = fdtd.YeeSolver(shape, npml=npml, sources=[("ez", (32, 32, 32), amp)])
+        s.step(400)
+        torch.cuda.synchronize()
+        s.check_status()
+        energies[npml] = sum(float((v.double() ** 2).sum()) for v in s.fields.values())
+        assert np.isfinite(energies[npml])
+    assert energies[10] < 0.01 * energies[0], energies

@@ -6,13 +6,14 @@ symplectic variant, as hand-written sm_103a CUDA kernels behind the C ABI
 in include/fdtd_gb300.h, with the reference's Python call shapes on top.
 """
 from . import _native
+from .batch import BatchSolver
 from .api import update_e, update_h, update_pbc_e, update_pbc_h
 from .cpml import CpmlLayer, cpml_tables
 from .solver import YeeSolver
 from .sources import PointSources, gaussian_sine
 
 __all__ = ["update_e", "update_h", "update_pbc_e", "update_pbc_h", "CpmlLayer", "cpml_tables",
-           "YeeSolver", "PointSources", "gaussian_sine", "build"]
+           "YeeSolver", "BatchSolver", "PointSources", "gaussian_sine", "build"]
 
 
 def build(force=False, verbose=False):

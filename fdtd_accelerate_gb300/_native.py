@@ -82,6 +82,14 @@ _SIGS = {
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
     "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
+    "fdtd_batch_workspace_bytes": (C.c_size_t, [I32]),
+    "fdtd_batch_plan_create": (C.c_int, [C.POINTER(P), I32, C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
+                                         C.POINTER(Sources), C.POINTER(Tile), P, P, C.c_size_t, I32]),
+    "fdtd_batch_plan_run": (C.c_int, [P, I64, I64, P]),
+    "fdtd_batch_plan_current": (C.c_int, [P]),
+    "fdtd_batch_plan_set_current": (C.c_int, [P, I32]),
+    "fdtd_batch_plan_info": (C.c_int, [P, P, I32]),
+    "fdtd_batch_plan_destroy": (C.c_int, [P]),
 }
 
 _lib = None

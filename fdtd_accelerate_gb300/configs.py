@@ -12,6 +12,9 @@ Workloads
   cpml1024   1024 x 1024 x 512, 12-cell CPML on all faces (m=4, R=1e-8,
              kappa_max=5, alpha_max=0.05), 200 seeded spheres (radius 5..40,
              eps_r U[1,12]), 6 seeded dipoles (delays t0 in [100, 300])
+  batched64  64 independent grids, each axis drawn from {32, 48, ..., 192},
+             8-cell CPML, 10 spheres per grid (radius 2..n_min/6, eps_r
+             U[1,8]), Ez source at the centre, 500 steps
 """
 import math
 from dataclasses import dataclass, field
@@ -21,7 +24,7 @@ import torch
 
 from .sources import gaussian_sine
 
-__all__ = ["Workload", "plain128", "cpml1024", "scaled", "paint_spheres", "ce_from_spheres",
+__all__ = ["Workload", "plain128", "cpml1024", "batched64", "scaled", "paint_spheres", "ce_from_spheres",
            "random_spheres", "random_dipoles", "STAGGER"]
 
 # offsets of (ex, ey, ez) sample points from (i, j, k)
@@ -82,6 +85,20 @@ def cpml1024(steps=2000, shape=(1024, 1024, 512), seed=20261203, nspheres=200, n
     dipoles = random_dipoles(rng, shape, ndipoles, npml + 2)
     return Workload("Yee+CPML %dx%dx%d, %d-cell CPML, %d spheres, %d dipoles" % (*shape, npml, nspheres, ndipoles),
                     tuple(shape), steps, npml=npml, spheres=spheres, dipoles=dipoles, seed=seed)
+
+
+def batched64(nsims=64, steps=500, seed=20261204, sizes=tuple(range(32, 193, 16)), npml=8, nspheres=10):
+    """Ragged batch: per-axis sizes drawn independently, per-grid spheres."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(nsims):
+        shape = tuple(int(rng.choice(sizes)) for _ in range(3))
+        rmax = max(2, min(shape) // 6)
+        spheres = random_spheres(rng, shape, nspheres, 2, rmax, 1.0, 8.0)
+        centre = tuple(n // 2 for n in shape)
+        out.append(Workload("batched grid %d: %dx%dx%d" % ((s,) + shape), shape, steps, npml=npml,
+                            spheres=spheres, dipoles=[("ez", centre, 150.0)], seed=seed))
+    return out
 
 
 def scaled(work, shape, steps=None):

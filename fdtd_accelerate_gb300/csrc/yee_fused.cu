@@ -26,6 +26,10 @@
 //    FDTD_ERR_TIMEOUT in a device status word and the CTA leaves its loop.
 #include <cuda.h>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "common.cuh"
 
 namespace fdtd {
@@ -91,6 +95,18 @@ struct Params {
     int32_t stage_bytes;  // bytes per pipeline stage (fields + z-psi boxes)
     int32_t zbox;         // bytes per z-psi box in shared memory (128-aligned)
     uint32_t tx_z;        // bytes the 4 z-psi boxes deliver
+};
+
+// Many independent grids advanced by one launch: work items of all grids are
+// numbered consecutively; item_off[s] is the first item of grid s.
+struct BatchDesc {
+    int32_t nsims;
+    int32_t cur;             // buffer holding the current state (same for every grid)
+    int64_t t;               // step number (source amplitude index)
+    const Params *params;    // [2*nsims]: grid s reading buffer b at params[2*s + b]
+    const TMaps *maps;       // [2*nsims]: tensor maps of grid s, input buffer b
+    const int64_t *item_off; // [nsims + 1]
+    int32_t stage_bytes;     // pipeline stage size (max over grids)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -212,9 +228,9 @@ __device__ __forceinline__ Coef tab_coef(const float *tabs, int base, int n2, in
     return Coef{t[s], t[n2 + s], t[2 * n2 + s]};
 }
 
-template <int TY, int NS>
+template <int TY, int NS, bool BATCH>
 __global__ void __launch_bounds__(Layout<TY, NS>::THREADS, Layout<TY, NS>::MINB)
-k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
+k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk, const __grid_constant__ BatchDesc bd) {
     using L = Layout<TY, NS>;
     // A stage is released one iteration after its plane was consumed, and each
     // iteration holds two planes: fewer than 3 stages would wait on a plane
@@ -223,11 +239,16 @@ k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *enew = reinterpret_cast<float *>(smem + NS * p.stage_bytes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * p.stage_bytes + L::ENEW);
+    // stage size: read from the kernel parameters at each use (a constant-bank
+    // operand) rather than held in a register
+#define FDTD_SB (BATCH ? bd.stage_bytes : pk.stage_bytes)
+    float *enew = reinterpret_cast<float *>(smem + NS * FDTD_SB);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * FDTD_SB + L::ENEW);
     float *Nx = enew, *Ny = enew + L::ENEWC, *Nz = enew + 2 * L::ENEWC;
     // CPML tables in shared memory: tab[(axis*2 + eh)*3 + {b,a,km}] has 2P[axis] entries
-    float *tabs = reinterpret_cast<float *>(smem + NS * p.stage_bytes + L::ENEW + 128);
+    float *tabs = reinterpret_cast<float *>(smem + NS * FDTD_SB + L::ENEW + 128);
+    // batched launches: parameters of the grid the current item belongs to
+    __shared__ __align__(16) Params s_p;
 
     __shared__ int s_abort;
     __shared__ int s_nls;
@@ -246,33 +267,19 @@ k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
     const int eko = col_warp ? -2 : 2 * lane;  // pair start relative to k0
     const bool own_row = warp < TY;
 
-    auto stage_ptr = [&](int st) { return smem + st * p.stage_bytes; };
+    auto stage_ptr = [&](int st) { return smem + st * FDTD_SB; };
     auto sH = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + c * L::HBOXB); };
     auto sE = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + 3 * L::HBOXB + c * L::EBOXB); };
     auto sC = [&](int st, int c) {
         return reinterpret_cast<float *>(stage_ptr(st) + 3 * L::HBOXB + (3 + c) * L::EBOXB);
     };
     // z-psi boxes: 0,1 = E psi (exz, eyz) input; 2,3 = H psi (hxz, hyz); row r holds 2P values
+    const Params &p = BATCH ? s_p : pk;
+    // z-psi boxes: 0,1 = E psi (exz, eyz) input; 2,3 = H psi (hxz, hyz); row r holds 2P values
     auto sZ = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + L::STAGE + c * p.zbox); };
 
-    if (tid == 0) {
-        for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (int c = 0; c < 3; c++) {
-            prefetch_tmap(&maps.h[c]);
-            prefetch_tmap(&maps.e[c]);
-            prefetch_tmap(&maps.ce[c]);
-        }
-        if (p.zpsi)
-            for (int c = 0; c < 2; c++) {
-                prefetch_tmap(&maps.zpe[c]);
-                prefetch_tmap(&maps.zph[c]);
-            }
-        s_abort = 0;
-    }
-    {
-        // stage the CPML coefficient tables (a few hundred floats) once per CTA
+    // stage the CPML coefficient tables of the current grid (a few hundred floats)
+    auto stage_tables = [&]() {
         int off = 0;
         for (int a = 0; a < 3; a++) {
             const int n2 = 2 * p.P[a];
@@ -282,23 +289,94 @@ k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
                 off += n2;
             }
         }
-    }
-    // offsets of each axis's six tables (b_e, a_e, km_e, b_h, a_h, km_h)
-    const int toff0 = 0, toff1 = 6 * 2 * p.P[0], toff2 = toff1 + 6 * 2 * p.P[1];
+    };
 
-    const int64_t nx = p.nx, ny = p.ny, nz = p.nz;
-    const int front0 = p.faces & 1, back0 = (p.faces >> 1) & 1;
-    const int front1 = (p.faces >> 2) & 1, back1 = (p.faces >> 3) & 1;
-    const int front2 = (p.faces >> 4) & 1, back2 = (p.faces >> 5) & 1;
-    const int P0 = p.P[0], P1 = p.P[1], P2 = p.P[2];
+    if (tid == 0) {
+        for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (!BATCH) {
+            for (int c = 0; c < 3; c++) {
+                prefetch_tmap(&mk.h[c]);
+                prefetch_tmap(&mk.e[c]);
+                prefetch_tmap(&mk.ce[c]);
+            }
+            if (pk.zpsi)
+                for (int c = 0; c < 2; c++) {
+                    prefetch_tmap(&mk.zpe[c]);
+                    prefetch_tmap(&mk.zph[c]);
+                }
+        }
+        s_abort = 0;
+    }
+    // per-grid values (loop invariant for a single grid; reloaded when a batched
+    // item switches grid)
+    int64_t nx, ny, nz;
+    int front0, back0, front1, back1, front2, back2, P0, P1, P2, toff1, toff2;
+    const int toff0 = 0;
+    auto load_derived = [&]() {
+        nx = p.nx;
+        ny = p.ny;
+        nz = p.nz;
+        front0 = p.faces & 1;
+        back0 = (p.faces >> 1) & 1;
+        front1 = (p.faces >> 2) & 1;
+        back1 = (p.faces >> 3) & 1;
+        front2 = (p.faces >> 4) & 1;
+        back2 = (p.faces >> 5) & 1;
+        P0 = p.P[0];
+        P1 = p.P[1];
+        P2 = p.P[2];
+        // offsets of each axis's six tables (b_e, a_e, km_e, b_h, a_h, km_h)
+        toff1 = 6 * 2 * P0;
+        toff2 = toff1 + 6 * 2 * P1;
+    };
+    if (!BATCH) {
+        stage_tables();
+        load_derived();
+    }
 
     uint32_t g0 = 0;          // planes this CTA has issued before the current item
     int64_t issued_hi = -1;   // highest plane index (relative) issued in the current item (tid 0)
     int64_t q_abort = 0, i_start_abort = 0;
     bool aborted = false;
-    const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
+    const int64_t nitems = BATCH ? bd.item_off[bd.nsims] : (int64_t)pk.ntz * pk.nty * pk.nxc;
+    int cur_sim = -1;
 
-    for (int64_t item = blockIdx.x; item < nitems && !aborted; item += gridDim.x) {
+    for (int64_t gitem = blockIdx.x; gitem < nitems && !aborted; gitem += gridDim.x) {
+        int64_t item = gitem;
+        const TMaps *mp = &mk;
+        if (BATCH) {
+            // grid of this item: largest s with item_off[s] <= gitem
+            int lo = 0, hi = bd.nsims - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (bd.item_off[mid] <= gitem) lo = mid;
+                else hi = mid - 1;
+            }
+            item = gitem - bd.item_off[lo];
+            mp = &bd.maps[2 * lo + bd.cur];
+            if (lo != cur_sim) {
+                __syncthreads();  // every thread is done with the previous grid's parameters
+                if (tid < (int)(sizeof(Params) / 4))
+                    reinterpret_cast<int32_t *>(&s_p)[tid] =
+                        reinterpret_cast<const int32_t *>(&bd.params[2 * lo + bd.cur])[tid];
+                __syncthreads();
+                if (tid == 0) {
+                    s_p.t = bd.t;
+                    for (int c = 0; c < 3; c++) {
+                        prefetch_tmap(&mp->h[c]);
+                        prefetch_tmap(&mp->e[c]);
+                        prefetch_tmap(&mp->ce[c]);
+                    }
+                }
+                stage_tables();
+                __syncthreads();
+                load_derived();
+                cur_sim = lo;
+            }
+        }
+        const TMaps &maps = *mp;
         const int64_t tzi = item % p.ntz, tyi = (item / p.ntz) % p.nty, xci = item / ((int64_t)p.ntz * p.nty);
         const int64_t k0 = tzi * TZ, j0 = tyi * TY;
         const int64_t x0 = xci * p.x_chunk;
@@ -638,6 +716,7 @@ k_yee_fused(const __grid_constant__ TMaps maps, const Params p) {
         __syncthreads();
     }
 }
+#undef FDTD_SB
 
 }  // namespace fused
 }  // namespace fdtd
@@ -666,17 +745,17 @@ static EncodeTiledFn get_encode_fn() {
     return fn;
 }
 
-typedef void (*FusedKernel)(const TMaps, const Params);
+typedef void (*FusedKernel)(const TMaps, const Params, const BatchDesc);
 
 struct KernelEntry {
     int ty, ns, threads, stage, enew;
-    FusedKernel fn;
+    FusedKernel fn, fn_batch;
 };
 
 template <int TY, int NS>
 static KernelEntry entry() {
     return KernelEntry{TY, NS, Layout<TY, NS>::THREADS, Layout<TY, NS>::STAGE, Layout<TY, NS>::ENEW,
-                       k_yee_fused<TY, NS>};
+                       k_yee_fused<TY, NS, false>, k_yee_fused<TY, NS, true>};
 }
 
 // Tile heights and pipeline depths compiled in (the autotuner picks among them).
@@ -892,7 +971,8 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
             p.psi_e_out[q] = pl->psi_e[outb][q];
         }
         p.t = t0 + n;
-        pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p);
+        BatchDesc bd{};
+        pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
         FDTD_TRY(check_launch());
         pl->cur = outb;
     }
@@ -920,6 +1000,162 @@ int fdtd_yee_plan_info(const fdtd_yee_plan *pl, int32_t *info, int32_t n) {
 
 int fdtd_yee_plan_destroy(fdtd_yee_plan *pl) {
     delete pl;
+    return FDTD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched plan: many grids, one launch per step.  Every grid gets an ordinary
+// plan (validation, tensor maps, parameters); their Params/TMaps and the item
+// offsets live in a caller-provided device workspace.
+// ---------------------------------------------------------------------------
+struct fdtd_batch_plan {
+    int32_t nsims;
+    const KernelEntry *k;
+    int smem;
+    int nblocks;
+    int cur;
+    int64_t nitems;
+    int stage_bytes;
+    TMaps *d_maps;
+    Params *d_params;
+    int64_t *d_off;
+};
+
+static size_t batch_ws_layout(int32_t nsims, size_t *off_params, size_t *off_items) {
+    size_t o = 0;
+    o += (size_t)2 * nsims * sizeof(TMaps);
+    o = (o + 63) / 64 * 64;
+    *off_params = o;
+    o += (size_t)2 * nsims * sizeof(Params);
+    o = (o + 63) / 64 * 64;
+    *off_items = o;
+    o += (size_t)(nsims + 1) * sizeof(int64_t);
+    return o;
+}
+
+extern "C" {
+
+size_t fdtd_batch_workspace_bytes(int32_t nsims) {
+    size_t a, b;
+    return nsims > 0 ? batch_ws_layout(nsims, &a, &b) : 0;
+}
+
+int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid *grids, const fdtd_yee_state *states,
+                           const fdtd_cpml *cpmls, const fdtd_sources *srcs, const fdtd_tile *tile,
+                           int32_t *status_dev, void *workspace, size_t workspace_bytes, int32_t cur) {
+    if (!out || nsims <= 0 || !grids || !states || !status_dev || !workspace) return FDTD_ERR_ARG;
+    *out = nullptr;
+    if ((reinterpret_cast<uintptr_t>(workspace) & 63) != 0) return FDTD_ERR_ALIGN;
+    size_t off_p, off_i;
+    const size_t need = batch_ws_layout(nsims, &off_p, &off_i);
+    if (workspace_bytes < need) return FDTD_ERR_CAPACITY;
+    std::vector<TMaps> maps((size_t)2 * nsims);
+    std::vector<Params> params((size_t)2 * nsims);
+    std::vector<int64_t> off((size_t)nsims + 1, 0);
+    const KernelEntry *ke = nullptr;
+    int stage_bytes = 0, tab_bytes = 0;
+    for (int32_t s = 0; s < nsims; s++) {
+        fdtd_yee_plan *pl = nullptr;
+        const int st = fdtd_yee_plan_create(&pl, &grids[s], &states[s], cpmls ? &cpmls[s] : nullptr,
+                                            srcs ? &srcs[s] : nullptr, tile, status_dev, cur);
+        if (st != FDTD_OK) return st;
+        ke = pl->k;
+        stage_bytes = std::max(stage_bytes, pl->base.stage_bytes);
+        tab_bytes = std::max(tab_bytes, 6 * 2 * (pl->base.P[0] + pl->base.P[1] + pl->base.P[2]) * 4);
+        for (int b = 0; b < 2; b++) {
+            Params p = pl->base;
+            for (int q = 0; q < 6; q++) {
+                p.out[q] = pl->f[1 - b][q];
+                p.psi_e_in[q] = pl->psi_e[b][q];
+                p.psi_e_out[q] = pl->psi_e[1 - b][q];
+            }
+            params[2 * s + b] = p;
+            maps[2 * s + b] = pl->maps[b];
+        }
+        off[s + 1] = off[s] + pl->nitems;
+        fdtd_yee_plan_destroy(pl);
+    }
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    cudaError_t e = cudaMemcpy(ws, maps.data(), maps.size() * sizeof(TMaps), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ws + off_p, params.data(), params.size() * sizeof(Params), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ws + off_i, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
+
+    fdtd_batch_plan *bp = new fdtd_batch_plan();
+    bp->nsims = nsims;
+    bp->k = ke;
+    bp->stage_bytes = stage_bytes;
+    bp->smem = ke->ns * stage_bytes + ke->enew + 128 + tab_bytes + 128;
+    bp->cur = cur;
+    bp->nitems = off[nsims];
+    bp->d_maps = reinterpret_cast<TMaps *>(ws);
+    bp->d_params = reinterpret_cast<Params *>(ws + off_p);
+    bp->d_off = reinterpret_cast<int64_t *>(ws + off_i);
+    int dev = 0, nsm = 0, occ = 0, optin = 0;
+    cudaFuncAttributes fa;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)ke->fn_batch);
+    if (e != cudaSuccess) { set_cuda_error(e); delete bp; return FDTD_ERR_CUDA; }
+    const int max_dyn = optin - (int)fa.sharedSizeBytes;
+    if (bp->smem > max_dyn) { delete bp; return FDTD_ERR_UNSUPPORTED; }
+    e = cudaFuncSetAttribute((const void *)ke->fn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)ke->fn_batch, ke->threads, bp->smem);
+    if (e != cudaSuccess) { set_cuda_error(e); delete bp; return FDTD_ERR_CUDA; }
+    if (occ < 1) { delete bp; return FDTD_ERR_UNSUPPORTED; }
+    if (tile && tile->ctas_per_sm > 0) occ = std::min(occ, (int)tile->ctas_per_sm);
+    bp->nblocks = (int)std::min<int64_t>(bp->nitems, (int64_t)nsm * occ);
+    *out = bp;
+    return FDTD_OK;
+}
+
+int fdtd_batch_plan_run(fdtd_batch_plan *bp, int64_t t0, int64_t nsteps, void *stream) {
+    if (!bp || nsteps < 0) return FDTD_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    TMaps dummy_maps;
+    memset(&dummy_maps, 0, sizeof(dummy_maps));
+    Params dummy{};
+    for (int64_t n = 0; n < nsteps; n++) {
+        BatchDesc bd{};
+        bd.nsims = bp->nsims;
+        bd.cur = bp->cur;
+        bd.t = t0 + n;
+        bd.params = bp->d_params;
+        bd.maps = bp->d_maps;
+        bd.item_off = bp->d_off;
+        bd.stage_bytes = bp->stage_bytes;
+        bp->k->fn_batch<<<bp->nblocks, bp->k->threads, bp->smem, st>>>(dummy_maps, dummy, bd);
+        FDTD_TRY(check_launch());
+        bp->cur = 1 - bp->cur;
+    }
+    return FDTD_OK;
+}
+
+int fdtd_batch_plan_current(const fdtd_batch_plan *bp) { return bp ? bp->cur : -1; }
+
+int fdtd_batch_plan_set_current(fdtd_batch_plan *bp, int32_t cur) {
+    if (!bp || (cur != 0 && cur != 1)) return FDTD_ERR_ARG;
+    bp->cur = cur;
+    return FDTD_OK;
+}
+
+int fdtd_batch_plan_info(const fdtd_batch_plan *bp, int32_t *info, int32_t n) {
+    if (!bp || !info || n < 6) return FDTD_ERR_ARG;
+    info[0] = bp->k->ty;
+    info[1] = bp->k->ns;
+    info[2] = (int32_t)std::min<int64_t>(bp->nitems, 0x7fffffff);
+    info[3] = bp->nblocks;
+    info[4] = bp->k->threads;
+    info[5] = bp->smem;
+    return FDTD_OK;
+}
+
+int fdtd_batch_plan_destroy(fdtd_batch_plan *bp) {
+    delete bp;
     return FDTD_OK;
 }
 

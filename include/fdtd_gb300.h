@@ -37,6 +37,7 @@
 #ifndef FDTD_GB300_H
 #define FDTD_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -162,6 +163,28 @@ int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
 /* info[0..5] = tile_y, stages, x_chunk, CTAs launched, threads/CTA, shared bytes/CTA */
 int fdtd_yee_plan_info(const fdtd_yee_plan *plan, int32_t *info, int32_t n);
 int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
+
+/* ---- batched fused step: many independent grids, one launch per step --- */
+/* Every grid keeps its own state, CPML and sources (arrays as for
+ * fdtd_yee_plan_create); all grids advance together (same buffer index,
+ * same step number).  The per-grid launch parameters and TMA descriptors
+ * live in a caller-provided device workspace of
+ * fdtd_batch_workspace_bytes(nsims) bytes, 64-byte aligned (the plan
+ * allocates no device memory).  Each grid's result equals its own
+ * fdtd_yee_plan_run bit for bit.  No reference counterpart as one call:
+ * replaces one reference time loop per simulation. */
+typedef struct fdtd_batch_plan fdtd_batch_plan;
+size_t fdtd_batch_workspace_bytes(int32_t nsims);
+int fdtd_batch_plan_create(fdtd_batch_plan **plan, int32_t nsims, const fdtd_grid *grids,
+                           const fdtd_yee_state *states, const fdtd_cpml *cpmls,
+                           const fdtd_sources *srcs, const fdtd_tile *tile, int32_t *status_dev,
+                           void *workspace, size_t workspace_bytes, int32_t cur);
+int fdtd_batch_plan_run(fdtd_batch_plan *plan, int64_t t0, int64_t nsteps, void *stream);
+int fdtd_batch_plan_current(const fdtd_batch_plan *plan);
+int fdtd_batch_plan_set_current(fdtd_batch_plan *plan, int32_t cur);
+/* info[0..5] = tile_y, stages, work items, CTAs launched, threads/CTA, shared bytes/CTA */
+int fdtd_batch_plan_info(const fdtd_batch_plan *plan, int32_t *info, int32_t n);
+int fdtd_batch_plan_destroy(fdtd_batch_plan *plan);
 
 /* ---- 4th-order symplectic stages (in place) --------------------------- */
 int fdtd_symplectic_h_f32(const fdtd_grid *g, float cl,

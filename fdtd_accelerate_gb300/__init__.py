@@ -7,13 +7,14 @@ in include/fdtd_gb300.h, with the reference's Python call shapes on top.
 """
 from . import _native
 from .batch import BatchSolver
+from .adjoint import YeeAdjoint, fdtd_run
 from .api import update_e, update_h, update_pbc_e, update_pbc_h
 from .cpml import CpmlLayer, cpml_tables
 from .solver import YeeSolver
 from .sources import PointSources, gaussian_sine
 
 __all__ = ["update_e", "update_h", "update_pbc_e", "update_pbc_h", "CpmlLayer", "cpml_tables",
-           "YeeSolver", "BatchSolver", "PointSources", "gaussian_sine", "build"]
+           "YeeSolver", "BatchSolver", "YeeAdjoint", "fdtd_run", "PointSources", "gaussian_sine", "build"]
 
 
 def build(force=False, verbose=False):

@@ -47,7 +47,17 @@ class YeeState(C.Structure):
 
 
 class Tile(C.Structure):
-    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32)]
+    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32),
+                ("z_band", I32)]
+
+
+class Points(C.Structure):
+    _fields_ = [("n", I32), ("ijk", P), ("comp", P)]
+
+
+class AdjointState(C.Structure):
+    _fields_ = [("lf", P * 6), ("lpsi_e", P * 6), ("lpsi_h", P * 6), ("w_e", P * 6), ("w_h", P * 6),
+                ("grad_ce", P * 3)]
 
 
 class FdtdError(RuntimeError):
@@ -82,6 +92,10 @@ _SIGS = {
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
     "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
+    "fdtd_adjoint_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P, P,
+                                        C.POINTER(Points), P, P]),
+    "fdtd_gather_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
+    "fdtd_add_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_batch_workspace_bytes": (C.c_size_t, [I32]),
     "fdtd_batch_plan_create": (C.c_int, [C.POINTER(P), I32, C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
                                          C.POINTER(Sources), C.POINTER(Tile), P, P, C.c_size_t, I32]),

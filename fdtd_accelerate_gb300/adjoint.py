@@ -1,0 +1,307 @@
+"""Gradient of an FDTD run with respect to the E coefficients (CE = dt/eps).
+
+The reference has no gradient path; this is the reverse-time form of its
+2nd-order Yee step with CPML (the step of solver.py).  ``YeeAdjoint`` runs
+the forward simulation with the fused kernel, recording
+
+  * the field values at monitor points after every step, and
+  * a checkpoint of the whole state (E, H, psi_e, psi_h) every K steps,
+
+and its backward pass walks the segments last to first: it recomputes the K
+states of a segment from its checkpoint into K+1 state slots (one fused launch
+per step, each writing its own slot), then applies the hand-written adjoint
+step (fdtd_adjoint_step_f32) from the last state of the segment down to the
+first, accumulating dL/dCE.  Memory: ceil(N/K) checkpoints + (K+1) slots.
+
+``fdtd_run(ce, engine)`` is the differentiable call:
+
+    mon, fields = fdtd_run(ce, engine)      # ce: (3, nx, ny, nz), requires_grad
+    loss = (mon.double() ** 2).sum()
+    loss.backward()                         # ce.grad = dL/dCE (cex, cey, cez)
+
+The gradient with respect to a permittivity map follows through torch from
+CE = dt / eps (kuFDTD/v0.2.0/dim3/cpu/matter.py:81-83).
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .cpml import CpmlLayer
+from .solver import padded_nz
+from .sources import PointSources
+
+__all__ = ["YeeAdjoint", "fdtd_run", "COMPONENTS6"]
+
+COMPONENTS6 = ("ex", "ey", "ez", "hx", "hy", "hz")
+
+
+class YeeAdjoint:
+    """Forward/backward engine for one grid.
+
+    monitors: list of (component, (i, j, k)); component in ex..hz.
+    segment: checkpoint interval K (steps).
+    """
+
+    def __init__(self, shape, nsteps, npml=0, faces=0x3F, cpml_params=None, sources=(), monitors=(),
+                 segment=100, device="cuda", tile=None):
+        nx, ny, nz = (int(v) for v in shape)
+        self.shape = (nx, ny, nz)
+        self.nsteps = int(nsteps)
+        if self.nsteps < 1:
+            raise ValueError("nsteps must be positive")
+        self.K = max(1, min(int(segment), self.nsteps))
+        self.device = torch.device(device)
+        dev = self.device
+        self.nzp = padded_nz(nz)
+        self.cpml = CpmlLayer(self.shape, npml, faces, device=dev, **(cpml_params or {}))
+        self.sources = PointSources(self.shape, sources, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.tile = tile
+        K = self.K
+        # state slots: slot m holds the state after m steps of the current segment
+        self.slots = torch.zeros((K + 1, 6, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        self.slot_psi_e = [self._psi_like(self.cpml.psi_e[0]) for _ in range(K + 1)]
+        self.psi_h = self.cpml.psi_h
+        self._ce = torch.zeros((3, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        mons = list(monitors)
+        for comp, ijk in mons:
+            if comp not in COMPONENTS6:
+                raise ValueError("monitor component must be one of %s: %r" % (", ".join(COMPONENTS6), comp))
+            if len(ijk) != 3 or not all(0 <= int(v) < n for v, n in zip(ijk, self.shape)):
+                raise ValueError("monitor point %r outside the grid %r" % (tuple(ijk), self.shape))
+        self.nmon = len(mons)
+        self._mon_ijk = torch.tensor([list(map(int, p)) for _, p in mons] or [[0, 0, 0]],
+                                     dtype=torch.int32, device=dev)
+        self._mon_comp = torch.tensor([COMPONENTS6.index(c) for c, _ in mons] or [0],
+                                      dtype=torch.int32, device=dev)
+        self._plans = None
+        self._slots_hold = None   # (run id, segment) whose states the slots hold
+        self._run_id = 0
+
+    # ------------------------------------------------------------ helpers
+    @staticmethod
+    def _psi_like(lst):
+        return [torch.zeros_like(t) if t is not None else None for t in lst]
+
+    def grid(self):
+        nx, ny, nz = self.shape
+        return N.Grid(nx, ny, nz, ny * self.nzp, self.nzp)
+
+    def points(self):
+        p = N.Points()
+        p.n = self.nmon
+        p.ijk = self._mon_ijk.data_ptr()
+        p.comp = self._mon_comp.data_ptr()
+        return p
+
+    def _plan_state(self, m):
+        s = N.YeeState()
+        for b, slot in ((0, m), (1, m + 1)):
+            for q in range(6):
+                s.f[b][q] = self.slots[slot, q].data_ptr()
+                e = self.slot_psi_e[slot][q]
+                s.psi_e[b][q] = e.data_ptr() if e is not None else None
+        for q in range(6):
+            h = self.psi_h[q]
+            s.psi_h[q] = h.data_ptr() if h is not None else None
+        for q in range(3):
+            s.ce[q] = self._ce[q].data_ptr()
+        return s
+
+    def plans(self):
+        """One fused plan per slot pair (m -> m+1)."""
+        if self._plans is None:
+            g = self.grid()
+            cp = self.cpml.struct()
+            src = self.sources.struct()
+            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0, 0))[:6])
+            plans = []
+            with torch.cuda.device(self.device):
+                for m in range(self.K):
+                    h = C.c_void_p()
+                    st = self._plan_state(m)
+                    N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
+                           C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), 0)
+                    plans.append(h)
+            self._plans = plans
+        return self._plans
+
+    def _stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _step_slot(self, m, t):
+        """Fused step from slot m to slot m+1 with step number t."""
+        L = N.lib()
+        plan = self.plans()[m]
+        L.fdtd_yee_plan_set_current(plan, 0)
+        N.call("fdtd_yee_plan_run", plan, int(t), 1, self._stream())
+
+    def _slot_ptrs(self):
+        """Per-slot pointer arrays (fields, H, E-psi) built once."""
+        if getattr(self, "_ptrs", None) is None:
+            f, h, pe = [], [], []
+            for m in range(self.K + 1):
+                f.append((C.c_void_p * 6)(*[self.slots[m, q].data_ptr() for q in range(6)]))
+                h.append((C.c_void_p * 3)(*[self.slots[m, 3 + q].data_ptr() for q in range(3)]))
+                pe.append((C.c_void_p * 6)(*[t.data_ptr() if t is not None else None for t in self.slot_psi_e[m]]))
+            self._ptrs = (f, h, pe, self.grid(), self.points())
+        return self._ptrs
+
+    def _gather(self, slot, out_row):
+        if not self.nmon:
+            return
+        f, _, _, g, pts = self._slot_ptrs()
+        N.call("fdtd_gather_points_f32", C.byref(g), C.byref(pts), f[slot], C.c_void_p(out_row.data_ptr()),
+               self._stream())
+
+    def _segments(self):
+        K, N_ = self.K, self.nsteps
+        return [(c * K, min(K, N_ - c * K)) for c in range((N_ + K - 1) // K)]
+
+    def set_ce(self, ce):
+        nz = self.shape[2]
+        self._ce[:, :, :, :nz].copy_(ce.detach().to(device=self.device, dtype=torch.float32))
+
+    def _load(self, ck):
+        state, pe, ph = ck
+        self.slots[0].copy_(state)
+        for dst, src in zip(self.slot_psi_e[0], pe):
+            if dst is not None:
+                dst.copy_(src)
+        for dst, src in zip(self.psi_h, ph):
+            if dst is not None:
+                dst.copy_(src)
+
+    def _checkpoint(self):
+        return (self.slots[0].clone(), [t.clone() if t is not None else None for t in self.slot_psi_e[0]],
+                [t.clone() if t is not None else None for t in self.psi_h])
+
+    # ------------------------------------------------------------ forward
+    def forward(self, ce):
+        """Run nsteps from a zero state.  Returns (monitors (nsteps, nmon),
+        final fields (6, nx, ny, nz), checkpoints, run id)."""
+        nz = self.shape[2]
+        self.set_ce(ce)
+        self.plans()
+        self.slots[0].zero_()
+        for t in self.slot_psi_e[0] + self.psi_h:
+            if t is not None:
+                t.zero_()
+        mon = torch.zeros((self.nsteps, max(self.nmon, 1)), dtype=torch.float32, device=self.device)
+        checkpoints = []
+        segs = self._segments()
+        with torch.cuda.device(self.device):
+            for c, (t0, L) in enumerate(segs):
+                if c > 0:
+                    # slot 0 <- last state of the previous segment
+                    self.slots[0].copy_(self.slots[segs[c - 1][1]])
+                    for dst, src in zip(self.slot_psi_e[0], self.slot_psi_e[segs[c - 1][1]]):
+                        if dst is not None:
+                            dst.copy_(src)
+                checkpoints.append(self._checkpoint())
+                for m in range(L):
+                    self._step_slot(m, t0 + m + 1)
+                    self._gather(m + 1, mon[t0 + m])
+        self._run_id += 1
+        self._slots_hold = (self._run_id, len(segs) - 1)
+        final = self.slots[segs[-1][1], :, :, :, :nz].clone()
+        return mon[:, :self.nmon], final, checkpoints, self._run_id
+
+    # ------------------------------------------------------------ backward
+    def backward(self, ce, checkpoints, run_id, grad_mon=None, grad_fields=None):
+        """dL/dCE (3, nx, ny, nz) for the run that made ``checkpoints``."""
+        nx, ny, nz = self.shape
+        dev = self.device
+        self.set_ce(ce)
+        lf = torch.zeros((6, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        if grad_fields is not None:
+            lf[:, :, :, :nz].copy_(grad_fields)
+        gce = torch.zeros((3, nx, ny, self.nzp), dtype=torch.float32, device=dev)
+        lpe = self._psi_like(self.cpml.psi_e[0])
+        lph = self._psi_like(self.psi_h)
+        we = self._psi_like(self.cpml.psi_e[0])
+        wh = self._psi_like(self.psi_h)
+        st = N.AdjointState()
+        for q in range(6):
+            st.lf[q] = lf[q].data_ptr()
+            for arr, lst in ((st.lpsi_e, lpe), (st.lpsi_h, lph), (st.w_e, we), (st.w_h, wh)):
+                arr[q] = lst[q].data_ptr() if lst[q] is not None else None
+        for q in range(3):
+            st.grad_ce[q] = gce[q].data_ptr()
+        _, hps, pes, g, pts = self._slot_ptrs()
+        cp = self.cpml.struct()
+        ce_p = (C.c_void_p * 3)(*[self._ce[q].data_ptr() for q in range(3)])
+        gm = None
+        if grad_mon is not None and self.nmon:
+            gm = grad_mon.detach().to(device=dev, dtype=torch.float32).contiguous()
+        segs = self._segments()
+        with torch.cuda.device(dev):
+            stream = self._stream()
+            for c in range(len(segs) - 1, -1, -1):
+                t0, L = segs[c]
+                if self._slots_hold != (run_id, c):
+                    self._load(checkpoints[c])
+                    for m in range(L):
+                        self._step_slot(m, t0 + m + 1)
+                    self._slots_hold = (run_id, c)
+                fn = N.lib().fdtd_adjoint_step_f32
+                gp, cpp, stp = C.byref(g), C.byref(cp), C.byref(st)
+                ptsp = C.byref(pts) if gm is not None else None
+                row = gm.stride(0) * 4 if gm is not None else 0
+                base = gm.data_ptr() if gm is not None else 0
+                for n in range(L, 0, -1):
+                    T = t0 + n
+                    mon_ptr = C.c_void_p(base + (T - 1) * row) if gm is not None else None
+                    rc = fn(gp, cpp, stp, hps[n - 1], pes[n], ce_p, ptsp, mon_ptr, stream)
+                    if rc:
+                        N.check(rc, "fdtd_adjoint_step_f32")
+        return gce[:, :, :, :nz]
+
+    def check_status(self):
+        v = int(self.status.item())
+        if v:
+            self.status.zero_()
+            N.check(v, "fdtd_yee_plan_run (device status)")
+
+    def close(self):
+        if self._plans is not None:
+            L = N.lib()
+            for h in self._plans:
+                L.fdtd_yee_plan_destroy(h)
+            self._plans = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _YeeRun(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, ce, engine):
+        mon, final, cks, run_id = engine.forward(ce)
+        ctx.set_materialize_grads(False)
+        ctx.engine = engine
+        ctx.cks = cks
+        ctx.run_id = run_id
+        ctx.save_for_backward(ce)
+        return mon, final
+
+    @staticmethod
+    def backward(ctx, grad_mon, grad_fields):
+        (ce,) = ctx.saved_tensors
+        g = ctx.engine.backward(ce, ctx.cks, ctx.run_id, grad_mon=grad_mon, grad_fields=grad_fields)
+        return g.to(ce.dtype), None
+
+
+def fdtd_run(ce, engine):
+    """Differentiable run: (monitor series (nsteps, nmon), final fields
+    (6, nx, ny, nz)) as functions of ce (3, nx, ny, nz)."""
+    if not isinstance(engine, YeeAdjoint):
+        raise TypeError("engine must be a YeeAdjoint")
+    if tuple(ce.shape) != (3,) + engine.shape:
+        raise ValueError("ce must have shape (3, %d, %d, %d)" % engine.shape)
+    return _YeeRun.apply(ce, engine)

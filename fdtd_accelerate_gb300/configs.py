@@ -15,6 +15,11 @@ Workloads
   batched64  64 independent grids, each axis drawn from {32, 48, ..., 192},
              8-cell CPML, 10 spheres per grid (radius 2..n_min/6, eps_r
              U[1,8]), Ez source at the centre, 500 steps
+  adjoint256 256 x 256 x 128, 12-cell CPML, a centred 128 x 128 x 64 design
+             region of eps_r U[1,12] per cell in vacuum, an Ez line source
+             along z at x = npml+3, 16 seeded Ez probes in the far side of the
+             region, loss = sum over steps and probes of Ez^2, 3000 steps,
+             checkpoints every 100
 """
 import math
 from dataclasses import dataclass, field
@@ -24,7 +29,7 @@ import torch
 
 from .sources import gaussian_sine
 
-__all__ = ["Workload", "plain128", "cpml1024", "batched64", "scaled", "paint_spheres", "ce_from_spheres",
+__all__ = ["Workload", "plain128", "cpml1024", "batched64", "adjoint256", "scaled", "paint_spheres", "ce_from_spheres",
            "random_spheres", "random_dipoles", "STAGGER"]
 
 # offsets of (ex, ey, ez) sample points from (i, j, k)
@@ -99,6 +104,46 @@ def batched64(nsims=64, steps=500, seed=20261204, sizes=tuple(range(32, 193, 16)
         out.append(Workload("batched grid %d: %dx%dx%d" % ((s,) + shape), shape, steps, npml=npml,
                             spheres=spheres, dipoles=[("ez", centre, 150.0)], seed=seed))
     return out
+
+
+@dataclass
+class AdjointWorkload:
+    name: str
+    shape: tuple
+    steps: int
+    npml: int
+    eps: torch.Tensor          # (nx, ny, nz) eps_r per cell (CE = dt/eps for all three components)
+    design: tuple               # slices of the design region
+    sources: list               # (comp, ijk, FP64 table indexed by step number)
+    monitors: list              # (comp, ijk)
+    segment: int = 100
+    dt: float = 0.5
+
+
+def adjoint256(steps=3000, shape=(256, 256, 128), region=(128, 128, 64), npml=12, nprobes=16, seed=20261205,
+               segment=100):
+    """Inverse-design style run: gradient of a probe loss w.r.t. the permittivity of a design region."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    lo = [(n - r) // 2 for n, r in zip(shape, region)]
+    design = tuple(slice(l, l + r) for l, r in zip(lo, region))
+    eps = torch.ones(shape, dtype=torch.float32)
+    eps[design] = torch.from_numpy(rng.uniform(1.0, 12.0, size=region).astype(np.float32))
+    t = np.arange(steps + 1, dtype=np.float64)
+    amp = gaussian_sine(t, 150.0, 30.0, 0.05)
+    x_src = npml + 3
+    sources = [("ez", (x_src, ny // 2, k), amp) for k in range(npml + 1, nz - npml - 1)]
+    # probes in the far quarter (in x) of the design region
+    x0 = lo[0] + 3 * region[0] // 4
+    probes = []
+    while len(probes) < nprobes:
+        p = (int(rng.integers(x0, lo[0] + region[0])), int(rng.integers(lo[1], lo[1] + region[1])),
+             int(rng.integers(lo[2], lo[2] + region[2])))
+        if p not in probes:
+            probes.append(p)
+    return AdjointWorkload("adjoint %dx%dx%d, %d-cell CPML, design %dx%dx%d eps U[1,12], Ez line source, "
+                           "%d Ez probes, %d steps" % (*shape, npml, *region, nprobes, steps),
+                           tuple(shape), steps, npml, eps, design, sources, [("ez", p) for p in probes], segment)
 
 
 def scaled(work, shape, steps=None):

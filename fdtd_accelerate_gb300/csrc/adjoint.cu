@@ -1,0 +1,488 @@
+// Reverse-time (adjoint) kernels of the 2nd-order Yee step with CPML.
+//
+// The forward step (update_e, cpml_e, sources, update_h, cpml_h; the order of
+// 2nd_order-Yee/CUDA/fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:718-742
+// with the kappa CPML of kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c)
+// is linear in the state (E, H, psi_e, psi_h) for fixed CE.  One adjoint step
+// applies the transpose of that map to the adjoint state (lE, lH, lpsi_e,
+// lpsi_h) and adds this step's share of dL/dCE:
+//
+//   reverse H part  lE += -0.5 curl_f(lH)                   (E-update form)
+//                   + transpose of cpml_h (psi_h recursion, scatter of d)
+//   reverse E part  nu = CE * lE
+//                   lH += curl_b(nu)                        (H-update form)
+//                   + transpose of cpml_e
+//   gradient        dL/dCE += lE * G,  G = curl_f(H_prev) + sum sigma (km1 d + psi_e')
+//
+// where H_prev is the forward H entering the step and psi_e' the forward E-psi
+// after its update in the step (G is the E increment divided by CE).
+// Fields outside a component's update region never change in the forward
+// step, so their adjoints feed nothing: every gather below reads the other
+// family through its update mask, and only cells inside a mask are written.
+// No atomics: each output element is produced by one thread, so the result
+// does not depend on scheduling.
+#include "common.cuh"
+
+namespace fdtd {
+namespace adj {
+
+constexpr int kB = 128;
+
+struct Args {
+    Grid g;
+    int P[3], front[3], back[3];
+    float *lf[6];                 // lex, ley, lez, lhx, lhy, lhz
+    float *lpe[6], *lph[6];       // adjoint psi (layouts of fdtd_psi)
+    float *we[6], *wh[6];         // adjoint of the psi-driving differences (scratch)
+    float *gce[3];                // dL/dCE accumulators
+    const float *hp[3];           // forward H entering the step
+    const float *pe[6];           // forward E-psi after its update in the step
+    const float *ce[3];
+    const float *be[3], *ae[3], *ke[3];
+    const float *bh[3], *ah[3], *kh[3];
+};
+
+// dense psi indices: x (2P, ny, nz), y (nx, 2P, nz), z (nx, ny, 2P)
+__device__ __forceinline__ int64_t px(const Grid &g, int64_t s, int64_t j, int64_t k) { return (s * g.ny + j) * g.nz + k; }
+__device__ __forceinline__ int64_t py(const Grid &g, int P, int64_t i, int64_t s, int64_t k) {
+    return (i * 2 * P + s) * g.nz + k;
+}
+__device__ __forceinline__ int64_t pz(const Grid &g, int P, int64_t i, int64_t j, int64_t s) {
+    return (i * g.ny + j) * 2 * P + s;
+}
+
+// node index -> slab index (or -1) on an enabled face; inverse of slab_node_e/h
+__device__ __forceinline__ int slab_of_e(int64_t x, int P, int64_t n, int front, int back) {
+    if (P == 0) return -1;
+    if (front && x >= 1 && x <= P) return (int)(x - 1);
+    if (back && x >= n - P - 1 && x <= n - 2) return (int)(P + x - (n - P - 1));
+    return -1;
+}
+__device__ __forceinline__ int slab_of_h(int64_t x, int P, int64_t n, int front, int back) {
+    if (P == 0) return -1;
+    if (front && x >= 1 && x <= P) return (int)(x - 1);
+    if (back && x >= n - P && x <= n - 1) return (int)(P + x - (n - P));
+    return -1;
+}
+
+// update masks (2nd_order-Yee/Numpy/fdtd3d.py:4-13)
+__device__ __forceinline__ bool em(const Grid &g, int q, int64_t i, int64_t j, int64_t k) {
+    return q == 0 ? (j < g.ny - 1 && k < g.nz - 1) : q == 1 ? (i < g.nx - 1 && k < g.nz - 1) : (i < g.nx - 1 && j < g.ny - 1);
+}
+__device__ __forceinline__ bool hm(int q, int64_t i, int64_t j, int64_t k) {
+    return q == 0 ? (j > 0 && k > 0) : q == 1 ? (i > 0 && k > 0) : (i > 0 && j > 0);
+}
+
+// ---------------------------------------------------------------------------
+// 1. transpose of cpml_h on one axis: lpsi_h <- b*mu, w_h <- adjoint of d
+//    (mu = lpsi + sigma*0.5*lH_target).  Invalid elements get w = 0.
+//    psi order per axis: x (hyx, hzx), y (hzy, hxy), z (hxz, hyz); sigma (+, -)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void adj_psi(float &lpsi, float &w, float lt, float coef, int sigma, float b, float a,
+                                        float km1) {
+    const float h = fmul(coef, lt);
+    const float mu = sigma > 0 ? fadd(lpsi, h) : fsub(lpsi, h);
+    lpsi = fmul(b, mu);
+    const float t = fmul(km1, h);
+    w = fadd(sigma > 0 ? t : -t, fmul(a, mu));
+}
+
+template <int AX>
+__global__ void __launch_bounds__(kB) k_adj_hpsi(Args A) {
+    const Grid &g = A.g;
+    const int P = A.P[AX];
+    int64_t i, j, k, s, p;
+    if (AX == 0) {
+        k = (int64_t)blockIdx.x * kB + threadIdx.x; j = blockIdx.y; s = blockIdx.z;
+        if (k >= g.nz) return;
+        i = slab_node_h(s, P, g.nx);
+        p = px(g, s, j, k);
+    } else if (AX == 1) {
+        k = (int64_t)blockIdx.x * kB + threadIdx.x; s = blockIdx.y; i = blockIdx.z;
+        if (k >= g.nz) return;
+        j = slab_node_h(s, P, g.ny);
+        p = py(g, P, i, s, k);
+    } else {
+        const int64_t t = (int64_t)blockIdx.x * kB + threadIdx.x;
+        if (t >= g.nx * g.ny * 2 * P) return;
+        s = t % (2 * P); j = (t / (2 * P)) % g.ny; i = t / (2 * P * g.ny);
+        k = slab_node_h(s, P, g.nz);
+        p = t;
+    }
+    if (!(s < P ? A.front[AX] : A.back[AX])) return;
+    const int64_t c = i * g.sx + j * g.sy + k;
+    const float b = A.bh[AX][s], a = A.ah[AX][s], km1 = A.kh[AX][s];
+    // (target H component, validity) of psi1 / psi2 on this axis
+    const int t1 = AX == 0 ? 1 : AX == 1 ? 2 : 0;   // hy, hz, hx
+    const int t2 = AX == 0 ? 2 : AX == 1 ? 0 : 1;   // hz, hx, hy
+    const bool v1 = AX == 0 ? k > 0 : AX == 1 ? i > 0 : j > 0;
+    const bool v2 = AX == 0 ? j > 0 : AX == 1 ? k > 0 : i > 0;
+    float *lp1 = A.lph[2 * AX], *lp2 = A.lph[2 * AX + 1];
+    float *w1 = A.wh[2 * AX], *w2 = A.wh[2 * AX + 1];
+    if (v1) {
+        float l = lp1[p], w;
+        adj_psi(l, w, A.lf[3 + t1][c], 0.5f, +1, b, a, km1);
+        lp1[p] = l;
+        w1[p] = w;
+    } else {
+        w1[p] = 0.f;
+    }
+    if (v2) {
+        float l = lp2[p], w;
+        adj_psi(l, w, A.lf[3 + t2][c], 0.5f, -1, b, a, km1);
+        lp2[p] = l;
+        w2[p] = w;
+    } else {
+        w2[p] = 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. reverse H part on E cells + gradient.  One thread per cell.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kB) k_adj_e(Args A) {
+    const Grid &g = A.g;
+    const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
+    const int64_t j = blockIdx.y, i = blockIdx.z;
+    if (k >= g.nz) return;
+    const int64_t c = i * g.sx + j * g.sy + k;
+    const float *lhx = A.lf[3], *lhy = A.lf[4], *lhz = A.lf[5];
+    const float *hx = A.hp[0], *hy = A.hp[1], *hz = A.hp[2];
+    // masked adjoint H reads
+    auto LH = [&](int q, const float *f, int64_t di, int64_t dj, int64_t dk) {
+        const int64_t ii = i + di, jj = j + dj, kk = k + dk;
+        return hm(q, ii, jj, kk) ? f[c + di * g.sx + dj * g.sy + dk] : 0.f;
+    };
+    // slab indices of this cell's nodes (H-node form for the w_h gather,
+    // E-node form for the gradient's psi terms)
+    const int sxh0 = slab_of_h(i, A.P[0], g.nx, A.front[0], A.back[0]);
+    const int sxh1 = slab_of_h(i + 1, A.P[0], g.nx, A.front[0], A.back[0]);
+    const int syh0 = slab_of_h(j, A.P[1], g.ny, A.front[1], A.back[1]);
+    const int syh1 = slab_of_h(j + 1, A.P[1], g.ny, A.front[1], A.back[1]);
+    const int szh0 = slab_of_h(k, A.P[2], g.nz, A.front[2], A.back[2]);
+    const int szh1 = slab_of_h(k + 1, A.P[2], g.nz, A.front[2], A.back[2]);
+    const int sxe = slab_of_e(i, A.P[0], g.nx, A.front[0], A.back[0]);
+    const int sye = slab_of_e(j, A.P[1], g.ny, A.front[1], A.back[1]);
+    const int sze = slab_of_e(k, A.P[2], g.nz, A.front[2], A.back[2]);
+    const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
+
+    // ex: E source of hzy (y axis, psi 0 of h) and hyz (z axis, psi 1 of h)
+    if (em(g, 0, i, j, k)) {
+        float d = fmul(-0.5f, curl4(LH(2, lhz, 0, 1, 0), LH(2, lhz, 0, 0, 0), LH(1, lhy, 0, 0, 1), LH(1, lhy, 0, 0, 0)));
+        if (syh0 >= 0) d = fadd(d, A.wh[2][py(g, Py, i, syh0, k)]);
+        if (syh1 >= 0) d = fsub(d, A.wh[2][py(g, Py, i, syh1, k)]);
+        if (szh0 >= 0) d = fadd(d, A.wh[5][pz(g, Pz, i, j, szh0)]);
+        if (szh1 >= 0) d = fsub(d, A.wh[5][pz(g, Pz, i, j, szh1)]);
+        const float l = fadd(A.lf[0][c], d);
+        A.lf[0][c] = l;
+        // G = curl_f(H) + (exy: +) + (exz: -)
+        float G = curl4(hz[c + g.sy], hz[c], hy[c + 1], hy[c]);
+        if (sye >= 0) {
+            const float dd = fsub(hz[c + g.sy], hz[c]);
+            G = fadd(G, fadd(fmul(A.ke[1][sye], dd), A.pe[3][py(g, Py, i, sye, k)]));
+        }
+        if (sze >= 0) {
+            const float dd = fsub(hy[c + 1], hy[c]);
+            G = fsub(G, fadd(fmul(A.ke[2][sze], dd), A.pe[4][pz(g, Pz, i, j, sze)]));
+        }
+        A.gce[0][c] = fadd(A.gce[0][c], fmul(l, G));
+    }
+    // ey: E source of hzx (x axis, psi 1) and hxz (z axis, psi 0)
+    if (em(g, 1, i, j, k)) {
+        float d = fmul(-0.5f, curl4(LH(0, lhx, 0, 0, 1), LH(0, lhx, 0, 0, 0), LH(2, lhz, 1, 0, 0), LH(2, lhz, 0, 0, 0)));
+        if (sxh0 >= 0) d = fadd(d, A.wh[1][px(g, sxh0, j, k)]);
+        if (sxh1 >= 0) d = fsub(d, A.wh[1][px(g, sxh1, j, k)]);
+        if (szh0 >= 0) d = fadd(d, A.wh[4][pz(g, Pz, i, j, szh0)]);
+        if (szh1 >= 0) d = fsub(d, A.wh[4][pz(g, Pz, i, j, szh1)]);
+        const float l = fadd(A.lf[1][c], d);
+        A.lf[1][c] = l;
+        // G = curl_f(H) + (eyx: -) + (eyz: +)
+        float G = curl4(hx[c + 1], hx[c], hz[c + g.sx], hz[c]);
+        if (sxe >= 0) {
+            const float dd = fsub(hz[c + g.sx], hz[c]);
+            G = fsub(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[0][px(g, sxe, j, k)]));
+        }
+        if (sze >= 0) {
+            const float dd = fsub(hx[c + 1], hx[c]);
+            G = fadd(G, fadd(fmul(A.ke[2][sze], dd), A.pe[5][pz(g, Pz, i, j, sze)]));
+        }
+        A.gce[1][c] = fadd(A.gce[1][c], fmul(l, G));
+    }
+    // ez: E source of hyx (x axis, psi 0) and hxy (y axis, psi 1)
+    if (em(g, 2, i, j, k)) {
+        float d = fmul(-0.5f, curl4(LH(1, lhy, 1, 0, 0), LH(1, lhy, 0, 0, 0), LH(0, lhx, 0, 1, 0), LH(0, lhx, 0, 0, 0)));
+        if (sxh0 >= 0) d = fadd(d, A.wh[0][px(g, sxh0, j, k)]);
+        if (sxh1 >= 0) d = fsub(d, A.wh[0][px(g, sxh1, j, k)]);
+        if (syh0 >= 0) d = fadd(d, A.wh[3][py(g, Py, i, syh0, k)]);
+        if (syh1 >= 0) d = fsub(d, A.wh[3][py(g, Py, i, syh1, k)]);
+        const float l = fadd(A.lf[2][c], d);
+        A.lf[2][c] = l;
+        // G = curl_f(H) + (ezx: +) + (ezy: -)
+        float G = curl4(hy[c + g.sx], hy[c], hx[c + g.sy], hx[c]);
+        if (sxe >= 0) {
+            const float dd = fsub(hy[c + g.sx], hy[c]);
+            G = fadd(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[1][px(g, sxe, j, k)]));
+        }
+        if (sye >= 0) {
+            const float dd = fsub(hx[c + g.sy], hx[c]);
+            G = fsub(G, fadd(fmul(A.ke[1][sye], dd), A.pe[2][py(g, Py, i, sye, k)]));
+        }
+        A.gce[2][c] = fadd(A.gce[2][c], fmul(l, G));
+    }
+    (void)Px;
+}
+
+// ---------------------------------------------------------------------------
+// 3. transpose of cpml_e on one axis: nu = CE*lE_target, mu = lpsi + sigma*nu,
+//    lpsi_e <- b*mu, w_e <- sigma*km1*nu + a*mu.
+//    psi order per axis: x (eyx -, ezx +), y (ezy -, exy +), z (exz -, eyz +)
+// ---------------------------------------------------------------------------
+template <int AX>
+__global__ void __launch_bounds__(kB) k_adj_epsi(Args A) {
+    const Grid &g = A.g;
+    const int P = A.P[AX];
+    int64_t i, j, k, s, p;
+    if (AX == 0) {
+        k = (int64_t)blockIdx.x * kB + threadIdx.x; j = blockIdx.y; s = blockIdx.z;
+        if (k >= g.nz) return;
+        i = slab_node_e(s, P, g.nx);
+        p = px(g, s, j, k);
+    } else if (AX == 1) {
+        k = (int64_t)blockIdx.x * kB + threadIdx.x; s = blockIdx.y; i = blockIdx.z;
+        if (k >= g.nz) return;
+        j = slab_node_e(s, P, g.ny);
+        p = py(g, P, i, s, k);
+    } else {
+        const int64_t t = (int64_t)blockIdx.x * kB + threadIdx.x;
+        if (t >= g.nx * g.ny * 2 * P) return;
+        s = t % (2 * P); j = (t / (2 * P)) % g.ny; i = t / (2 * P * g.ny);
+        k = slab_node_e(s, P, g.nz);
+        p = t;
+    }
+    if (!(s < P ? A.front[AX] : A.back[AX])) return;
+    const int64_t c = i * g.sx + j * g.sy + k;
+    const float b = A.be[AX][s], a = A.ae[AX][s], km1 = A.ke[AX][s];
+    const int t1 = AX == 0 ? 1 : AX == 1 ? 2 : 0;   // ey, ez, ex
+    const int t2 = AX == 0 ? 2 : AX == 1 ? 0 : 1;   // ez, ex, ey
+    const bool v1 = AX == 0 ? k < g.nz - 1 : AX == 1 ? i < g.nx - 1 : j < g.ny - 1;
+    const bool v2 = AX == 0 ? j < g.ny - 1 : AX == 1 ? k < g.nz - 1 : i < g.nx - 1;
+    float *lp1 = A.lpe[2 * AX], *lp2 = A.lpe[2 * AX + 1];
+    float *w1 = A.we[2 * AX], *w2 = A.we[2 * AX + 1];
+    if (v1) {
+        float l = lp1[p], w;
+        adj_psi(l, w, A.lf[t1][c], A.ce[t1][c], -1, b, a, km1);
+        lp1[p] = l;
+        w1[p] = w;
+    } else {
+        w1[p] = 0.f;
+    }
+    if (v2) {
+        float l = lp2[p], w;
+        adj_psi(l, w, A.lf[t2][c], A.ce[t2][c], +1, b, a, km1);
+        lp2[p] = l;
+        w2[p] = w;
+    } else {
+        w2[p] = 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. reverse E part on H cells: lH += curl_b(CE*lE) + scatter of w_e.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kB) k_adj_h(Args A) {
+    const Grid &g = A.g;
+    const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
+    const int64_t j = blockIdx.y, i = blockIdx.z;
+    if (k >= g.nz) return;
+    const int64_t c = i * g.sx + j * g.sy + k;
+    auto NU = [&](int q, int64_t di, int64_t dj, int64_t dk) {
+        const int64_t ii = i + di, jj = j + dj, kk = k + dk;
+        const int64_t cc = c + di * g.sx + dj * g.sy + dk;
+        return em(g, q, ii, jj, kk) ? fmul(A.ce[q][cc], A.lf[q][cc]) : 0.f;
+    };
+    const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
+    // E-node slabs at this index and one below (H cell h: +w at node h-1, -w at node h)
+    const int sx0 = slab_of_e(i - 1, Px, g.nx, A.front[0], A.back[0]);
+    const int sx1 = slab_of_e(i, Px, g.nx, A.front[0], A.back[0]);
+    const int sy0 = slab_of_e(j - 1, Py, g.ny, A.front[1], A.back[1]);
+    const int sy1 = slab_of_e(j, Py, g.ny, A.front[1], A.back[1]);
+    const int sz0 = slab_of_e(k - 1, Pz, g.nz, A.front[2], A.back[2]);
+    const int sz1 = slab_of_e(k, Pz, g.nz, A.front[2], A.back[2]);
+    // hx: H source of ezy (y axis, psi 0 of e) and eyz (z axis, psi 1)
+    if (hm(0, i, j, k)) {
+        float d = curl4(NU(2, 0, 0, 0), NU(2, 0, -1, 0), NU(1, 0, 0, 0), NU(1, 0, 0, -1));
+        if (sy0 >= 0) d = fadd(d, A.we[2][py(g, Py, i, sy0, k)]);
+        if (sy1 >= 0) d = fsub(d, A.we[2][py(g, Py, i, sy1, k)]);
+        if (sz0 >= 0) d = fadd(d, A.we[5][pz(g, Pz, i, j, sz0)]);
+        if (sz1 >= 0) d = fsub(d, A.we[5][pz(g, Pz, i, j, sz1)]);
+        A.lf[3][c] = fadd(A.lf[3][c], d);
+    }
+    // hy: H source of ezx (x axis, psi 1) and exz (z axis, psi 0)
+    if (hm(1, i, j, k)) {
+        float d = curl4(NU(0, 0, 0, 0), NU(0, 0, 0, -1), NU(2, 0, 0, 0), NU(2, -1, 0, 0));
+        if (sx0 >= 0) d = fadd(d, A.we[1][px(g, sx0, j, k)]);
+        if (sx1 >= 0) d = fsub(d, A.we[1][px(g, sx1, j, k)]);
+        if (sz0 >= 0) d = fadd(d, A.we[4][pz(g, Pz, i, j, sz0)]);
+        if (sz1 >= 0) d = fsub(d, A.we[4][pz(g, Pz, i, j, sz1)]);
+        A.lf[4][c] = fadd(A.lf[4][c], d);
+    }
+    // hz: H source of eyx (x axis, psi 0) and exy (y axis, psi 1)
+    if (hm(2, i, j, k)) {
+        float d = curl4(NU(1, 0, 0, 0), NU(1, -1, 0, 0), NU(0, 0, 0, 0), NU(0, 0, -1, 0));
+        if (sx0 >= 0) d = fadd(d, A.we[0][px(g, sx0, j, k)]);
+        if (sx1 >= 0) d = fsub(d, A.we[0][px(g, sx1, j, k)]);
+        if (sy0 >= 0) d = fadd(d, A.we[3][py(g, Py, i, sy0, k)]);
+        if (sy1 >= 0) d = fsub(d, A.we[3][py(g, Py, i, sy1, k)]);
+        A.lf[5][c] = fadd(A.lf[5][c], d);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// point lists: gather (monitors) and add (adjoint injection), list order
+// ---------------------------------------------------------------------------
+// cell offset of point p, or -1 when the point or its component is out of range
+__device__ __forceinline__ int64_t point_offset(const Grid &g, const fdtd_points &pts, int p) {
+    const int64_t i = pts.ijk[3 * p], j = pts.ijk[3 * p + 1], k = pts.ijk[3 * p + 2];
+    const int q = pts.comp[p];
+    if (i < 0 || i >= g.nx || j < 0 || j >= g.ny || k < 0 || k >= g.nz || q < 0 || q > 5) return -1;
+    return i * g.sx + j * g.sy + k;
+}
+
+// out-of-range points read as NaN
+__global__ void k_gather_points(Grid g, fdtd_points pts, fdtd_fields6 f, float *out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pts.n) return;
+    const int64_t c = point_offset(g, pts, p);
+    out[p] = c >= 0 ? f.f[pts.comp[p]][c] : __int_as_float(0x7fc00000);
+}
+
+// one thread walks the list so repeated points add in list order;
+// out-of-range points are skipped
+__global__ void k_add_points(Grid g, fdtd_points pts, fdtd_fields6 f, const float *vals) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int p = 0; p < pts.n; p++) {
+        const int64_t c = point_offset(g, pts, p);
+        if (c < 0) continue;
+        float *fp = f.f[pts.comp[p]] + c;
+        *fp = fadd(*fp, vals[p]);
+    }
+}
+
+static dim3 cells(const Grid &g) {
+    return dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)g.ny, (unsigned)g.nx);
+}
+
+template <int AX>
+static void launch_slab(const Grid &g, int P, bool e, const Args &A, cudaStream_t st) {
+    dim3 grid;
+    if (AX == 0) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)g.ny, (unsigned)(2 * P));
+    else if (AX == 1) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)(2 * P), (unsigned)g.nx);
+    else grid = dim3((unsigned)((g.nx * g.ny * 2 * P + kB - 1) / kB));
+    if (e) k_adj_epsi<AX><<<grid, kB, 0, st>>>(A);
+    else k_adj_hpsi<AX><<<grid, kB, 0, st>>>(A);
+}
+
+static int validate_points(const Grid &g, const fdtd_points *pts) {
+    if (!pts || pts->n < 0) return FDTD_ERR_ARG;
+    if (pts->n > 0 && !all_nonnull(pts->ijk, pts->comp)) return FDTD_ERR_ARG;
+    (void)g;
+    return FDTD_OK;
+}
+
+}  // namespace adj
+}  // namespace fdtd
+
+using namespace fdtd;
+using namespace fdtd::adj;
+
+extern "C" {
+
+int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
+                          const float *const h_prev[3], const float *const psi_e_cur[6], const float *const ce[3],
+                          const fdtd_points *mon, const float *mon_grad, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!s || !h_prev || !ce) return FDTD_ERR_ARG;
+    for (int q = 0; q < 6; q++)
+        if (!s->lf[q]) return FDTD_ERR_ARG;
+    for (int q = 0; q < 3; q++)
+        if (!all_nonnull(s->grad_ce[q], h_prev[q], ce[q])) return FDTD_ERR_ARG;
+    Args A{};
+    A.g = g;
+    const int64_t n[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; a++) {
+        const int P = cp ? cp->npml[a] : 0;
+        if (P < 0) return FDTD_ERR_ARG;
+        A.P[a] = P;
+        A.front[a] = cp ? (cp->faces >> (2 * a)) & 1 : 0;
+        A.back[a] = cp ? (cp->faces >> (2 * a + 1)) & 1 : 0;
+        if (P == 0) continue;
+        if (n[a] < 2 * P + 2) return FDTD_ERR_SHAPE;
+        if (a < 2 && 2 * P > 65535) return FDTD_ERR_SHAPE;
+        if (!psi_e_cur) return FDTD_ERR_ARG;
+        if (!all_nonnull(cp->b_e[a], cp->a_e[a], cp->km1_e[a], cp->b_h[a], cp->a_h[a], cp->km1_h[a]))
+            return FDTD_ERR_ARG;
+        for (int q = 2 * a; q < 2 * a + 2; q++)
+            if (!all_nonnull(s->lpsi_e[q], s->lpsi_h[q], s->w_e[q], s->w_h[q], psi_e_cur[q])) return FDTD_ERR_ARG;
+        A.be[a] = cp->b_e[a]; A.ae[a] = cp->a_e[a]; A.ke[a] = cp->km1_e[a];
+        A.bh[a] = cp->b_h[a]; A.ah[a] = cp->a_h[a]; A.kh[a] = cp->km1_h[a];
+    }
+    for (int q = 0; q < 6; q++) {
+        A.lf[q] = s->lf[q];
+        A.lpe[q] = s->lpsi_e[q];
+        A.lph[q] = s->lpsi_h[q];
+        A.we[q] = s->w_e[q];
+        A.wh[q] = s->w_h[q];
+        A.pe[q] = psi_e_cur ? psi_e_cur[q] : nullptr;
+    }
+    for (int q = 0; q < 3; q++) {
+        A.gce[q] = s->grad_ce[q];
+        A.hp[q] = h_prev[q];
+        A.ce[q] = ce[q];
+    }
+    cudaStream_t st = as_stream(stream);
+    if (mon && mon->n > 0) {
+        FDTD_TRY(validate_points(g, mon));
+        if (!mon_grad) return FDTD_ERR_ARG;
+        fdtd_fields6 lf;
+        for (int q = 0; q < 6; q++) lf.f[q] = s->lf[q];
+        k_add_points<<<1, 32, 0, st>>>(g, *mon, lf, mon_grad);
+    }
+    if (A.P[0]) launch_slab<0>(g, A.P[0], false, A, st);
+    if (A.P[1]) launch_slab<1>(g, A.P[1], false, A, st);
+    if (A.P[2]) launch_slab<2>(g, A.P[2], false, A, st);
+    k_adj_e<<<cells(g), kB, 0, st>>>(A);
+    if (A.P[0]) launch_slab<0>(g, A.P[0], true, A, st);
+    if (A.P[1]) launch_slab<1>(g, A.P[1], true, A, st);
+    if (A.P[2]) launch_slab<2>(g, A.P[2], true, A, st);
+    k_adj_h<<<cells(g), kB, 0, st>>>(A);
+    return check_launch();
+}
+
+int fdtd_gather_points_f32(const fdtd_grid *gp, const fdtd_points *pts, const float *const f[6], float *out,
+                           void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    FDTD_TRY(validate_points(g, pts));
+    if (pts->n == 0) return FDTD_OK;
+    if (!f || !out) return FDTD_ERR_ARG;
+    fdtd_fields6 ff;
+    for (int q = 0; q < 6; q++) ff.f[q] = const_cast<float *>(f[q]);
+    k_gather_points<<<(pts->n + 127) / 128, 128, 0, as_stream(stream)>>>(g, *pts, ff, out);
+    return check_launch();
+}
+
+int fdtd_add_points_f32(const fdtd_grid *gp, const fdtd_points *pts, float *const f[6], const float *vals,
+                        void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    FDTD_TRY(validate_points(g, pts));
+    if (pts->n == 0) return FDTD_OK;
+    if (!f || !vals) return FDTD_ERR_ARG;
+    fdtd_fields6 ff;
+    for (int q = 0; q < 6; q++) ff.f[q] = f[q];
+    k_add_points<<<1, 32, 0, as_stream(stream)>>>(g, *pts, ff, vals);
+    return check_launch();
+}
+
+}  // extern "C"

@@ -12,7 +12,7 @@
 //  * The state lives in two buffers (ping-pong): a step reads buffer `cur`
 //    and writes buffer `1-cur`.  E-psi slabs are ping-ponged too; H-psi is
 //    updated in place (only its owner touches it).
-//  * A CTA owns a tile of TZ=32 (z) x TY (y) cells for a chunk of x planes
+//  * A CTA owns a tile of TZ=64 (z) x TY (y) cells for a chunk of x planes
 //    and marches along x.  For plane i it needs H(i), H(i+1), E(i), CE(i)
 //    with a one-cell halo at j0-1 / k0-1 (and j0+TY / k0+TZ for H).  These
 //    arrive by 3-D TMA box loads (cp.async.bulk.tensor) into a ring of NS
@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -40,7 +41,8 @@ constexpr int TZ = 64;
 constexpr int HC = TZ + 8;   // H box:    k0-4 .. k0+TZ+3 (needs k0-1 .. k0+TZ)
 constexpr int EC = TZ + 4;   // E/CE box: k0-4 .. k0+TZ-1 (needs k0-1 .. k0+TZ-1)
 constexpr int NCW = TZ + 4;  // E_new row stride; column c holds k = k0-2+c
-constexpr int MAX_LOCAL_SRC = 16;
+constexpr int MAX_LOCAL_SRC = 128;
+constexpr int MAX_BAND_SRC = 32;
 constexpr uint64_t WAIT_NS = 1000000000ull;  // a wait gives up after 1 s
 
 constexpr int al128(int b) { return (b + 127) / 128 * 128; }
@@ -95,6 +97,14 @@ struct Params {
     int32_t stage_bytes;  // bytes per pipeline stage (fields + z-psi boxes)
     int32_t zbox;         // bytes per z-psi box in shared memory (128-aligned)
     uint32_t tx_z;        // bytes the 4 z-psi boxes deliver
+    // z band (1 when the z-slab CPML is finished by the band kernels): the
+    // fused kernel then leaves the E z-psi correction, sources on E z-slab
+    // nodes and every H cell of the band (k in [1, P+1], [n-P-1, n-1]) to them
+    int32_t zfix;
+    const float *in[6];   // input buffer fields (read by the band kernels)
+    const float *in_ce[3];
+    int32_t nbsrc;        // sources on E z-slab nodes (applied by the E band kernel)
+    int32_t bsrc[MAX_BAND_SRC];
 };
 
 // Many independent grids advanced by one launch: work items of all grids are
@@ -182,6 +192,13 @@ __device__ __forceinline__ int slab_h(int64_t idx, int P, int64_t n, int front, 
     return -1;
 }
 
+// H cells whose update reads an E z-slab node or that carry a z psi:
+// k in [1, P+1] (front) or [n-P-1, n-1] (back)
+__device__ __forceinline__ bool in_zband_h(int64_t k, int P, int64_t n, int front, int back) {
+    if (P <= 0) return false;
+    return (front && k >= 1 && k <= P + 1) || (back && k >= n - P - 1 && k <= n - 1);
+}
+
 __device__ __forceinline__ float cpml_corr(float &psi, float b, float a, float km1, float d) {
     psi = fadd(fmul(b, psi), fmul(a, d));
     return fadd(fmul(km1, d), psi);
@@ -252,8 +269,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
 
     __shared__ int s_abort;
     __shared__ int s_nls;
-    __shared__ int s_ls_i[MAX_LOCAL_SRC], s_ls_j[MAX_LOCAL_SRC], s_ls_k[MAX_LOCAL_SRC];
-    __shared__ int s_ls_comp[MAX_LOCAL_SRC], s_ls_s[MAX_LOCAL_SRC];
+    // sources of the current work item, list order: (i << 16 | j), (k << 2 | comp), list index
+    __shared__ uint32_t s_ls_ij[MAX_LOCAL_SRC];
+    __shared__ int s_ls_kc[MAX_LOCAL_SRC], s_ls_s[MAX_LOCAL_SRC];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // Roles.  E phase: warps 0..TY-1 -> own row r = warp+1 (j = j0+warp), pair
@@ -385,11 +403,13 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const int64_t nplanes = x1 - i_start + 1;  // planes i_start .. x1 (H(x1) feeds E(x1-1))
         // Tile-uniform: no grid edge and no y/z CPML slab inside the tile's E/H region.
         // tile's E (k0-1..k0+TZ-1) or H (k0..k0+TZ-1) columns touch a z slab
-        const bool ztile = P2 > 0 && ((front2 && k0 - 1 <= P2) || (back2 && k0 + TZ - 1 >= nz - P2 - 1));
+        // with the band kernels the z slab is not this kernel's work (P2k = 0)
+        const int P2k = p.zfix ? 0 : P2;
+        const bool ztile = P2k > 0 && ((front2 && k0 - 1 <= P2k) || (back2 && k0 + TZ - 1 >= nz - P2k - 1));
         const bool zstage = ztile && p.zpsi;
         const bool yz_plain = j0 >= 1 && j0 + TY <= ny - 1 && k0 >= 1 && k0 + TZ <= nz - 1 &&
                               (P1 == 0 || ((j0 - 1 > P1 || !front1) && (j0 + TY - 1 < ny - P1 - 1 || !back1))) &&
-                              (P2 == 0 || ((k0 - 1 > P2 || !front2) && (k0 + TZ - 1 < nz - P2 - 1 || !back2)));
+                              (P2k == 0 || ((k0 - 1 > P2k || !front2) && (k0 + TZ - 1 < nz - P2k - 1 || !back2)));
 
         // ---- per-item, per-thread cell description (pair at row j, columns k, k+1) ----
         const int64_t jj = j0 - 1 + er, kk = k0 + eko;
@@ -399,10 +419,13 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const bool k0_lt = kk < nz - 1, k1_lt = kk + 1 < nz - 1, k0_gt = kk > 0, k1_gt = kk + 1 > 0;
         const int sye = row_in ? slab_e(jj, P1, ny, front1, back1) : -1;
         const int syh = row_in ? slab_h(jj, P1, ny, front1, back1) : -1;
-        const int sze0 = in0 ? slab_e(kk, P2, nz, front2, back2) : -1;
-        const int sze1 = in1 ? slab_e(kk + 1, P2, nz, front2, back2) : -1;
-        const int szh0 = in0 ? slab_h(kk, P2, nz, front2, back2) : -1;
-        const int szh1 = in1 ? slab_h(kk + 1, P2, nz, front2, back2) : -1;
+        const int sze0 = in0 ? slab_e(kk, P2k, nz, front2, back2) : -1;
+        const int sze1 = in1 ? slab_e(kk + 1, P2k, nz, front2, back2) : -1;
+        const int szh0 = in0 ? slab_h(kk, P2k, nz, front2, back2) : -1;
+        const int szh1 = in1 ? slab_h(kk + 1, P2k, nz, front2, back2) : -1;
+        // H cells of the z band: left to the band kernel (no psi_h update here)
+        const bool hb0 = p.zfix && in_zband_h(kk, P2, nz, front2, back2);
+        const bool hb1 = p.zfix && in_zband_h(kk + 1, P2, nz, front2, back2);
 
         auto issue = [&](int64_t q) {
             const int64_t plane = i_start + q;
@@ -429,17 +452,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         };
 
         if (tid == 0) {
-            // sources inside the extended region of this work item
+            // sources inside the extended region of this work item, in list
+            // order (one thread: a warp-wide scan costs the kernel registers)
             int n = 0;
             if (p.t >= 0 && p.t < p.namp) {
                 for (int s = 0; s < p.nsrc; s++) {
                     const int64_t si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
-                    if (si >= i_start && si < x1 && sj >= j0 - 1 && sj < j0 + TY && sk >= k0 - 1 && sk < k0 + TZ) {
+                    if (si >= i_start && si < x1 && sj >= j0 - 1 && sj < j0 + TY && sk >= k0 - 1 && sk < k0 + TZ &&
+                        !(p.zfix && slab_e(sk, P2, nz, front2, back2) >= 0)) {
                         if (n < MAX_LOCAL_SRC) {
-                            s_ls_i[n] = (int)si;
-                            s_ls_j[n] = (int)sj;
-                            s_ls_k[n] = (int)sk;
-                            s_ls_comp[n] = p.src_comp[s];
+                            s_ls_ij[n] = ((uint32_t)si << 16) | (uint32_t)sj;
+                            s_ls_kc[n] = (int)(sk << 2) | p.src_comp[s];
                             s_ls_s[n] = s;
                         }
                         n++;
@@ -572,14 +595,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             set(ey, e, fadd(get(ey, e), fmul(get(cey, e), tc)));
                         }
                     }
+                    const uint32_t ij_here = ((uint32_t)i << 16) | (uint32_t)jj;
                     for (int s = 0; s < nls; s++) {  // soft sources, list order
-                        if (s_ls_i[s] != i || s_ls_j[s] != jj) continue;
-                        const int64_t sk = s_ls_k[s];
+                        if (s_ls_ij[s] != ij_here) continue;
+                        const int kc = s_ls_kc[s];
+                        const int64_t sk = kc >> 2;
                         if (sk != kk && sk != kk + 1) continue;
                         const int e = (int)(sk - kk);
                         const float v = p.src_amp[(int64_t)s_ls_s[s] * p.namp + p.t];
-                        if (s_ls_comp[s] == 0) set(ex, e, fadd(get(ex, e), v));
-                        else if (s_ls_comp[s] == 1) set(ey, e, fadd(get(ey, e), v));
+                        const int comp = kc & 3;
+                        if (comp == 0) set(ex, e, fadd(get(ex, e), v));
+                        else if (comp == 1) set(ey, e, fadd(get(ey, e), v));
                         else set(ez, e, fadd(get(ez, e), v));
                     }
                 }
@@ -619,7 +645,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             const int64_t qb = ((int64_t)sxh * ny + jj) * nz + kk;
 #pragma unroll
                             for (int e = 0; e < 2; e++) {
-                                if (!(e ? in1 : in0)) continue;
+                                if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (e ? k1_gt : k0_gt) {
                                     float psi = p.psi_h[0][qb + e];
                                     const float tc = corr(psi, c, fsub(get(oez, e), get(prev_ez, e)));
@@ -639,7 +665,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             const int64_t qb = (i * 2 * P1 + syh) * nz + kk;
 #pragma unroll
                             for (int e = 0; e < 2; e++) {
-                                if (!(e ? in1 : in0)) continue;
+                                if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (i_gt) {
                                     float psi = p.psi_h[2][qb + e];
                                     const float tc = corr(psi, cyh, fsub(get(oex, e), get(ex_jm, e)));
@@ -717,6 +743,144 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     }
 }
 #undef FDTD_SB
+
+// ---------------------------------------------------------------------------
+// z band kernels (single-grid plans).  The fused kernel treats z-slab tiles
+// like interior tiles; these two kernels then finish the band in the same
+// operation order as the in-kernel path (and the reference's cpml_e/cpml_h):
+//   E: on E z-slab nodes, psi_e(z) update and E correction, then the sources
+//      on those cells (list order);
+//   H: on k in [1, P+1] and [n-P-1, n-1], H recomputed from the input buffer
+//      and the final E with its x, y and z CPML terms (x/y psi_h were left
+//      untouched there by the fused kernel).
+// One thread per cell; z is the fastest index inside each band.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ Coef gcoef(const float *b, const float *a, const float *k, int s) {
+    return Coef{b[s], a[s], k[s]};
+}
+
+__global__ void __launch_bounds__(128) k_zband_e(const __grid_constant__ Params p) {
+    const int P = p.P[2];
+    const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
+    const int nf = front ? P : 0, nb = back ? P : 0, nk = nf + nb;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nx * p.ny * nk) return;
+    const int kb = (int)(t % nk);
+    const int64_t j = (t / nk) % p.ny, i = t / ((int64_t)nk * p.ny);
+    const int64_t k = kb < nf ? 1 + kb : p.nz - P - 1 + (kb - nf);
+    const int sz = kb < nf ? kb : P + (kb - nf);
+    const int64_t c = i * p.sx + j * p.sy + k, qz = (i * p.ny + j) * 2 * P + sz;
+    const Coef cf = gcoef(p.tb_e[2], p.ta_e[2], p.tk_e[2], sz);
+    const float *hx = p.in[3], *hy = p.in[4];
+    if (j < p.ny - 1) {  // ex -= cex (..dHy/dz..)
+        float psi = p.psi_e_in[4][qz];
+        const float tc = corr(psi, cf, fsub(hy[c + 1], hy[c]));
+        p.psi_e_out[4][qz] = psi;
+        float *ex = p.out[0] + c;
+        *ex = fsub(*ex, fmul(p.in_ce[0][c], tc));
+    }
+    if (i < p.nx - 1) {  // ey += cey (..dHx/dz..)
+        float psi = p.psi_e_in[5][qz];
+        const float tc = corr(psi, cf, fsub(hx[c + 1], hx[c]));
+        p.psi_e_out[5][qz] = psi;
+        float *ey = p.out[1] + c;
+        *ey = fadd(*ey, fmul(p.in_ce[1][c], tc));
+    }
+    if (p.t >= 0 && p.t < p.namp)
+        for (int b = 0; b < p.nbsrc; b++) {  // sources on this cell, list order
+            const int s = p.bsrc[b];
+            if (p.src_ijk[3 * s] != i || p.src_ijk[3 * s + 1] != j || p.src_ijk[3 * s + 2] != k) continue;
+            float *f = p.out[p.src_comp[s]] + c;
+            *f = fadd(*f, p.src_amp[(int64_t)s * p.namp + p.t]);
+        }
+}
+
+__global__ void __launch_bounds__(128) k_zband_h(const __grid_constant__ Params p) {
+    const int P = p.P[2];
+    const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
+    const int64_t nz = p.nz, ny = p.ny, nx = p.nx;
+    const int64_t fend = front ? P + 1 : 0;                       // front band: k = 1 .. fend
+    const int64_t bstart = back ? max(nz - P - 1, fend + 1) : nz;  // back band: k = bstart .. nz-1
+    const int nf = (int)fend, nk = nf + (int)(nz - bstart);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nx * ny * nk) return;
+    const int kb = (int)(t % nk);
+    const int64_t j = (t / nk) % ny, i = t / ((int64_t)nk * ny);
+    const int64_t k = kb < nf ? 1 + kb : bstart + (kb - nf);
+    const int64_t c = i * p.sx + j * p.sy + k;
+    const float *ex = p.out[0], *ey = p.out[1], *ez = p.out[2];
+    const int f0 = p.faces & 1, b0 = (p.faces >> 1) & 1, f1 = (p.faces >> 2) & 1, b1 = (p.faces >> 3) & 1;
+    const int sxh = slab_h(i, p.P[0], nx, f0, b0), syh = slab_h(j, p.P[1], ny, f1, b1);
+    const int szh = slab_h(k, P, nz, front, back);
+    const int P0 = p.P[0], P1 = p.P[1];
+    // hx: curl, y slab (hx -=), z slab (hx +=)
+    {
+        float h = p.in[3][c];
+        if (j > 0 && k > 0) {
+            h = fsub(h, fmul(0.5f, curl4(ez[c], ez[c - p.sy], ey[c], ey[c - 1])));
+            if (syh >= 0) {
+                const int64_t q = (i * 2 * P1 + syh) * nz + k;
+                float psi = p.psi_h[3][q];
+                const float tc = corr(psi, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ez[c], ez[c - p.sy]));
+                p.psi_h[3][q] = psi;
+                h = fsub(h, fmul(0.5f, tc));
+            }
+            if (szh >= 0) {
+                const int64_t q = (i * ny + j) * 2 * P + szh;
+                float psi = p.psi_h[4][q];
+                const float tc = corr(psi, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ey[c], ey[c - 1]));
+                p.psi_h[4][q] = psi;
+                h = fadd(h, fmul(0.5f, tc));
+            }
+        }
+        p.out[3][c] = h;
+    }
+    // hy: curl, x slab (hy +=), z slab (hy -=)
+    {
+        float h = p.in[4][c];
+        if (i > 0 && k > 0) {
+            h = fsub(h, fmul(0.5f, curl4(ex[c], ex[c - 1], ez[c], ez[c - p.sx])));
+            if (sxh >= 0) {
+                const int64_t q = ((int64_t)sxh * ny + j) * nz + k;
+                float psi = p.psi_h[0][q];
+                const float tc = corr(psi, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ez[c], ez[c - p.sx]));
+                p.psi_h[0][q] = psi;
+                h = fadd(h, fmul(0.5f, tc));
+            }
+            if (szh >= 0) {
+                const int64_t q = (i * ny + j) * 2 * P + szh;
+                float psi = p.psi_h[5][q];
+                const float tc = corr(psi, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ex[c], ex[c - 1]));
+                p.psi_h[5][q] = psi;
+                h = fsub(h, fmul(0.5f, tc));
+            }
+        }
+        p.out[4][c] = h;
+    }
+    // hz: curl, x slab (hz -=), y slab (hz +=)
+    {
+        float h = p.in[5][c];
+        if (i > 0 && j > 0) {
+            h = fsub(h, fmul(0.5f, curl4(ey[c], ey[c - p.sx], ex[c], ex[c - p.sy])));
+            if (sxh >= 0) {
+                const int64_t q = ((int64_t)sxh * ny + j) * nz + k;
+                float psi = p.psi_h[1][q];
+                const float tc = corr(psi, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ey[c], ey[c - p.sx]));
+                p.psi_h[1][q] = psi;
+                h = fsub(h, fmul(0.5f, tc));
+            }
+            if (syh >= 0) {
+                const int64_t q = (i * 2 * P1 + syh) * nz + k;
+                float psi = p.psi_h[2][q];
+                const float tc = corr(psi, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ex[c], ex[c - p.sy]));
+                p.psi_h[2][q] = psi;
+                h = fadd(h, fmul(0.5f, tc));
+            }
+        }
+        p.out[5][c] = h;
+    }
+    (void)P0;
+}
 
 }  // namespace fused
 }  // namespace fdtd
@@ -827,8 +991,18 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     const int ns = tile && tile->stages ? tile->stages : 3;
     const KernelEntry *ke = find_kernel(ty, ns);
     if (!ke) return FDTD_ERR_UNSUPPORTED;
-    const int xch = tile && tile->x_chunk ? tile->x_chunk : 128;
+    int xch = tile && tile->x_chunk ? tile->x_chunk : 128;
     if (xch < 1) return FDTD_ERR_ARG;
+    if (!(tile && tile->x_chunk)) {
+        // default chunk: at least ~3 work items per SM so small grids fill the
+        // GPU (shorter chunks add pipeline fill and halo planes per item)
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0) {
+            const int64_t tiles = ((g.nz + TZ - 1) / TZ) * ((g.ny + ty - 1) / ty);
+            while (xch > 8 && tiles * ((g.nx + xch - 1) / xch) < 3 * (int64_t)nsm) xch /= 2;
+        }
+    }
 
     fdtd_yee_plan *pl = new fdtd_yee_plan();
     pl->g = g;
@@ -865,6 +1039,12 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         }
         for (int q = 0; q < 6; q++) p.psi_h[q] = s->psi_h[q];
     }
+    for (int q = 0; q < 3; q++) p.in_ce[q] = s->ce[q];
+    // z slab on the band kernels unless asked otherwise
+    const int zmode = tile ? tile->z_band : 0;
+    if (zmode < 0 || zmode > 2) { delete pl; return FDTD_ERR_ARG; }
+    const bool zslab = p.P[2] > 0 && ((p.faces >> 4) & 3);
+    p.zfix = (zslab && zmode != 1) ? 1 : 0;
     if (src && src->nsrc > 0) {
         if (!all_nonnull(src->ijk, src->comp, src->amp) || src->namp < 0) { delete pl; return FDTD_ERR_ARG; }
         p.nsrc = src->nsrc; p.src_ijk = src->ijk; p.src_comp = src->comp; p.src_amp = src->amp; p.namp = src->namp;
@@ -873,20 +1053,49 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         if (cudaMemcpy(hijk, src->ijk, sizeof(int32_t) * 3 * src->nsrc, cudaMemcpyDeviceToHost) != cudaSuccess) {
             delete[] hijk; delete pl; return FDTD_ERR_CUDA;
         }
+        // sources on E z-slab nodes: applied by the E band kernel
+        if (p.zfix) {
+            const int64_t P2 = p.P[2];
+            const int f2 = (p.faces >> 4) & 1, b2 = (p.faces >> 5) & 1;
+            for (int a = 0; a < src->nsrc; a++) {
+                const int64_t sk = hijk[3 * a + 2];
+                const bool node = (f2 && sk >= 1 && sk <= P2) || (b2 && sk >= g.nz - P2 - 1 && sk <= g.nz - 2);
+                if (!node) continue;
+                if (p.nbsrc == MAX_BAND_SRC) {  // too many: keep the z slab inside the fused kernel
+                    p.zfix = 0;
+                    p.nbsrc = 0;
+                    break;
+                }
+                p.bsrc[p.nbsrc++] = a;
+            }
+        }
+        // sources per work item, counted with the kernel's own membership test
+        // (x in [i_start, x1), y in [j0-1, j0+TY), z in [k0-1, k0+TZ)); a source
+        // lies in at most two chunks/tiles per axis
+        std::unordered_map<int64_t, int> per_item;
+        const int64_t xc = pl->x_chunk;
+        const int64_t ntz = (g.nz + TZ - 1) / TZ, nty = (g.ny + ty - 1) / ty;
         for (int a = 0; a < src->nsrc; a++) {
-            if (hijk[3 * a] < 0 || hijk[3 * a] >= g.nx || hijk[3 * a + 1] < 0 || hijk[3 * a + 1] >= g.ny ||
-                hijk[3 * a + 2] < 0 || hijk[3 * a + 2] >= g.nz) {
+            const int64_t si = hijk[3 * a], sj = hijk[3 * a + 1], sk = hijk[3 * a + 2];
+            if (si < 0 || si >= g.nx || sj < 0 || sj >= g.ny || sk < 0 || sk >= g.nz || sk >= (int64_t(1) << 28)) {
                 delete[] hijk; delete pl; return FDTD_ERR_ARG;
             }
-            int cnt = 0;
-            for (int b = 0; b < src->nsrc; b++) {
-                // conservative: neighbouring tile in y/z, neighbouring chunk in x
-                if (std::abs(hijk[3 * a + 1] / ty - hijk[3 * b + 1] / ty) <= 1 &&
-                    std::abs(hijk[3 * a + 2] / TZ - hijk[3 * b + 2] / TZ) <= 1 &&
-                    std::abs(hijk[3 * a] / pl->x_chunk - hijk[3 * b] / pl->x_chunk) <= 1)
-                    cnt++;
+            for (int64_t xi = si / xc; xi <= (si + 1) / xc; xi++) {
+                const int64_t x0 = xi * xc, x1 = std::min(x0 + xc, (int64_t)g.nx);
+                const int64_t is = x0 > 0 ? x0 - 1 : 0;
+                if (x0 >= g.nx || si < is || si >= x1) continue;
+                for (int64_t yi = sj / ty; yi <= (sj + 1) / ty && yi < nty; yi++) {
+                    const int64_t j0 = yi * ty;
+                    if (sj < j0 - 1 || sj >= j0 + ty) continue;
+                    for (int64_t zi = sk / TZ; zi <= (sk + 1) / TZ && zi < ntz; zi++) {
+                        const int64_t k0 = zi * TZ;
+                        if (sk < k0 - 1 || sk >= k0 + TZ) continue;
+                        if (++per_item[(xi * nty + yi) * ntz + zi] > MAX_LOCAL_SRC) {
+                            delete[] hijk; delete pl; return FDTD_ERR_CAPACITY;
+                        }
+                    }
+                }
             }
-            if (cnt > MAX_LOCAL_SRC) { delete[] hijk; delete pl; return FDTD_ERR_CAPACITY; }
         }
         delete[] hijk;
     }
@@ -913,7 +1122,7 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     }
     // z-slab psi staged by TMA: needs rows of 2P floats that are 16-byte multiples
     const int P2 = p.P[2];
-    const bool zpsi = P2 > 0 && (2 * P2 * 4) % 16 == 0 && 2 * P2 <= 256 && g.ny <= 0x7fffffff;
+    const bool zpsi = !p.zfix && P2 > 0 && (2 * P2 * 4) % 16 == 0 && 2 * P2 <= 256 && g.ny <= 0x7fffffff;
     int zbox = 0;
     if (zpsi) {
         const int box_bytes = (ty + 1) * 2 * P2 * 4;
@@ -973,6 +1182,16 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
         p.t = t0 + n;
         BatchDesc bd{};
         pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
+        if (p.zfix) {
+            for (int q = 0; q < 6; q++) p.in[q] = pl->f[in][q];
+            const int P2 = p.P[2], f2 = (p.faces >> 4) & 1, b2 = (p.faces >> 5) & 1;
+            const int64_t ne = pl->g.nx * pl->g.ny * ((f2 + b2) * (int64_t)P2);
+            const int64_t fend = f2 ? P2 + 1 : 0;
+            const int64_t bstart = b2 ? std::max<int64_t>(pl->g.nz - P2 - 1, fend + 1) : pl->g.nz;
+            const int64_t nh = pl->g.nx * pl->g.ny * (fend + pl->g.nz - bstart);
+            k_zband_e<<<(unsigned)((ne + 127) / 128), 128, 0, st>>>(p);
+            k_zband_h<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(p);
+        }
         FDTD_TRY(check_launch());
         pl->cur = outb;
     }
@@ -1058,8 +1277,11 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     int stage_bytes = 0, tab_bytes = 0;
     for (int32_t s = 0; s < nsims; s++) {
         fdtd_yee_plan *pl = nullptr;
+        // one launch per step for the whole batch: the z slab stays inside the fused kernel
+        fdtd_tile t1 = tile ? *tile : fdtd_tile{};
+        t1.z_band = 1;
         const int st = fdtd_yee_plan_create(&pl, &grids[s], &states[s], cpmls ? &cpmls[s] : nullptr,
-                                            srcs ? &srcs[s] : nullptr, tile, status_dev, cur);
+                                            srcs ? &srcs[s] : nullptr, &t1, status_dev, cur);
         if (st != FDTD_OK) return st;
         ke = pl->k;
         stage_bytes = std::max(stage_bytes, pl->base.stage_bytes);

@@ -141,13 +141,16 @@ typedef struct {
  * or 16 cells; the tile is 64 cells wide in z), x planes per work item,
  * resident CTAs per SM (persistent grid), pipeline stages (planes staged in
  * shared memory), L2 promotion of the tile loads (0 = 256 B, 1 = none,
- * 2 = 64 B, 3 = 128 B). */
+ * 2 = 64 B, 3 = 128 B), z-slab CPML path (0 = default, 1 = inside the
+ * fused kernel, 2 = two band kernels after it; the default is 2 for single
+ * grids and 1 in batched plans).  Both z paths give identical results. */
 typedef struct {
     int32_t tile_y;
     int32_t x_chunk;
     int32_t ctas_per_sm;
     int32_t stages;
     int32_t l2_promotion;
+    int32_t z_band;
 } fdtd_tile;
 
 typedef struct fdtd_yee_plan fdtd_yee_plan;
@@ -185,6 +188,46 @@ int fdtd_batch_plan_set_current(fdtd_batch_plan *plan, int32_t cur);
 /* info[0..5] = tile_y, stages, work items, CTAs launched, threads/CTA, shared bytes/CTA */
 int fdtd_batch_plan_info(const fdtd_batch_plan *plan, int32_t *info, int32_t n);
 int fdtd_batch_plan_destroy(fdtd_batch_plan *plan);
+
+/* ---- adjoint (reverse-time) step -------------------------------------- */
+/* Point lists: comp 0..5 = ex, ey, ez, hx, hy, hz at (i, j, k); device arrays. */
+typedef struct {
+    int32_t n;
+    const int32_t *ijk;   /* 3*n */
+    const int32_t *comp;  /* n   */
+} fdtd_points;
+
+typedef struct {
+    float *f[6];
+} fdtd_fields6;
+
+/* Adjoint state of the fused/unfused 2nd-order step (ch = 0.5).  lf: adjoint
+ * fields (grid layout); lpsi_e/lpsi_h: adjoint psi (layouts of fdtd_psi);
+ * w_e/w_h: scratch of the same layouts; grad_ce: dL/dCE accumulators (grid
+ * layout).  psi entries may be NULL on axes without PML. */
+typedef struct {
+    float *lf[6];
+    float *lpsi_e[6], *lpsi_h[6];
+    float *w_e[6], *w_h[6];
+    float *grad_ce[3];
+} fdtd_adjoint_state;
+
+/* One reverse step n: first adds mon_grad[p] to the adjoint of monitor
+ * point p (the monitors read the state at the end of step n), then applies
+ * the transpose of step n (cpml_h, update_h, cpml_e, update_e) and adds
+ * lE * (E increment / CE) to grad_ce.  h_prev: forward H entering step n;
+ * psi_e_cur: forward E-psi after step n.  mon may be NULL.  No reference
+ * counterpart: the reference has no gradient path. */
+int fdtd_adjoint_step_f32(const fdtd_grid *g, const fdtd_cpml *c, const fdtd_adjoint_state *s,
+                          const float *const h_prev[3], const float *const psi_e_cur[6],
+                          const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
+                          void *stream);
+/* out[p] = f[comp[p]][i, j, k] (NaN for a point outside the grid) */
+int fdtd_gather_points_f32(const fdtd_grid *g, const fdtd_points *pts, const float *const f[6],
+                           float *out, void *stream);
+/* f[comp[p]][i, j, k] += vals[p], in list order (points outside the grid skipped) */
+int fdtd_add_points_f32(const fdtd_grid *g, const fdtd_points *pts, float *const f[6],
+                        const float *vals, void *stream);
 
 /* ---- 4th-order symplectic stages (in place) --------------------------- */
 int fdtd_symplectic_h_f32(const fdtd_grid *g, float cl,

@@ -169,6 +169,9 @@ def _oracle_sim(work_shape, ce, npml, faces, sources, init):
     ((40, 40, 200), 4, (8, 16, 0, 4)),   # interior tiles take the packed fast path
     ((30, 44, 260), 3, None),
     ((24, 40, 200), 0, (4, 8, 0, 4)),
+    ((37, 29, 45), 5, (8, 16, 0, 3, 0, 1)),   # z slab inside the fused kernel
+    ((40, 40, 200), 4, (8, 16, 0, 4, 0, 1)),
+    ((30, 44, 260), 3, (16, 8, 1, 3, 0, 2)),  # z slab on the band kernels
 ])
 def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     from fdtd_accelerate_gb300 import configs
@@ -200,6 +203,33 @@ def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
         for q in range(6):
             np.testing.assert_array_equal(_host(fused.psi_e()[q]), sim.psi_e[q], err_msg="psi_e%d" % q)
             np.testing.assert_array_equal(_host(fused.cpml.psi_h[q]), sim.psi_h[q], err_msg="psi_h%d" % q)
+
+
+@pytest.mark.parametrize("tile", [None, (8, 16, 0, 3)])
+def test_fused_line_source_many_per_tile(fdtd, tile):
+    """A z line of 90 sources (a tile holds up to 65 of them, plus a second
+    line crossing the same tiles in y) equals the oracle; a layout with more
+    sources in one tile than the kernel can hold is refused at plan time."""
+    shape, npml = (30, 34, 100), 4
+    rng = np.random.default_rng(2)
+    t = np.arange(12, dtype=np.float64)
+    amp = fdtd.gaussian_sine(t, 3.0, 2.0, 0.1)
+    sources = [("ez", (7, 17, k), amp * (1 + 0.01 * k)) for k in range(5, 95)]
+    sources += [("ex", (12, j, 40), amp) for j in range(5, 29)]
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    ce = [np.full(shape, 0.5, np.float32) for _ in range(3)]
+    sim = _oracle_sim(shape, ce, (npml,) * 3, 0x3F, sources, init)
+    sim.step(8)
+    fused = fdtd.YeeSolver(shape, ce=ce, npml=npml, sources=sources, tile=tile)
+    fused.set_fields(**init)
+    fused.step(8)
+    torch.cuda.synchronize()
+    fused.check_status()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(fused.fields[k]), sim.f[k], err_msg=k)
+    crowded = [("ez", (7, 17, k), amp) for k in range(5, 95)] * 3   # 177 in the first z tile
+    with pytest.raises(ValueError):
+        fdtd.YeeSolver(shape, npml=npml, sources=crowded).plan()
 
 
 def test_fused_then_unfused_interleave(fdtd):

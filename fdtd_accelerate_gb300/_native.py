@@ -94,6 +94,8 @@ _SIGS = {
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
     "fdtd_adjoint_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P, P,
                                         C.POINTER(Points), P, P]),
+    "fdtd_adjoint_step_noalloc_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P,
+                                                P, C.POINTER(Points), P, P]),
     "fdtd_gather_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_add_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_batch_workspace_bytes": (C.c_size_t, [I32]),

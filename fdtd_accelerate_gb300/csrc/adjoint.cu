@@ -23,6 +23,8 @@
 // does not depend on scheduling.
 #include "common.cuh"
 
+#include <mutex>
+
 namespace fdtd {
 namespace adj {
 
@@ -457,6 +459,96 @@ int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_a
     if (A.P[2]) launch_slab<2>(g, A.P[2], true, A, st);
     k_adj_h<<<cells(g), kB, 0, st>>>(A);
     return check_launch();
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free adjoint step.
+//
+// fdtd_adjoint_step_f32 needs scratch for the w_e / w_h arrays (the adjoint
+// of the psi-driving differences, psi-shaped, written and read within one
+// call).  Some callers cannot provide it: a host binding with no device
+// allocator of its own (a plain C, cgo or JNI caller of this library), or a
+// loop that must not call cudaMalloc, which synchronises the device and is
+// not allowed while a stream is being captured.  This entry point takes the
+// scratch from a fixed device array compiled into the library instead.
+//
+//  * Maximum: kNoAllocScratchFloats floats (4 Mi floats = 16 MiB) for the
+//    12 w arrays, i.e. 4 * (2Px*ny*nz + nx*2Py*nz + nx*ny*2Pz) floats plus
+//    alignment; larger CPML layers are refused with FDTD_ERR_CAPACITY.
+//  * Set-up: the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress, with that device current) and caches it; make
+//    that first call before any stream capture.
+//  * Nothing in the scratch has to start at zero: every element the kernels
+//    read is written earlier in the same call (disabled faces are neither
+//    written nor read).
+//  * One scratch per device: calls that overlap in time (different streams
+//    or host threads on one device) race on it.
+// ---------------------------------------------------------------------------
+namespace fdtd {
+namespace adj {
+
+constexpr size_t kNoAllocScratchFloats = size_t(4) << 20;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+
+static std::mutex g_noalloc_mu;
+static float *g_noalloc_ptr[kMaxDevices];
+
+static int noalloc_scratch(float **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
+    if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
+        g_noalloc_ptr[dev] = static_cast<float *>(ptr);
+    }
+    *out = g_noalloc_ptr[dev];
+    return FDTD_OK;
+}
+
+}  // namespace adj
+}  // namespace fdtd
+
+extern "C" {
+
+int fdtd_adjoint_step_noalloc_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
+                                  const float *const h_prev[3], const float *const psi_e_cur[6],
+                                  const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
+                                  void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!s) return FDTD_ERR_ARG;
+    // psi-shaped w arrays of each axis, 256-byte aligned inside the scratch
+    size_t sz[3] = {0, 0, 0};
+    if (cp) {
+        for (int a = 0; a < 3; a++)
+            if (cp->npml[a] < 0) return FDTD_ERR_ARG;
+        sz[0] = (size_t)2 * cp->npml[0] * g.ny * g.nz;
+        sz[1] = (size_t)g.nx * 2 * cp->npml[1] * g.nz;
+        sz[2] = (size_t)g.nx * g.ny * 2 * cp->npml[2];
+    }
+    auto al = [](size_t n) { return (n + 63) / 64 * 64; };
+    const size_t need = 4 * (al(sz[0]) + al(sz[1]) + al(sz[2]));
+    if (need > kNoAllocScratchFloats) return FDTD_ERR_CAPACITY;
+    float *base = nullptr;
+    FDTD_TRY(noalloc_scratch(&base));
+    fdtd_adjoint_state t = *s;
+    size_t off = 0;
+    for (int a = 0; a < 3; a++) {
+        float **slots[4] = {&t.w_e[2 * a], &t.w_e[2 * a + 1], &t.w_h[2 * a], &t.w_h[2 * a + 1]};
+        for (float **w : slots) {
+            *w = sz[a] ? base + off : nullptr;
+            off += al(sz[a]);
+        }
+    }
+    return fdtd_adjoint_step_f32(gp, cp, &t, h_prev, psi_e_cur, ce, mon, mon_grad, stream);
 }
 
 int fdtd_gather_points_f32(const fdtd_grid *gp, const fdtd_points *pts, const float *const f[6], float *out,

@@ -222,6 +222,18 @@ int fdtd_adjoint_step_f32(const fdtd_grid *g, const fdtd_cpml *c, const fdtd_adj
                           const float *const h_prev[3], const float *const psi_e_cur[6],
                           const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
                           void *stream);
+/* fdtd_adjoint_step_f32 without caller scratch: s->w_e / s->w_h are ignored
+ * and a device array of 4 Mi floats (16 MiB) inside the library is used
+ * instead, for callers that cannot allocate device memory.  A CPML layer
+ * whose 12 w arrays (4*(2Px*ny*nz + nx*2Py*nz + nx*ny*2Pz) floats plus
+ * alignment) do not fit returns FDTD_ERR_CAPACITY.  The first call on a
+ * device sets it up and should come before any stream capture; calls that
+ * overlap in time on one device race on the shared scratch.  No counterpart
+ * in the reference. */
+int fdtd_adjoint_step_noalloc_f32(const fdtd_grid *g, const fdtd_cpml *c, const fdtd_adjoint_state *s,
+                                  const float *const h_prev[3], const float *const psi_e_cur[6],
+                                  const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
+                                  void *stream);
 /* out[p] = f[comp[p]][i, j, k] (NaN for a point outside the grid) */
 int fdtd_gather_points_f32(const fdtd_grid *g, const fdtd_points *pts, const float *const f[6],
                            float *out, void *stream);

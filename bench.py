@@ -3,9 +3,19 @@ all faces, 200 seeded dielectric spheres, 6 Gaussian dipoles (FP32).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-One step = one fused kernel launch advancing the whole grid by one time
-step (E + E-CPML + sources + H + H-CPML).  The state (33 GB) is far larger
-than L2, so no flush is needed between steps.  Prints one JSON line.
+One step advances the whole grid by one time step (E + E-CPML + sources +
+H + H-CPML): the fused kernel plus the two z-band kernels that finish the
+z-slab CPML.  The state (33 GB) is far larger than L2, so no flush is needed
+between steps.  Prints one JSON line.
+
+Other workloads (each prints its own line; the default is the headline):
+  --workload plain128    128^3 PEC vacuum, 1000 steps, plus the error against
+                         the FP64 oracle after those steps
+  --workload symp512     4th-order symplectic 512^3, 10-cell CPML, eps U[1,4]
+  --workload batched64   64 ragged grids, 500 steps, one graph launch, against
+                         64 sequential single-grid solves
+  --workload adjoint256  gradient run at 256x256x128, 3000 steps: backward /
+                         forward cost and central differences at 32 cells
 
 --impl reference times the reference's CPU path on the host cores: the
 reference's own C cannot be built on the benchmark host (SSE intrinsics,
@@ -243,6 +253,7 @@ def run_ours(args, rank, world):
         line_note = "scaled workload %dx%dx%d (not the headline size)" % tuple(shape)
     else:
         line_note = None
+    info = solver.plan_info()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -251,16 +262,19 @@ def run_ours(args, rank, world):
         "config": {"workload": "Yee+CPML %dx%dx%d, 12-cell CPML (m=4, R=1e-8, kappa_max=5, alpha_max=0.05), "
                                "200 spheres eps_r U[1,12], 6 Gaussian dipoles" % tuple(shape),
                    "cells": cells, "l2": "state 33 GB >> L2 (no flush needed)",
-                   "kernel": "k_yee_fused (TMA 3-D boxes, ping-pong state)",
-                   "tile": solver.plan_info(),
+                   "kernel": "k_yee_fused (TMA 3-D boxes, ping-pong state)" +
+                             (" + k_zband_e + k_zband_h (z-slab CPML)" if info["z_band"] else ""),
+                   "tile": info,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "alg_bytes_per_launch": alg, "peak_source": peak_src,
-                     "avg_launch_ms": avg_launch_s * 1e3},
+                     "avg_launch_ms": avg_launch_s * 1e3,
+                     "scope": "one time step (%d launch%s, timed together with CUDA events)"
+                              % (info["launches_per_step"], "es" if info["launches_per_step"] > 1 else "")},
         "clocks": clocks,
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * info["launches_per_step"],
     }
     if line_note:
         line["config"]["note"] = line_note
@@ -269,10 +283,258 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# secondary workloads (one JSON line each; not the headline)
+# ---------------------------------------------------------------------------
+def _flush_l2(buf):
+    """Overwrite a buffer larger than L2 (126 MB) so the next step starts cold."""
+    buf.add_(1.0)
+
+
+def _timed_steps(torch, stream, step, nsteps, flush=None):
+    """Per-step CUDA-event times (ms); an L2 flush runs outside each timed step."""
+    times = []
+    for _ in range(nsteps):
+        if flush is not None:
+            flush()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        times.append((a, b))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in times]
+
+
+def _base_line(metric, value, unit, args, ms, dtype, workload, extra=None):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)", "config": {"workload": workload}}
+    if extra:
+        line.update(extra)
+    return line
+
+
+def run_plain128(args):
+    """128^3 PEC vacuum, Ez source at the centre (one fused launch per step)."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs
+    dev = torch.device("cuda", 0)
+    w = configs.plain128(steps=max(1000, args.warmup + args.steps + 2))
+    s = F.YeeSolver(w.shape, sources=w.source_list(), device=dev, tile=args.tile)
+    stream = torch.cuda.current_stream(dev)
+    flush_buf = torch.zeros(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+    for _ in range(args.warmup):
+        s.step(1)
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = _timed_steps(torch, stream, lambda: s.step(1), args.steps, lambda: _flush_l2(flush_buf))
+    clocks = sampler.stop()
+    s.check_status()
+    cells = w.cells
+    avg = statistics.mean(ms)
+    alg = algorithmic_bytes_per_step(w.shape, 0)
+    peak, src = measured_peak()
+    achieved = alg / (avg / 1e3) / 1e9
+    info = s.plan_info()
+    line = _base_line("Mcell-updates/s (plain Yee 128^3 PEC, FP32)", cells / (avg / 1e3) / 1e6, UNIT, args, avg,
+                      "f32", "plain Yee 128x128x128, PEC walls, vacuum, Ez source at the centre (L2 flushed "
+                      "before every timed step)",
+                      {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": None, "peak_source": src},
+                       "clocks": clocks, "gpu_launches": args.steps * info["launches_per_step"],
+                       "accuracy": "bit-exact against the FP32 oracle after 1000 steps; FP32-vs-FP64 floor in "
+                                   "tests/test_gpu_accuracy.py"})
+    line["config"]["tile"] = info
+    print(json.dumps(line), flush=True)
+
+
+def run_symp512(args):
+    """4th-order symplectic, 512^3, 10-cell CPML, 60 spheres eps U[1,4], one dipole."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs, symplectic
+    dev = torch.device("cuda", 0)
+    shape, npml = (512, 512, 512), 10
+    rng = np.random.default_rng(20261206)
+    spheres = configs.random_spheres(rng, shape, 60, 5, 40, 1.0, 4.0)
+    ce = [(c * np.float32(symplectic.COURANT / 24 / 0.5)) for c in configs.ce_from_spheres(shape, spheres, device=dev)]
+    src = [("ez", (256, 256, 256), lambda t: float(np.sin(2 * np.pi * 0.05 * t) * np.exp(-0.5 * ((t - 150.0) / 30.0) ** 2)))]
+    s = symplectic.SymplecticSolver(shape, ce=ce, npml=npml, sources=src, device=dev,
+                                    max_steps=args.warmup + args.steps + 2)
+    del ce
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        s.step(1)
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = _timed_steps(torch, stream, lambda: s.step(1), args.steps)
+    clocks = sampler.stop()
+    avg = statistics.mean(ms)
+    cells = int(np.prod(shape))
+    alg = algorithmic_bytes_per_step(shape, npml)
+    peak, psrc = measured_peak()
+    achieved = alg / (avg / 1e3) / 1e9
+    # per step: 5 H stages (stage kernel + one CPML kernel per axis) and 4 E stages
+    # (stage kernel + CPML kernels + the source kernel)
+    naxes = sum(1 for p in s.cpml.npml if p) if s.cpml.active else 0
+    per_step = 5 * (1 + naxes) + 4 * (2 + naxes)
+    line = _base_line("Mcell-updates/s (4th-order symplectic 512^3, 10-cell CPML, FP32)", cells / (avg / 1e3) / 1e6,
+                      UNIT, args, avg, "f32", "4th-order symplectic 512x512x512, 10-cell CPML, 60 spheres eps_r "
+                      "U[1,4], Ez dipole; 4 E + 5 H stages per step (state 3.2 GB >> L2)",
+                      {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": None, "peak_source": psrc,
+                                    "alg_bytes_per_launch": alg,
+                                    "scope": "one time step (stage kernels, compulsory bytes of the whole step)"},
+                       "clocks": clocks, "gpu_launches": args.steps * per_step})
+    print(json.dumps(line), flush=True)
+
+
+def run_batched64(args):
+    """64 ragged grids in one launch per step (autotuned, graph-captured) against
+    the same 64 grids solved one after another with the single-grid path."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs
+    dev = torch.device("cuda", 0)
+    works = configs.batched64()
+    batch = F.BatchSolver.from_workloads(works, device=dev)
+    tune = batch.autotune()
+    stream = torch.cuda.current_stream(dev)
+    n = args.steps
+    for _ in range(args.warmup):
+        batch.step(1)
+    g = batch.capture(n)
+    g.replay()  # first replay outside the timed region
+    batch._advance(n)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    g.replay()
+    b.record(stream)
+    b.synchronize()
+    clocks = sampler.stop()
+    batch._advance(n)
+    batch.check_status()
+    ms_batch = a.elapsed_time(b) / n
+    # sequential: each grid alone, one single-grid fused step per launch group
+    for sv in batch.solvers:
+        sv.step(2)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for sv in batch.solvers:
+        sv.step(n)
+    b.record(stream)
+    b.synchronize()
+    ms_seq = a.elapsed_time(b) / n
+    cells = batch.cells
+    info = batch.plan_info()
+    line = _base_line("Mcell-updates/s (64 ragged Yee+CPML grids, one launch per step, FP32)",
+                      cells / (ms_batch / 1e3) / 1e6, UNIT, args, ms_batch, "f32",
+                      "64 grids, axes from {32..192 step 16}, 8-cell CPML, 10 spheres eps_r U[1,8] each, Ez "
+                      "centre source; %d steps captured in one CUDA graph; %d cells in all" % (n, cells),
+                      {"sequential": {"value": cells / (ms_seq / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms_seq,
+                                      "how": "the same 64 grids stepped one after another (single-grid plans)"},
+                       "speedup_vs_sequential": ms_seq / ms_batch,
+                       "clocks": clocks, "gpu_launches": n})
+    line["config"]["tile"] = info
+    line["config"]["autotune"] = tune
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint256(args):
+    """Gradient of a probe loss w.r.t. the permittivity of a 128x128x64 design
+    region: forward and backward cost, and central differences at 32 cells."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs
+    dev = torch.device("cuda", 0)
+    w = configs.adjoint256(steps=args.steps)
+    eng = F.YeeAdjoint(w.shape, w.steps, npml=w.npml, sources=w.sources, monitors=w.monitors,
+                       segment=w.segment, device=dev)
+    eps = w.eps.to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def ce_of(e):
+        return (w.dt / e).float().unsqueeze(0).expand(3, -1, -1, -1).contiguous()
+
+    def loss_of(mon):
+        return (mon.double() ** 2).sum()
+
+    times = []
+    for rep in range(3):  # rep 0 warms up
+        e = eps.clone().requires_grad_(True)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t2 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        mon, _ = F.fdtd_run(ce_of(e), eng)
+        t1.record(stream)
+        L = loss_of(mon)
+        L.backward()
+        t2.record(stream)
+        t2.synchronize()
+        if rep:
+            times.append((t0.elapsed_time(t1), t1.elapsed_time(t2)))
+        grad = e.grad.detach()
+        L0 = float(L.detach())
+    eng.check_status()
+    fwd = statistics.mean(t[0] for t in times)
+    bwd = statistics.mean(t[1] for t in times)
+    # central differences (FP32 forward, loss accumulated in FP64) at random design cells
+    rng = np.random.default_rng(7)
+    cells, errs, g_fd = [], [], []
+    h = 1e-3
+    ds = w.design
+    with torch.no_grad():
+        for _ in range(args.fd_cells):
+            c = tuple(int(rng.integers(sl.start, sl.stop)) for sl in ds)
+            vals = []
+            for sgn in (1, -1):
+                e2 = eps.clone()
+                e2[c] += sgn * h
+                m2, _ = F.fdtd_run(ce_of(e2), eng)
+                vals.append(float(loss_of(m2)))
+            fd = (vals[0] - vals[1]) / (2 * h)
+            gc = float(grad[c])
+            cells.append(c)
+            g_fd.append((gc, fd))
+            errs.append(abs(gc - fd) / max(abs(fd), 1e-300))
+    gmax = max(abs(f) for _, f in g_fd) if g_fd else 0.0
+    norm_err = max(abs(a - b) for a, b in g_fd) / gmax if gmax else None
+    nc = int(np.prod(w.shape))
+    line = _base_line("adjoint cost: backward time / forward time (gradient run 256x256x128, 3000 steps)",
+                      bwd / fwd, "x", args, (fwd + bwd) / w.steps, "f32",
+                      w.name + "; loss = sum_t sum_p Ez^2; checkpoints every %d steps" % w.segment,
+                      {"higher_is_better": False,
+                       "forward": {"ms": fwd, "Mcells_per_s": nc * w.steps / (fwd / 1e3) / 1e6},
+                       "backward": {"ms": bwd, "Mcells_per_s": nc * w.steps / (bwd / 1e3) / 1e6,
+                                    "what": "segment recompute from checkpoints + reverse-time adjoint steps"},
+                       "gradient_over_forward": (fwd + bwd) / fwd,
+                       "fd_check": {"cells": len(cells), "h": h, "loss": L0,
+                                    "median_rel_err": float(np.median(errs)) if errs else None,
+                                    "max_rel_err": float(max(errs)) if errs else None,
+                                    "max_err_over_max_fd": norm_err,
+                                    "note": "FP32 forward runs: the perturbation changes the loss by g*h/L ~ "
+                                            "1e-7..1e-5, the order of FP32 roundoff, so this bounds noise more "
+                                            "than the gradient; the FP64-loss check is tests/test_gpu_adjoint.py"},
+                       "gpu_launches": None})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200; plain128 1000, symp512 50, batched64 500, adjoint256 3000)")
+    ap.add_argument("--workload", default="cpml1024",
+                    choices=["cpml1024", "plain128", "symp512", "batched64", "adjoint256"])
+    ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", type=lambda s: tuple(int(v) for v in s.split(",")), default=SHAPE,
@@ -284,6 +546,17 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = {"cpml1024": 200, "plain128": 1000, "symp512": 50, "batched64": 500,
+                      "adjoint256": 3000}[args.workload]
+    if args.workload != "cpml1024":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "workload": args.workload,
+                              "unavailable": "the reference arm covers the headline workload only"}), flush=True)
+            return
+        {"plain128": run_plain128, "symp512": run_symp512, "batched64": run_batched64,
+         "adjoint256": run_adjoint256}[args.workload](args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":

@@ -1214,6 +1214,10 @@ int fdtd_yee_plan_info(const fdtd_yee_plan *pl, int32_t *info, int32_t n) {
     info[3] = pl->nblocks;
     info[4] = pl->k->threads;
     info[5] = pl->smem;
+    if (n >= 8) {
+        info[6] = pl->base.zfix;                  // 1: z slab on the band kernels
+        info[7] = pl->base.zfix ? 3 : 1;          // kernel launches per step
+    }
     return FDTD_OK;
 }
 

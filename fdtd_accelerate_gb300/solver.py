@@ -125,9 +125,10 @@ class YeeSolver:
 
     def plan_info(self):
         """Launch shape chosen for the fused kernel."""
-        info = (C.c_int32 * 6)()
-        N.call("fdtd_yee_plan_info", self.plan(), info, 6)
-        return dict(zip(("tile_y", "stages", "x_chunk", "ctas", "threads", "smem_bytes"), list(info)))
+        info = (C.c_int32 * 8)()
+        N.call("fdtd_yee_plan_info", self.plan(), info, 8)
+        return dict(zip(("tile_y", "stages", "x_chunk", "ctas", "threads", "smem_bytes", "z_band",
+                         "launches_per_step"), list(info)))
 
     def step(self, n=1):
         """Advance n steps with the fused kernel (one launch per step)."""

@@ -163,7 +163,9 @@ int fdtd_yee_plan_create(fdtd_yee_plan **plan, const fdtd_grid *g, const fdtd_ye
 int fdtd_yee_plan_run(fdtd_yee_plan *plan, int64_t t0, int64_t nsteps, void *stream);
 int fdtd_yee_plan_current(const fdtd_yee_plan *plan);
 int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
-/* info[0..5] = tile_y, stages, x_chunk, CTAs launched, threads/CTA, shared bytes/CTA */
+/* info[0..5] = tile_y, stages, x_chunk, CTAs launched, threads/CTA, shared bytes/CTA;
+ * with n >= 8 also info[6] = 1 when the z slab runs on the band kernels and
+ * info[7] = kernel launches per step */
 int fdtd_yee_plan_info(const fdtd_yee_plan *plan, int32_t *info, int32_t n);
 int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 

@@ -47,8 +47,7 @@ class YeeState(C.Structure):
 
 
 class Tile(C.Structure):
-    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32),
-                ("z_band", I32)]
+    _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32)]
 
 
 class Points(C.Structure):

@@ -116,7 +116,7 @@ class YeeAdjoint:
             g = self.grid()
             cp = self.cpml.struct()
             src = self.sources.struct()
-            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0, 0))[:6])
+            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             plans = []
             with torch.cuda.device(self.device):
                 for m in range(self.K):

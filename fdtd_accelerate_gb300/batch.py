@@ -84,7 +84,7 @@ class BatchSolver:
             states = (N.YeeState * n)(*[s._state_struct() for s in self.solvers])
             cpmls = (N.Cpml * n)(*[s.cpml.struct() for s in self.solvers])
             srcs = (N.Sources * n)(*[s.sources.struct() for s in self.solvers])
-            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0, 0))[:6])
+            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             h = C.c_void_p()
             # the workspace is rewritten: no launch of an earlier plan may still read it
             torch.cuda.synchronize(self.device)

@@ -61,7 +61,10 @@ struct Layout {
     static constexpr int ENEWC = NR * NCW;  // floats per component
     static constexpr int THREADS = (TY + 2) * 32;
     static constexpr int ENEW = al128(3 * ENEWC * 4);
-    static constexpr int SMEM = NS * STAGE + ENEW + 128 /*barriers*/ + 128 /*align slack*/;
+    // psi ring: 2 slots x 4 boxes (E psi 1, 2 and H psi 1, 2 of one axis)
+    static constexpr int PSIRING = 2 * 4 * EBOXB;
+    static constexpr uint32_t PSI_TX = EBOX * 4;
+    static constexpr int SMEM = NS * STAGE + ENEW + 128 /*barriers*/ + PSIRING + 128 /*align slack*/;
     // CTAs per SM the register budget is sized for (shared memory may allow fewer)
     static constexpr int MINB = TY == 4 ? 4 : (TY == 8 ? 2 : 1);
 };
@@ -70,8 +73,12 @@ struct TMaps {
     CUtensorMap h[3];   // hx, hy, hz of the input buffer, box (HC, TY+2, 1)
     CUtensorMap e[3];   // ex, ey, ez of the input buffer, box (EC, TY+1, 1)
     CUtensorMap ce[3];  // cex, cey, cez,                  box (EC, TY+1, 1)
-    CUtensorMap zpe[2]; // z-slab E psi (exz, eyz) of the input buffer, box (2P, TY+1, 1)
-    CUtensorMap zph[2]; // z-slab H psi (hxz, hyz),                    box (2P, TY+1, 1)
+    // x/y CPML psi slabs, box (EC, TY+1, 1): x arrays (2P, ny, nz) at (k0-4, j0-1, s),
+    // y arrays (nx, 2P, nz) at (k0-4, first slab index of the tile, i)
+    CUtensorMap xpe[2];  // eyx, ezx of the input buffer
+    CUtensorMap xph[2];  // hyx, hzx
+    CUtensorMap ype[2];  // ezy, exy of the input buffer
+    CUtensorMap yph[2];  // hzy, hxy
 };
 
 struct Params {
@@ -92,18 +99,18 @@ struct Params {
     int64_t namp;
     int64_t t;
     int32_t *status;
-    // z-slab psi staged by TMA with the fields (tiles touching a z slab)
-    int32_t zpsi;         // 1 when the z-psi boxes are used
-    int32_t stage_bytes;  // bytes per pipeline stage (fields + z-psi boxes)
-    int32_t zbox;         // bytes per z-psi box in shared memory (128-aligned)
-    uint32_t tx_z;        // bytes the 4 z-psi boxes deliver
-    // z band (1 when the z-slab CPML is finished by the band kernels): the
-    // fused kernel then leaves the E z-psi correction, sources on E z-slab
-    // nodes and every H cell of the band (k in [1, P+1], [n-P-1, n-1]) to them
+    int32_t stage_bytes;  // bytes per pipeline stage
+    int32_t xypsi;        // 1: x/y psi slabs arrive by TMA in the psi ring
+    // z band (1 when a z face has CPML): the z-slab CPML is finished by the
+    // band kernels.  The fused kernel leaves them the E z-psi correction, the
+    // sources on E z-slab nodes and every H cell of the band (k in [1, P+1]
+    // and [n-P-1, n-1]).
     int32_t zfix;
     const float *in[6];   // input buffer fields (read by the band kernels)
     const float *in_ce[3];
-    int32_t nbsrc;        // sources on E z-slab nodes (applied by the E band kernel)
+    // sources on E z-slab nodes, applied by the E band kernel in list order;
+    // nbsrc < 0: more than MAX_BAND_SRC of them, the band kernel scans the list
+    int32_t nbsrc;
     int32_t bsrc[MAX_BAND_SRC];
 };
 
@@ -262,8 +269,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     float *enew = reinterpret_cast<float *>(smem + NS * FDTD_SB);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NS * FDTD_SB + L::ENEW);
     float *Nx = enew, *Ny = enew + L::ENEWC, *Nz = enew + 2 * L::ENEWC;
-    // CPML tables in shared memory: tab[(axis*2 + eh)*3 + {b,a,km}] has 2P[axis] entries
-    float *tabs = reinterpret_cast<float *>(smem + NS * FDTD_SB + L::ENEW + 128);
+    // psi ring (2 slots of 4 boxes), then the CPML tables:
+    // tab[(axis*2 + eh)*3 + {b,a,km}] has 2P[axis] entries
+    unsigned char *psiring = smem + NS * FDTD_SB + L::ENEW + 128;
+    float *tabs = reinterpret_cast<float *>(psiring + L::PSIRING);
     // batched launches: parameters of the grid the current item belongs to
     __shared__ __align__(16) Params s_p;
 
@@ -291,26 +300,31 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     auto sC = [&](int st, int c) {
         return reinterpret_cast<float *>(stage_ptr(st) + 3 * L::HBOXB + (3 + c) * L::EBOXB);
     };
-    // z-psi boxes: 0,1 = E psi (exz, eyz) input; 2,3 = H psi (hxz, hyz); row r holds 2P values
+    // psi box b (0, 1 = E psi, 2, 3 = H psi of the x or y slab) of ring slot sl
+    auto sP = [&](int sl, int b) { return reinterpret_cast<float *>(psiring + (sl * 4 + b) * L::EBOXB); };
     const Params &p = BATCH ? s_p : pk;
-    // z-psi boxes: 0,1 = E psi (exz, eyz) input; 2,3 = H psi (hxz, hyz); row r holds 2P values
-    auto sZ = [&](int st, int c) { return reinterpret_cast<float *>(stage_ptr(st) + L::STAGE + c * p.zbox); };
 
     // stage the CPML coefficient tables of the current grid (a few hundred floats)
     auto stage_tables = [&]() {
         int off = 0;
+        auto copy = [&](const float *src, int n2) {
+            for (int x = tid; x < n2; x += blockDim.x) tabs[off + x] = src[x];
+            off += n2;
+        };
+#pragma unroll
         for (int a = 0; a < 3; a++) {
             const int n2 = 2 * p.P[a];
-            const float *src[6] = {p.tb_e[a], p.ta_e[a], p.tk_e[a], p.tb_h[a], p.ta_h[a], p.tk_h[a]};
-            for (int q = 0; q < 6; q++) {
-                for (int x = tid; x < n2; x += blockDim.x) tabs[off + x] = src[q][x];
-                off += n2;
-            }
+            copy(p.tb_e[a], n2);
+            copy(p.ta_e[a], n2);
+            copy(p.tk_e[a], n2);
+            copy(p.tb_h[a], n2);
+            copy(p.ta_h[a], n2);
+            copy(p.tk_h[a], n2);
         }
     };
 
     if (tid == 0) {
-        for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
+        for (int s = 0; s < NS + 2; s++) mbar_init(&bars[s], 1);  // stages, then the 2 psi slots
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         if (!BATCH) {
@@ -319,10 +333,12 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 prefetch_tmap(&mk.e[c]);
                 prefetch_tmap(&mk.ce[c]);
             }
-            if (pk.zpsi)
+            if (pk.xypsi)
                 for (int c = 0; c < 2; c++) {
-                    prefetch_tmap(&mk.zpe[c]);
-                    prefetch_tmap(&mk.zph[c]);
+                    prefetch_tmap(&mk.xpe[c]);
+                    prefetch_tmap(&mk.xph[c]);
+                    prefetch_tmap(&mk.ype[c]);
+                    prefetch_tmap(&mk.yph[c]);
                 }
         }
         s_abort = 0;
@@ -355,7 +371,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     }
 
     uint32_t g0 = 0;          // planes this CTA has issued before the current item
+    uint32_t gp0 = 0;         // psi ring phases this CTA has used before the current item
     int64_t issued_hi = -1;   // highest plane index (relative) issued in the current item (tid 0)
+    int64_t psi_hi = -1;      // highest plane whose psi boxes were issued (tid 0)
     int64_t q_abort = 0, i_start_abort = 0;
     bool aborted = false;
     const int64_t nitems = BATCH ? bd.item_off[bd.nsims] : (int64_t)pk.ntz * pk.nty * pk.nxc;
@@ -403,13 +421,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const int64_t nplanes = x1 - i_start + 1;  // planes i_start .. x1 (H(x1) feeds E(x1-1))
         // Tile-uniform: no grid edge and no y/z CPML slab inside the tile's E/H region.
         // tile's E (k0-1..k0+TZ-1) or H (k0..k0+TZ-1) columns touch a z slab
-        // with the band kernels the z slab is not this kernel's work (P2k = 0)
-        const int P2k = p.zfix ? 0 : P2;
-        const bool ztile = P2k > 0 && ((front2 && k0 - 1 <= P2k) || (back2 && k0 + TZ - 1 >= nz - P2k - 1));
-        const bool zstage = ztile && p.zpsi;
-        const bool yz_plain = j0 >= 1 && j0 + TY <= ny - 1 && k0 >= 1 && k0 + TZ <= nz - 1 &&
-                              (P1 == 0 || ((j0 - 1 > P1 || !front1) && (j0 + TY - 1 < ny - P1 - 1 || !back1))) &&
-                              (P2k == 0 || ((k0 - 1 > P2k || !front2) && (k0 + TZ - 1 < nz - P2k - 1 || !back2)));
+        // Tile-uniform: no y CPML slab among the tile's rows.  Grid edges are
+        // handled on the plain path by per-lane masks, and the z slab is the
+        // band kernels' work, so z-slab tiles are plain here too.
+        const bool y_plain = P1 == 0 || ((j0 - 1 > P1 || !front1) && (j0 + TY - 1 < ny - P1 - 1 || !back1));
+
+        // y psi by TMA for tiles whose y-slab rows lie on one side (box row r <-> j0-1+r)
+        const bool ye_f = front1 && P1 > 0 && j0 - 1 <= P1 && j0 + TY - 1 >= 1;
+        const bool ye_b = back1 && P1 > 0 && j0 + TY - 1 >= ny - P1 - 1 && j0 - 1 <= ny - 2;
+        const bool yh_f = front1 && P1 > 0 && j0 <= P1 && j0 + TY - 1 >= 1;
+        const bool yh_b = back1 && P1 > 0 && j0 + TY - 1 >= ny - P1 && j0 <= ny - 1;
+        const bool ytile = p.xypsi && (ye_f || ye_b || yh_f || yh_b) && !((ye_f || yh_f) && (ye_b || yh_b));
 
         // ---- per-item, per-thread cell description (pair at row j, columns k, k+1) ----
         const int64_t jj = j0 - 1 + er, kk = k0 + eko;
@@ -417,12 +439,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const bool in0 = row_in && kk >= 0 && kk < nz, in1 = row_in && kk + 1 >= 0 && kk + 1 < nz;
         const bool j_lt = jj < ny - 1, j_gt = jj > 0;
         const bool k0_lt = kk < nz - 1, k1_lt = kk + 1 < nz - 1, k0_gt = kk > 0, k1_gt = kk + 1 > 0;
+        // lanes with a cell outside an update region (grid edges); the i edges are plane-uniform
+        const bool emask = !(j_lt && k0_lt && k1_lt), hmask = !(j_gt && k0_gt && k1_gt);
         const int sye = row_in ? slab_e(jj, P1, ny, front1, back1) : -1;
         const int syh = row_in ? slab_h(jj, P1, ny, front1, back1) : -1;
-        const int sze0 = in0 ? slab_e(kk, P2k, nz, front2, back2) : -1;
-        const int sze1 = in1 ? slab_e(kk + 1, P2k, nz, front2, back2) : -1;
-        const int szh0 = in0 ? slab_h(kk, P2k, nz, front2, back2) : -1;
-        const int szh1 = in1 ? slab_h(kk + 1, P2k, nz, front2, back2) : -1;
         // H cells of the z band: left to the band kernel (no psi_h update here)
         const bool hb0 = p.zfix && in_zband_h(kk, P2, nz, front2, back2);
         const bool hb1 = p.zfix && in_zband_h(kk + 1, P2, nz, front2, back2);
@@ -438,16 +458,52 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
                 return;
             }
-            mbar_arrive_expect_tx(bar, L::TX + (zstage ? p.tx_z : 0u));
+            mbar_arrive_expect_tx(bar, L::TX);
             const int kc = (int)(k0 - 4), jc = (int)(j0 - 1), xc = (int)plane;
             for (int c = 0; c < 3; c++) tma_load_3d(sH(st, c), &maps.h[c], bar, kc, jc, xc);
             for (int c = 0; c < 3; c++) tma_load_3d(sE(st, c), &maps.e[c], bar, kc, jc, xc);
             for (int c = 0; c < 3; c++) tma_load_3d(sC(st, c), &maps.ce[c], bar, kc, jc, xc);
-            if (zstage) {
-                tma_load_3d(sZ(st, 0), &maps.zpe[0], bar, 0, jc, xc);
-                tma_load_3d(sZ(st, 1), &maps.zpe[1], bar, 0, jc, xc);
-                tma_load_3d(sZ(st, 2), &maps.zph[0], bar, 0, jc, xc);
-                tma_load_3d(sZ(st, 3), &maps.zph[1], bar, 0, jc, xc);
+        };
+        // psi boxes of plane q into ring slot (gp0+q)&1: the x slab's on x-slab
+        // planes, else the y slab's in y-slab tiles; otherwise a bare arrive
+        auto issue_psi = [&](int64_t q) {
+            const uint32_t Gp = gp0 + (uint32_t)q;
+            const int sl = (int)(Gp & 1);
+            uint64_t *bar = &bars[NS + sl];
+            psi_hi = q;
+            const int64_t plane = i_start + q;
+            const int xse = plane < nx ? slab_e(plane, P0, nx, front0, back0) : -1;
+            const int xsh = plane < nx ? slab_h(plane, P0, nx, front0, back0) : -1;
+            const bool xm = p.xypsi && (xse >= 0 || xsh >= 0);
+            const bool ym = !xm && ytile && plane < nx;
+            const bool ye = ye_f || ye_b, yh = yh_f || yh_b;
+            const uint32_t nbox = xm ? 2u * (xse >= 0) + 2u * (xsh >= 0) : (ym ? 2u * ye + 2u * yh : 0u);
+            if (nbox == 0) {
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+                return;
+            }
+            mbar_arrive_expect_tx(bar, nbox * L::PSI_TX);
+            const int kc = (int)(k0 - 4), jc = (int)(j0 - 1), xc = (int)plane;
+            if (xm) {
+                if (xse >= 0) {
+                    tma_load_3d(sP(sl, 0), &maps.xpe[0], bar, kc, jc, xse);
+                    tma_load_3d(sP(sl, 1), &maps.xpe[1], bar, kc, jc, xse);
+                }
+                if (xsh >= 0) {
+                    tma_load_3d(sP(sl, 2), &maps.xph[0], bar, kc, jc, xsh);
+                    tma_load_3d(sP(sl, 3), &maps.xph[1], bar, kc, jc, xsh);
+                }
+            } else {
+                if (ye) {
+                    const int ys = ye_b ? (int)(P1 + (j0 - 1) - (ny - P1 - 1)) : (int)(j0 - 2);
+                    tma_load_3d(sP(sl, 0), &maps.ype[0], bar, kc, ys, xc);
+                    tma_load_3d(sP(sl, 1), &maps.ype[1], bar, kc, ys, xc);
+                }
+                if (yh) {
+                    const int ys = yh_b ? (int)(P1 + (j0 - 1) - (ny - P1)) : (int)(j0 - 2);
+                    tma_load_3d(sP(sl, 2), &maps.yph[0], bar, kc, ys, xc);
+                    tma_load_3d(sP(sl, 3), &maps.yph[1], bar, kc, ys, xc);
+                }
             }
         };
 
@@ -476,10 +532,12 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             s_nls = n;
         }
         __syncthreads();  // previous item finished by every thread; source list ready
-        if (tid == 0)
+        if (tid == 0) {
             for (int64_t q = 0; q < NS && q < nplanes; q++) issue(q);
+            if (nplanes > 1) issue_psi(0);
+        }
         const int nls = s_nls;
-        const bool tile_plain = yz_plain && nls == 0;
+        const bool tile_plain = y_plain && nls == 0;
 
         float2 prev_ey = make_float2(0.f, 0.f), prev_ez = make_float2(0.f, 0.f);
         float2 oex = prev_ey, oey = prev_ey, oez = prev_ey;  // own E_new pair
@@ -488,11 +546,14 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             const uint32_t G = g0 + (uint32_t)q;
             const int st = (int)(G % NS), st1 = (int)((G + 1) % NS);
             const uint32_t par = (G / NS) & 1, par1 = ((G + 1) / NS) & 1;
+            const uint32_t Gp = gp0 + (uint32_t)q;
+            const int psl = (int)(Gp & 1);
             // One thread waits for the copies; the barrier then releases the CTA
             // (the mbarrier acquire by tid 0 plus bar.sync order the TMA writes
             // before every thread's reads).
             if (tid == 0 &&
-                (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status)))
+                (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status) ||
+                 !mbar_wait_bounded(&bars[NS + psl], (Gp >> 1) & 1, p.status)))
                 s_abort = 1;
             __syncthreads();  // (A) planes q, q+1 visible; iteration q-1 finished everywhere
             if (s_abort) {
@@ -501,13 +562,19 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 i_start_abort = i_start;
                 break;
             }
-            if (tid == 0 && q >= 1 && q - 1 + NS < nplanes) issue(q - 1 + NS);  // reuse plane q-1's stage
+            if (tid == 0) {
+                if (q >= 1 && q - 1 + NS < nplanes) issue(q - 1 + NS);  // reuse plane q-1's stage
+                if (q + 2 < nplanes) issue_psi(q + 1);                  // reuse plane q-1's psi slot
+            }
 
             // plane-uniform CPML (x) and masks
             const int sxe = slab_e(i, P0, nx, front0, back0), sxh = slab_h(i, P0, nx, front0, back0);
             const bool i_lt = i < nx - 1, i_gt = i > 0;
             const bool e_plain = tile_plain && i_lt && sxe < 0;
             const bool h_plain = tile_plain && i_gt && sxh < 0;
+            // where this plane's x/y psi come from (the choice of issue_psi)
+            const bool xm = p.xypsi && (sxe >= 0 || sxh >= 0);
+            const bool ym = !xm && ytile;
 
             // ---- E phase ----
             if (e_active) {
@@ -524,7 +591,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 float2 ex = add2(ex0, mul2(cex, curl4x2(hzj1, hz, hyk1, hy)));
                 float2 ey = add2(ey0, mul2(cey, curl4x2(hxk1, hx, hz1, hz)));
                 float2 ez = add2(ez0, mul2(cez, curl4x2(hy1, hy, hxj1, hx)));
-                if (!e_plain) {
+                if (!e_plain || emask) {
                     // component masks (cells the reference does not update keep their value)
                     if (!(j_lt && k0_lt)) ex.x = ex0.x;
                     if (!(j_lt && k1_lt)) ex.y = ex0.y;
@@ -534,6 +601,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         ez.x = ez0.x;
                         ez.y = ez0.y;
                     }
+                }
+                if (!e_plain) {
                     const bool own = own_row && i >= x0;
                     if (sxe >= 0) {  // x slab: ey -= cey (..dHz/dx..), ez += cez (..dHy/dx..)
                         const Coef c = tab_coef(tabs, toff0, 2 * P0, 0, sxe);
@@ -542,13 +611,13 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
                             if (e ? k1_lt : k0_lt) {
-                                float psi = p.psi_e_in[0][qb + e];
+                                float psi = xm ? sP(psl, 0)[er * EC + 4 + eko + e] : p.psi_e_in[0][qb + e];
                                 const float tc = corr(psi, c, fsub(get(hz1, e), get(hz, e)));
                                 if (own) p.psi_e_out[0][qb + e] = psi;
                                 set(ey, e, fsub(get(ey, e), fmul(get(cey, e), tc)));
                             }
                             if (j_lt) {
-                                float psi = p.psi_e_in[1][qb + e];
+                                float psi = xm ? sP(psl, 1)[er * EC + 4 + eko + e] : p.psi_e_in[1][qb + e];
                                 const float tc = corr(psi, c, fsub(get(hy1, e), get(hy, e)));
                                 if (own) p.psi_e_out[1][qb + e] = psi;
                                 set(ez, e, fadd(get(ez, e), fmul(get(cez, e), tc)));
@@ -562,37 +631,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
                             if (i_lt) {
-                                float psi = p.psi_e_in[2][qb + e];
+                                float psi = ym ? sP(psl, 0)[er * EC + 4 + eko + e] : p.psi_e_in[2][qb + e];
                                 const float tc = corr(psi, cye, fsub(get(hxj1, e), get(hx, e)));
                                 if (own) p.psi_e_out[2][qb + e] = psi;
                                 set(ez, e, fsub(get(ez, e), fmul(get(cez, e), tc)));
                             }
                             if (e ? k1_lt : k0_lt) {
-                                float psi = p.psi_e_in[3][qb + e];
+                                float psi = ym ? sP(psl, 1)[er * EC + 4 + eko + e] : p.psi_e_in[3][qb + e];
                                 const float tc = corr(psi, cye, fsub(get(hzj1, e), get(hz, e)));
                                 if (own) p.psi_e_out[3][qb + e] = psi;
                                 set(ex, e, fadd(get(ex, e), fmul(get(cex, e), tc)));
                             }
-                        }
-                    }
-#pragma unroll
-                    for (int e = 0; e < 2; e++) {  // z slab: ex -= cex (..dHy/dz..), ey += cey (..dHx/dz..)
-                        const int sz = e ? sze1 : sze0;
-                        if (sz < 0) continue;
-                        const Coef c = tab_coef(tabs, toff2, 2 * P2, 0, sz);
-                        const int64_t qz = (i * ny + jj) * 2 * P2 + sz;
-                        const int zs = er * 2 * P2 + sz;  // position in the staged z-psi box
-                        if (j_lt) {
-                            float psi = zstage ? sZ(st, 0)[zs] : p.psi_e_in[4][qz];
-                            const float tc = corr(psi, c, fsub(get(hyk1, e), get(hy, e)));
-                            if (own) p.psi_e_out[4][qz] = psi;
-                            set(ex, e, fsub(get(ex, e), fmul(get(cex, e), tc)));
-                        }
-                        if (i_lt) {
-                            float psi = zstage ? sZ(st, 1)[zs] : p.psi_e_in[5][qz];
-                            const float tc = corr(psi, c, fsub(get(hxk1, e), get(hx, e)));
-                            if (own) p.psi_e_out[5][qz] = psi;
-                            set(ey, e, fadd(get(ey, e), fmul(get(cey, e), tc)));
                         }
                     }
                     const uint32_t ij_here = ((uint32_t)i << 16) | (uint32_t)jj;
@@ -631,7 +680,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                     float2 hx = sub2(hx0, mul2(half, curl4x2(oez, ez_jm, oey, ey_km)));
                     float2 hy = sub2(hy0, mul2(half, curl4x2(oex, ex_km, oez, prev_ez)));
                     float2 hz = sub2(hz0, mul2(half, curl4x2(oey, prev_ey, oex, ex_jm)));
-                    if (!h_plain) {
+                    if (!h_plain || hmask) {
                         if (!(j_gt && k0_gt)) hx.x = hx0.x;
                         if (!(j_gt && k1_gt)) hx.y = hx0.y;
                         if (!(i_gt && k0_gt)) hy.x = hy0.x;
@@ -640,6 +689,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             hz.x = hz0.x;
                             hz.y = hz0.y;
                         }
+                    }
+                    if (!h_plain) {
                         if (sxh >= 0) {  // x slab: hy += (..dEz/dx..), hz -= (..dEy/dx..)
                             const Coef c = tab_coef(tabs, toff0, 2 * P0, 1, sxh);
                             const int64_t qb = ((int64_t)sxh * ny + jj) * nz + kk;
@@ -647,13 +698,13 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (e ? k1_gt : k0_gt) {
-                                    float psi = p.psi_h[0][qb + e];
+                                    float psi = xm ? sP(psl, 2)[er * EC + 4 + eko + e] : p.psi_h[0][qb + e];
                                     const float tc = corr(psi, c, fsub(get(oez, e), get(prev_ez, e)));
                                     p.psi_h[0][qb + e] = psi;
                                     set(hy, e, fadd(get(hy, e), fmul(0.5f, tc)));
                                 }
                                 if (j_gt) {
-                                    float psi = p.psi_h[1][qb + e];
+                                    float psi = xm ? sP(psl, 3)[er * EC + 4 + eko + e] : p.psi_h[1][qb + e];
                                     const float tc = corr(psi, c, fsub(get(oey, e), get(prev_ey, e)));
                                     p.psi_h[1][qb + e] = psi;
                                     set(hz, e, fsub(get(hz, e), fmul(0.5f, tc)));
@@ -667,37 +718,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (i_gt) {
-                                    float psi = p.psi_h[2][qb + e];
+                                    float psi = ym ? sP(psl, 2)[er * EC + 4 + eko + e] : p.psi_h[2][qb + e];
                                     const float tc = corr(psi, cyh, fsub(get(oex, e), get(ex_jm, e)));
                                     p.psi_h[2][qb + e] = psi;
                                     set(hz, e, fadd(get(hz, e), fmul(0.5f, tc)));
                                 }
                                 if (e ? k1_gt : k0_gt) {
-                                    float psi = p.psi_h[3][qb + e];
+                                    float psi = ym ? sP(psl, 3)[er * EC + 4 + eko + e] : p.psi_h[3][qb + e];
                                     const float tc = corr(psi, cyh, fsub(get(oez, e), get(ez_jm, e)));
                                     p.psi_h[3][qb + e] = psi;
                                     set(hx, e, fsub(get(hx, e), fmul(0.5f, tc)));
                                 }
-                            }
-                        }
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {  // z slab: hx += (..dEy/dz..), hy -= (..dEx/dz..)
-                            const int sz = e ? szh1 : szh0;
-                            if (sz < 0) continue;
-                            const Coef c = tab_coef(tabs, toff2, 2 * P2, 1, sz);
-                            const int64_t qz = (i * ny + jj) * 2 * P2 + sz;
-                            const int zs = er * 2 * P2 + sz;
-                            if (j_gt) {
-                                float psi = zstage ? sZ(st, 2)[zs] : p.psi_h[4][qz];
-                                const float tc = corr(psi, c, fsub(get(oey, e), get(ey_km, e)));
-                                p.psi_h[4][qz] = psi;
-                                set(hx, e, fadd(get(hx, e), fmul(0.5f, tc)));
-                            }
-                            if (i_gt) {
-                                float psi = zstage ? sZ(st, 3)[zs] : p.psi_h[5][qz];
-                                const float tc = corr(psi, c, fsub(get(oex, e), get(ex_km, e)));
-                                p.psi_h[5][qz] = psi;
-                                set(hy, e, fsub(get(hy, e), fmul(0.5f, tc)));
                             }
                         }
                     }
@@ -724,7 +755,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         }
         if (!aborted) {
             g0 += (uint32_t)nplanes;
+            gp0 += (uint32_t)(nplanes - 1);  // one psi phase per iteration
             issued_hi = -1;
+            psi_hi = -1;
         }
     }
 
@@ -737,6 +770,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 if (i_start_abort + q >= nx) continue;
                 const uint32_t G = g0 + (uint32_t)q;
                 mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr);
+            }
+            for (int64_t q = q_abort; q <= psi_hi; q++) {
+                const uint32_t Gp = gp0 + (uint32_t)q;
+                mbar_wait_bounded(&bars[NS + (Gp & 1)], (Gp >> 1) & 1, nullptr);
             }
         }
         __syncthreads();
@@ -759,127 +796,195 @@ __device__ __forceinline__ Coef gcoef(const float *b, const float *a, const floa
     return Coef{b[s], a[s], k[s]};
 }
 
-__global__ void __launch_bounds__(128) k_zband_e(const __grid_constant__ Params p) {
+// band cell counts of one grid: E (E z-slab nodes) and H (k in the H band)
+__host__ __device__ __forceinline__ int64_t zband_e_cells(const Params &p) {
+    const int P = p.P[2], f = (p.faces >> 4) & 1, b = (p.faces >> 5) & 1;
+    return p.zfix ? p.nx * p.ny * (int64_t)((f + b) * P) : 0;
+}
+__host__ __device__ __forceinline__ int64_t zband_h_start(const Params &p) {
+    const int P = p.P[2], f = (p.faces >> 4) & 1, b = (p.faces >> 5) & 1;
+    const int64_t fend = f ? P + 1 : 0;
+    return b ? (p.nz - P - 1 > fend + 1 ? p.nz - P - 1 : fend + 1) : p.nz;
+}
+__host__ __device__ __forceinline__ int64_t zband_h_cells(const Params &p) {
+    const int P = p.P[2], f = (p.faces >> 4) & 1;
+    const int64_t fend = f ? P + 1 : 0;
+    return p.zfix ? p.nx * p.ny * (fend + p.nz - zband_h_start(p)) : 0;
+}
+
+// E band cell number t of grid p at step tstep.  All loads come first, then
+// the arithmetic, then the stores: a store could alias a later load as far as
+// the compiler knows, so loads placed after stores would not be overlapped.
+__device__ __forceinline__ void zband_e_cell(const Params &p, int64_t tstep, int64_t t) {
     const int P = p.P[2];
     const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
     const int nf = front ? P : 0, nb = back ? P : 0, nk = nf + nb;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nx * p.ny * nk) return;
     const int kb = (int)(t % nk);
     const int64_t j = (t / nk) % p.ny, i = t / ((int64_t)nk * p.ny);
     const int64_t k = kb < nf ? 1 + kb : p.nz - P - 1 + (kb - nf);
     const int sz = kb < nf ? kb : P + (kb - nf);
     const int64_t c = i * p.sx + j * p.sy + k, qz = (i * p.ny + j) * 2 * P + sz;
     const Coef cf = gcoef(p.tb_e[2], p.ta_e[2], p.tk_e[2], sz);
-    const float *hx = p.in[3], *hy = p.in[4];
-    if (j < p.ny - 1) {  // ex -= cex (..dHy/dz..)
-        float psi = p.psi_e_in[4][qz];
-        const float tc = corr(psi, cf, fsub(hy[c + 1], hy[c]));
-        p.psi_e_out[4][qz] = psi;
-        float *ex = p.out[0] + c;
-        *ex = fsub(*ex, fmul(p.in_ce[0][c], tc));
+    const bool ux = j < p.ny - 1, uy = i < p.nx - 1;  // exz / eyz elements that exist
+    float px = 0.f, py = 0.f, hyd = 0.f, hxd = 0.f, ex = 0.f, ey = 0.f, cx = 0.f, cy = 0.f;
+    if (ux) {
+        px = p.psi_e_in[4][qz];
+        hyd = fsub(p.in[4][c + 1], p.in[4][c]);
+        ex = p.out[0][c];
+        cx = p.in_ce[0][c];
     }
-    if (i < p.nx - 1) {  // ey += cey (..dHx/dz..)
-        float psi = p.psi_e_in[5][qz];
-        const float tc = corr(psi, cf, fsub(hx[c + 1], hx[c]));
-        p.psi_e_out[5][qz] = psi;
-        float *ey = p.out[1] + c;
-        *ey = fadd(*ey, fmul(p.in_ce[1][c], tc));
+    if (uy) {
+        py = p.psi_e_in[5][qz];
+        hxd = fsub(p.in[3][c + 1], p.in[3][c]);
+        ey = p.out[1][c];
+        cy = p.in_ce[1][c];
     }
-    if (p.t >= 0 && p.t < p.namp)
-        for (int b = 0; b < p.nbsrc; b++) {  // sources on this cell, list order
-            const int s = p.bsrc[b];
+    if (ux) {  // ex -= cex (..dHy/dz..)
+        const float tc = corr(px, cf, hyd);
+        p.psi_e_out[4][qz] = px;
+        p.out[0][c] = fsub(ex, fmul(cx, tc));
+    }
+    if (uy) {  // ey += cey (..dHx/dz..)
+        const float tc = corr(py, cf, hxd);
+        p.psi_e_out[5][qz] = py;
+        p.out[1][c] = fadd(ey, fmul(cy, tc));
+    }
+    if (tstep >= 0 && tstep < p.namp) {  // sources on this cell, list order
+        const int n = p.nbsrc < 0 ? p.nsrc : p.nbsrc;
+        for (int b = 0; b < n; b++) {
+            const int s = p.nbsrc < 0 ? b : p.bsrc[b];
             if (p.src_ijk[3 * s] != i || p.src_ijk[3 * s + 1] != j || p.src_ijk[3 * s + 2] != k) continue;
             float *f = p.out[p.src_comp[s]] + c;
-            *f = fadd(*f, p.src_amp[(int64_t)s * p.namp + p.t]);
+            *f = fadd(*f, p.src_amp[(int64_t)s * p.namp + tstep]);
         }
+    }
 }
 
-__global__ void __launch_bounds__(128) k_zband_h(const __grid_constant__ Params p) {
+// H band cell number t of grid p: H recomputed from the input buffer and the
+// final E, with its curl, then the x, y and z CPML terms (in-kernel order)
+__device__ __forceinline__ void zband_h_cell(const Params &p, int64_t t) {
     const int P = p.P[2];
     const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
     const int64_t nz = p.nz, ny = p.ny, nx = p.nx;
-    const int64_t fend = front ? P + 1 : 0;                       // front band: k = 1 .. fend
-    const int64_t bstart = back ? max(nz - P - 1, fend + 1) : nz;  // back band: k = bstart .. nz-1
+    const int64_t fend = front ? P + 1 : 0;          // front band: k = 1 .. fend
+    const int64_t bstart = zband_h_start(p);         // back band: k = bstart .. nz-1
     const int nf = (int)fend, nk = nf + (int)(nz - bstart);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nx * ny * nk) return;
     const int kb = (int)(t % nk);
     const int64_t j = (t / nk) % ny, i = t / ((int64_t)nk * ny);
     const int64_t k = kb < nf ? 1 + kb : bstart + (kb - nf);
     const int64_t c = i * p.sx + j * p.sy + k;
-    const float *ex = p.out[0], *ey = p.out[1], *ez = p.out[2];
     const int f0 = p.faces & 1, b0 = (p.faces >> 1) & 1, f1 = (p.faces >> 2) & 1, b1 = (p.faces >> 3) & 1;
     const int sxh = slab_h(i, p.P[0], nx, f0, b0), syh = slab_h(j, p.P[1], ny, f1, b1);
     const int szh = slab_h(k, P, nz, front, back);
-    const int P0 = p.P[0], P1 = p.P[1];
-    // hx: curl, y slab (hx -=), z slab (hx +=)
-    {
-        float h = p.in[3][c];
-        if (j > 0 && k > 0) {
-            h = fsub(h, fmul(0.5f, curl4(ez[c], ez[c - p.sy], ey[c], ey[c - 1])));
-            if (syh >= 0) {
-                const int64_t q = (i * 2 * P1 + syh) * nz + k;
-                float psi = p.psi_h[3][q];
-                const float tc = corr(psi, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ez[c], ez[c - p.sy]));
-                p.psi_h[3][q] = psi;
-                h = fsub(h, fmul(0.5f, tc));
-            }
-            if (szh >= 0) {
-                const int64_t q = (i * ny + j) * 2 * P + szh;
-                float psi = p.psi_h[4][q];
-                const float tc = corr(psi, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ey[c], ey[c - 1]));
-                p.psi_h[4][q] = psi;
-                h = fadd(h, fmul(0.5f, tc));
-            }
-        }
-        p.out[3][c] = h;
+    const int P1 = p.P[1];
+    const bool ux = j > 0 && k > 0, uy = i > 0 && k > 0, uz = i > 0 && j > 0;  // update masks
+    // ---- loads
+    const float *__restrict__ ex = p.out[0];
+    const float *__restrict__ ey = p.out[1];
+    const float *__restrict__ ez = p.out[2];
+    const float hx0 = p.in[3][c], hy0 = p.in[4][c], hz0 = p.in[5][c];
+    const float ex_c = ex[c], ey_c = ey[c], ez_c = ez[c];
+    const float ez_j = j > 0 ? ez[c - p.sy] : 0.f, ex_j = j > 0 ? ex[c - p.sy] : 0.f;
+    const float ey_i = i > 0 ? ey[c - p.sx] : 0.f, ez_i = i > 0 ? ez[c - p.sx] : 0.f;
+    const float ey_k = ey[c - 1], ex_k = ex[c - 1];  // k >= 1 in the band
+    const int64_t qy = syh >= 0 ? (i * 2 * P1 + syh) * nz + k : 0;
+    const int64_t qx = sxh >= 0 ? ((int64_t)sxh * ny + j) * nz + k : 0;
+    const int64_t qz = szh >= 0 ? (i * ny + j) * 2 * P + szh : 0;
+    float ps_hxy = 0.f, ps_hxz = 0.f, ps_hyx = 0.f, ps_hyz = 0.f, ps_hzx = 0.f, ps_hzy = 0.f;
+    if (syh >= 0) {
+        if (ux) ps_hxy = p.psi_h[3][qy];
+        if (uz) ps_hzy = p.psi_h[2][qy];
     }
-    // hy: curl, x slab (hy +=), z slab (hy -=)
-    {
-        float h = p.in[4][c];
-        if (i > 0 && k > 0) {
-            h = fsub(h, fmul(0.5f, curl4(ex[c], ex[c - 1], ez[c], ez[c - p.sx])));
-            if (sxh >= 0) {
-                const int64_t q = ((int64_t)sxh * ny + j) * nz + k;
-                float psi = p.psi_h[0][q];
-                const float tc = corr(psi, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ez[c], ez[c - p.sx]));
-                p.psi_h[0][q] = psi;
-                h = fadd(h, fmul(0.5f, tc));
-            }
-            if (szh >= 0) {
-                const int64_t q = (i * ny + j) * 2 * P + szh;
-                float psi = p.psi_h[5][q];
-                const float tc = corr(psi, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ex[c], ex[c - 1]));
-                p.psi_h[5][q] = psi;
-                h = fsub(h, fmul(0.5f, tc));
-            }
-        }
-        p.out[4][c] = h;
+    if (sxh >= 0) {
+        if (uy) ps_hyx = p.psi_h[0][qx];
+        if (uz) ps_hzx = p.psi_h[1][qx];
     }
-    // hz: curl, x slab (hz -=), y slab (hz +=)
-    {
-        float h = p.in[5][c];
-        if (i > 0 && j > 0) {
-            h = fsub(h, fmul(0.5f, curl4(ey[c], ey[c - p.sx], ex[c], ex[c - p.sy])));
-            if (sxh >= 0) {
-                const int64_t q = ((int64_t)sxh * ny + j) * nz + k;
-                float psi = p.psi_h[1][q];
-                const float tc = corr(psi, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ey[c], ey[c - p.sx]));
-                p.psi_h[1][q] = psi;
-                h = fsub(h, fmul(0.5f, tc));
-            }
-            if (syh >= 0) {
-                const int64_t q = (i * 2 * P1 + syh) * nz + k;
-                float psi = p.psi_h[2][q];
-                const float tc = corr(psi, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ex[c], ex[c - p.sy]));
-                p.psi_h[2][q] = psi;
-                h = fadd(h, fmul(0.5f, tc));
-            }
-        }
-        p.out[5][c] = h;
+    if (szh >= 0) {
+        if (ux) ps_hxz = p.psi_h[4][qz];
+        if (uy) ps_hyz = p.psi_h[5][qz];
     }
-    (void)P0;
+    // ---- arithmetic
+    float hx = hx0, hy = hy0, hz = hz0;
+    if (ux) {
+        hx = fsub(hx, fmul(0.5f, curl4(ez_c, ez_j, ey_c, ey_k)));
+        if (syh >= 0)
+            hx = fsub(hx, fmul(0.5f, corr(ps_hxy, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ez_c, ez_j))));
+        if (szh >= 0)
+            hx = fadd(hx, fmul(0.5f, corr(ps_hxz, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ey_c, ey_k))));
+    }
+    if (uy) {
+        hy = fsub(hy, fmul(0.5f, curl4(ex_c, ex_k, ez_c, ez_i)));
+        if (sxh >= 0)
+            hy = fadd(hy, fmul(0.5f, corr(ps_hyx, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ez_c, ez_i))));
+        if (szh >= 0)
+            hy = fsub(hy, fmul(0.5f, corr(ps_hyz, gcoef(p.tb_h[2], p.ta_h[2], p.tk_h[2], szh), fsub(ex_c, ex_k))));
+    }
+    if (uz) {
+        hz = fsub(hz, fmul(0.5f, curl4(ey_c, ey_i, ex_c, ex_j)));
+        if (sxh >= 0)
+            hz = fsub(hz, fmul(0.5f, corr(ps_hzx, gcoef(p.tb_h[0], p.ta_h[0], p.tk_h[0], sxh), fsub(ey_c, ey_i))));
+        if (syh >= 0)
+            hz = fadd(hz, fmul(0.5f, corr(ps_hzy, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ex_c, ex_j))));
+    }
+    // ---- stores
+    p.out[3][c] = hx;
+    p.out[4][c] = hy;
+    p.out[5][c] = hz;
+    if (syh >= 0) {
+        if (ux) p.psi_h[3][qy] = ps_hxy;
+        if (uz) p.psi_h[2][qy] = ps_hzy;
+    }
+    if (sxh >= 0) {
+        if (uy) p.psi_h[0][qx] = ps_hyx;
+        if (uz) p.psi_h[1][qx] = ps_hzx;
+    }
+    if (szh >= 0) {
+        if (ux) p.psi_h[4][qz] = ps_hxz;
+        if (uy) p.psi_h[5][qz] = ps_hyz;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_zband_e(const __grid_constant__ Params p) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < zband_e_cells(p)) zband_e_cell(p, p.t, t);
+}
+
+__global__ void __launch_bounds__(128) k_zband_h(const __grid_constant__ Params p) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < zband_h_cells(p)) zband_h_cell(p, t);
+}
+
+// Batched band kernels: the band cells of all grids numbered consecutively
+// (off[s] = first cell of grid s); one launch each for E and H per step.
+struct BandBatch {
+    int32_t nsims, cur;
+    int64_t t;
+    const Params *params;   // [2*nsims], as BatchDesc
+    const int64_t *off;     // [nsims + 1]
+};
+
+__device__ __forceinline__ int band_sim(const BandBatch &d, int64_t t) {
+    int lo = 0, hi = d.nsims - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.off[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(128) k_zband_e_batch(const __grid_constant__ BandBatch d) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.off[d.nsims]) return;
+    const int s = band_sim(d, t);
+    zband_e_cell(d.params[2 * s + d.cur], d.t, t - d.off[s]);
+}
+
+__global__ void __launch_bounds__(128) k_zband_h_batch(const __grid_constant__ BandBatch d) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.off[d.nsims]) return;
+    const int s = band_sim(d, t);
+    zband_h_cell(d.params[2 * s + d.cur], t - d.off[s]);
 }
 
 }  // namespace fused
@@ -912,14 +1017,14 @@ static EncodeTiledFn get_encode_fn() {
 typedef void (*FusedKernel)(const TMaps, const Params, const BatchDesc);
 
 struct KernelEntry {
-    int ty, ns, threads, stage, enew;
+    int ty, ns, threads, stage, enew, psiring;
     FusedKernel fn, fn_batch;
 };
 
 template <int TY, int NS>
 static KernelEntry entry() {
     return KernelEntry{TY, NS, Layout<TY, NS>::THREADS, Layout<TY, NS>::STAGE, Layout<TY, NS>::ENEW,
-                       k_yee_fused<TY, NS, false>, k_yee_fused<TY, NS, true>};
+                       Layout<TY, NS>::PSIRING, k_yee_fused<TY, NS, false>, k_yee_fused<TY, NS, true>};
 }
 
 // Tile heights and pipeline depths compiled in (the autotuner picks among them).
@@ -1040,11 +1145,8 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         for (int q = 0; q < 6; q++) p.psi_h[q] = s->psi_h[q];
     }
     for (int q = 0; q < 3; q++) p.in_ce[q] = s->ce[q];
-    // z slab on the band kernels unless asked otherwise
-    const int zmode = tile ? tile->z_band : 0;
-    if (zmode < 0 || zmode > 2) { delete pl; return FDTD_ERR_ARG; }
-    const bool zslab = p.P[2] > 0 && ((p.faces >> 4) & 3);
-    p.zfix = (zslab && zmode != 1) ? 1 : 0;
+    // the z slab (when a z face has CPML) is finished by the band kernels
+    p.zfix = (p.P[2] > 0 && ((p.faces >> 4) & 3)) ? 1 : 0;
     if (src && src->nsrc > 0) {
         if (!all_nonnull(src->ijk, src->comp, src->amp) || src->namp < 0) { delete pl; return FDTD_ERR_ARG; }
         p.nsrc = src->nsrc; p.src_ijk = src->ijk; p.src_comp = src->comp; p.src_amp = src->amp; p.namp = src->namp;
@@ -1061,9 +1163,8 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
                 const int64_t sk = hijk[3 * a + 2];
                 const bool node = (f2 && sk >= 1 && sk <= P2) || (b2 && sk >= g.nz - P2 - 1 && sk <= g.nz - 2);
                 if (!node) continue;
-                if (p.nbsrc == MAX_BAND_SRC) {  // too many: keep the z slab inside the fused kernel
-                    p.zfix = 0;
-                    p.nbsrc = 0;
+                if (p.nbsrc == MAX_BAND_SRC) {  // too many for the list: the band kernel scans all sources
+                    p.nbsrc = -1;
                     break;
                 }
                 p.bsrc[p.nbsrc++] = a;
@@ -1120,34 +1221,40 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         }
         if (st != FDTD_OK) { delete pl; return st; }
     }
-    // z-slab psi staged by TMA: needs rows of 2P floats that are 16-byte multiples
-    const int P2 = p.P[2];
-    const bool zpsi = !p.zfix && P2 > 0 && (2 * P2 * 4) % 16 == 0 && 2 * P2 <= 256 && g.ny <= 0x7fffffff;
-    int zbox = 0;
-    if (zpsi) {
-        const int box_bytes = (ty + 1) * 2 * P2 * 4;
-        zbox = (box_bytes + 127) / 128 * 128;
-        p.tx_z = 4u * (uint32_t)box_bytes;
+    p.stage_bytes = ke->stage;
+    // x/y psi slabs through TMA: rows of nz floats must be 16-byte multiples
+    {
+        const int P0 = p.P[0], P1 = p.P[1];
+        bool ok = (P0 > 0 || P1 > 0) && g.nz % 4 == 0;
+        for (int q = 0; q < 2 && ok; q++) {
+            if (P0 > 0) ok = aligned16(s->psi_e[0][q]) && aligned16(s->psi_e[1][q]) && aligned16(s->psi_h[q]);
+            if (ok && P1 > 0)
+                ok = aligned16(s->psi_e[0][2 + q]) && aligned16(s->psi_e[1][2 + q]) && aligned16(s->psi_h[2 + q]);
+        }
         int st = FDTD_OK;
-        for (int b = 0; b < 2 && st == FDTD_OK; b++)
+        const int ec = EC, by = ty + 1;
+        for (int b = 0; b < 2 && ok && st == FDTD_OK; b++)
             for (int q = 0; q < 2 && st == FDTD_OK; q++) {
-                st = encode_map3(enc, &pl->maps[b].zpe[q], s->psi_e[b][4 + q], 2 * P2, g.ny, g.nx, 2 * P2,
-                                 g.ny * 2 * P2, 2 * P2, ty + 1, CU_TENSOR_MAP_L2_PROMOTION_NONE);
-                if (st == FDTD_OK)
-                    st = encode_map3(enc, &pl->maps[b].zph[q], s->psi_h[4 + q], 2 * P2, g.ny, g.nx, 2 * P2,
-                                     g.ny * 2 * P2, 2 * P2, ty + 1, CU_TENSOR_MAP_L2_PROMOTION_NONE);
+                if (P0 > 0) {
+                    st = encode_map3(enc, &pl->maps[b].xpe[q], s->psi_e[b][q], g.nz, g.ny, 2 * P0, g.nz,
+                                     g.ny * g.nz, ec, by, CU_TENSOR_MAP_L2_PROMOTION_L2_128B);
+                    if (st == FDTD_OK)
+                        st = encode_map3(enc, &pl->maps[b].xph[q], s->psi_h[q], g.nz, g.ny, 2 * P0, g.nz,
+                                         g.ny * g.nz, ec, by, CU_TENSOR_MAP_L2_PROMOTION_L2_128B);
+                }
+                if (P1 > 0 && st == FDTD_OK) {
+                    st = encode_map3(enc, &pl->maps[b].ype[q], s->psi_e[b][2 + q], g.nz, 2 * P1, g.nx, g.nz,
+                                     2 * P1 * g.nz, ec, by, CU_TENSOR_MAP_L2_PROMOTION_L2_128B);
+                    if (st == FDTD_OK)
+                        st = encode_map3(enc, &pl->maps[b].yph[q], s->psi_h[2 + q], g.nz, 2 * P1, g.nx, g.nz,
+                                         2 * P1 * g.nz, ec, by, CU_TENSOR_MAP_L2_PROMOTION_L2_128B);
+                }
             }
         if (st != FDTD_OK) { delete pl; return st; }
-        for (int q = 0; q < 2; q++)
-            if (!aligned16(s->psi_h[4 + q]) || !aligned16(s->psi_e[0][4 + q]) || !aligned16(s->psi_e[1][4 + q])) {
-                delete pl; return FDTD_ERR_ALIGN;
-            }
+        p.xypsi = ok ? 1 : 0;
     }
-    p.zpsi = zpsi ? 1 : 0;
-    p.zbox = zbox;
-    p.stage_bytes = ke->stage + 4 * zbox;
     const int tab_bytes = 6 * 2 * (p.P[0] + p.P[1] + p.P[2]) * 4;
-    pl->smem = ns * p.stage_bytes + ke->enew + 128 /*barriers*/ + tab_bytes + 128 /*align slack*/;
+    pl->smem = ns * p.stage_bytes + ke->enew + 128 /*barriers*/ + ke->psiring + tab_bytes + 128 /*align slack*/;
     int dev = 0, nsm = 0, occ = 0, optin = 0;
     cudaFuncAttributes fa;
     cudaError_t e = cudaGetDevice(&dev);
@@ -1184,11 +1291,7 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
         pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
         if (p.zfix) {
             for (int q = 0; q < 6; q++) p.in[q] = pl->f[in][q];
-            const int P2 = p.P[2], f2 = (p.faces >> 4) & 1, b2 = (p.faces >> 5) & 1;
-            const int64_t ne = pl->g.nx * pl->g.ny * ((f2 + b2) * (int64_t)P2);
-            const int64_t fend = f2 ? P2 + 1 : 0;
-            const int64_t bstart = b2 ? std::max<int64_t>(pl->g.nz - P2 - 1, fend + 1) : pl->g.nz;
-            const int64_t nh = pl->g.nx * pl->g.ny * (fend + pl->g.nz - bstart);
+            const int64_t ne = zband_e_cells(p), nh = zband_h_cells(p);
             k_zband_e<<<(unsigned)((ne + 127) / 128), 128, 0, st>>>(p);
             k_zband_h<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(p);
         }
@@ -1243,7 +1346,10 @@ struct fdtd_batch_plan {
     int stage_bytes;
     TMaps *d_maps;
     Params *d_params;
-    int64_t *d_off;
+    int64_t *d_off;        // work-item offsets of the fused kernel
+    int64_t *d_band_e;     // band cell offsets (E, H) of the band kernels
+    int64_t *d_band_h;
+    int64_t band_e, band_h;  // band cells in all grids
 };
 
 static size_t batch_ws_layout(int32_t nsims, size_t *off_params, size_t *off_items) {
@@ -1253,8 +1359,8 @@ static size_t batch_ws_layout(int32_t nsims, size_t *off_params, size_t *off_ite
     *off_params = o;
     o += (size_t)2 * nsims * sizeof(Params);
     o = (o + 63) / 64 * 64;
-    *off_items = o;
-    o += (size_t)(nsims + 1) * sizeof(int64_t);
+    *off_items = o;  // work-item offsets, then E and H band cell offsets
+    o += (size_t)3 * (nsims + 1) * sizeof(int64_t);
     return o;
 }
 
@@ -1276,16 +1382,14 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     if (workspace_bytes < need) return FDTD_ERR_CAPACITY;
     std::vector<TMaps> maps((size_t)2 * nsims);
     std::vector<Params> params((size_t)2 * nsims);
-    std::vector<int64_t> off((size_t)nsims + 1, 0);
+    std::vector<int64_t> off((size_t)3 * (nsims + 1), 0);
+    int64_t *boff_e = off.data() + (nsims + 1), *boff_h = off.data() + 2 * (nsims + 1);
     const KernelEntry *ke = nullptr;
     int stage_bytes = 0, tab_bytes = 0;
     for (int32_t s = 0; s < nsims; s++) {
         fdtd_yee_plan *pl = nullptr;
-        // one launch per step for the whole batch: the z slab stays inside the fused kernel
-        fdtd_tile t1 = tile ? *tile : fdtd_tile{};
-        t1.z_band = 1;
         const int st = fdtd_yee_plan_create(&pl, &grids[s], &states[s], cpmls ? &cpmls[s] : nullptr,
-                                            srcs ? &srcs[s] : nullptr, &t1, status_dev, cur);
+                                            srcs ? &srcs[s] : nullptr, tile, status_dev, cur);
         if (st != FDTD_OK) return st;
         ke = pl->k;
         stage_bytes = std::max(stage_bytes, pl->base.stage_bytes);
@@ -1296,11 +1400,14 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
                 p.out[q] = pl->f[1 - b][q];
                 p.psi_e_in[q] = pl->psi_e[b][q];
                 p.psi_e_out[q] = pl->psi_e[1 - b][q];
+                p.in[q] = pl->f[b][q];
             }
             params[2 * s + b] = p;
             maps[2 * s + b] = pl->maps[b];
         }
         off[s + 1] = off[s] + pl->nitems;
+        boff_e[s + 1] = boff_e[s] + zband_e_cells(pl->base);
+        boff_h[s + 1] = boff_h[s] + zband_h_cells(pl->base);
         fdtd_yee_plan_destroy(pl);
     }
     unsigned char *ws = static_cast<unsigned char *>(workspace);
@@ -1313,12 +1420,16 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     bp->nsims = nsims;
     bp->k = ke;
     bp->stage_bytes = stage_bytes;
-    bp->smem = ke->ns * stage_bytes + ke->enew + 128 + tab_bytes + 128;
+    bp->smem = ke->ns * stage_bytes + ke->enew + 128 + ke->psiring + tab_bytes + 128;
     bp->cur = cur;
     bp->nitems = off[nsims];
     bp->d_maps = reinterpret_cast<TMaps *>(ws);
     bp->d_params = reinterpret_cast<Params *>(ws + off_p);
     bp->d_off = reinterpret_cast<int64_t *>(ws + off_i);
+    bp->d_band_e = bp->d_off + (nsims + 1);
+    bp->d_band_h = bp->d_off + 2 * (nsims + 1);
+    bp->band_e = boff_e[nsims];
+    bp->band_h = boff_h[nsims];
     int dev = 0, nsm = 0, occ = 0, optin = 0;
     cudaFuncAttributes fa;
     e = cudaGetDevice(&dev);
@@ -1355,6 +1466,12 @@ int fdtd_batch_plan_run(fdtd_batch_plan *bp, int64_t t0, int64_t nsteps, void *s
         bd.item_off = bp->d_off;
         bd.stage_bytes = bp->stage_bytes;
         bp->k->fn_batch<<<bp->nblocks, bp->k->threads, bp->smem, st>>>(dummy_maps, dummy, bd);
+        if (bp->band_e > 0 || bp->band_h > 0) {
+            BandBatch d{bp->nsims, bp->cur, t0 + n, bp->d_params, bp->d_band_e};
+            if (bp->band_e > 0) k_zband_e_batch<<<(unsigned)((bp->band_e + 127) / 128), 128, 0, st>>>(d);
+            d.off = bp->d_band_h;
+            if (bp->band_h > 0) k_zband_h_batch<<<(unsigned)((bp->band_h + 127) / 128), 128, 0, st>>>(d);
+        }
         FDTD_TRY(check_launch());
         bp->cur = 1 - bp->cur;
     }

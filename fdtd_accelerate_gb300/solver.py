@@ -115,7 +115,7 @@ class YeeSolver:
             st = self._state_struct()
             cp = self.cpml.struct()
             src = self.sources.struct()
-            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0, 0))[:6])
+            tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             h = C.c_void_p()
             with torch.cuda.device(self.device):
                 N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),

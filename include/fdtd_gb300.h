@@ -141,16 +141,14 @@ typedef struct {
  * or 16 cells; the tile is 64 cells wide in z), x planes per work item,
  * resident CTAs per SM (persistent grid), pipeline stages (planes staged in
  * shared memory), L2 promotion of the tile loads (0 = 256 B, 1 = none,
- * 2 = 64 B, 3 = 128 B), z-slab CPML path (0 = default, 1 = inside the
- * fused kernel, 2 = two band kernels after it; the default is 2 for single
- * grids and 1 in batched plans).  Both z paths give identical results. */
+ * 2 = 64 B, 3 = 128 B).  x_chunk 0 picks a chunk that gives every SM
+ * about three work items. */
 typedef struct {
     int32_t tile_y;
     int32_t x_chunk;
     int32_t ctas_per_sm;
     int32_t stages;
     int32_t l2_promotion;
-    int32_t z_band;
 } fdtd_tile;
 
 typedef struct fdtd_yee_plan fdtd_yee_plan;

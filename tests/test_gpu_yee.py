@@ -169,9 +169,9 @@ def _oracle_sim(work_shape, ce, npml, faces, sources, init):
     ((40, 40, 200), 4, (8, 16, 0, 4)),   # interior tiles take the packed fast path
     ((30, 44, 260), 3, None),
     ((24, 40, 200), 0, (4, 8, 0, 4)),
-    ((37, 29, 45), 5, (8, 16, 0, 3, 0, 1)),   # z slab inside the fused kernel
-    ((40, 40, 200), 4, (8, 16, 0, 4, 0, 1)),
-    ((30, 44, 260), 3, (16, 8, 1, 3, 0, 2)),  # z slab on the band kernels
+    ((37, 29, 45), 5, (8, 16, 0, 3, 2)),      # L2 promotion variants
+    ((40, 40, 200), 4, (8, 16, 0, 4, 1)),
+    ((30, 44, 70), 14, (16, 8, 1, 3)),        # z band wider than half a tile
 ])
 def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     from fdtd_accelerate_gb300 import configs

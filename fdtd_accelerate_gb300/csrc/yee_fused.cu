@@ -343,32 +343,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         }
         s_abort = 0;
     }
-    // per-grid values (loop invariant for a single grid; reloaded when a batched
-    // item switches grid)
-    int64_t nx, ny, nz;
-    int front0, back0, front1, back1, front2, back2, P0, P1, P2, toff1, toff2;
-    const int toff0 = 0;
-    auto load_derived = [&]() {
-        nx = p.nx;
-        ny = p.ny;
-        nz = p.nz;
-        front0 = p.faces & 1;
-        back0 = (p.faces >> 1) & 1;
-        front1 = (p.faces >> 2) & 1;
-        back1 = (p.faces >> 3) & 1;
-        front2 = (p.faces >> 4) & 1;
-        back2 = (p.faces >> 5) & 1;
-        P0 = p.P[0];
-        P1 = p.P[1];
-        P2 = p.P[2];
-        // offsets of each axis's six tables (b_e, a_e, km_e, b_h, a_h, km_h)
-        toff1 = 6 * 2 * P0;
-        toff2 = toff1 + 6 * 2 * P1;
-    };
-    if (!BATCH) {
-        stage_tables();
-        load_derived();
-    }
+    // Per-grid values are read from p at each use: constant-bank operands for a
+    // single grid, shared-memory loads of the current grid's copy in a batch
+    // (held in registers they would be live across the whole item loop).
+    if (!BATCH) stage_tables();
 
     uint32_t g0 = 0;          // planes this CTA has issued before the current item
     uint32_t gp0 = 0;         // psi ring phases this CTA has used before the current item
@@ -408,7 +386,6 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 }
                 stage_tables();
                 __syncthreads();
-                load_derived();
                 cur_sim = lo;
             }
         }
@@ -416,7 +393,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const int64_t tzi = item % p.ntz, tyi = (item / p.ntz) % p.nty, xci = item / ((int64_t)p.ntz * p.nty);
         const int64_t k0 = tzi * TZ, j0 = tyi * TY;
         const int64_t x0 = xci * p.x_chunk;
-        const int64_t x1 = min(x0 + (int64_t)p.x_chunk, nx);
+        const int64_t x1 = min(x0 + (int64_t)p.x_chunk, p.nx);
         const int64_t i_start = x0 > 0 ? x0 - 1 : 0;
         const int64_t nplanes = x1 - i_start + 1;  // planes i_start .. x1 (H(x1) feeds E(x1-1))
         // Tile-uniform: no grid edge and no y/z CPML slab inside the tile's E/H region.
@@ -424,37 +401,37 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         // Tile-uniform: no y CPML slab among the tile's rows.  Grid edges are
         // handled on the plain path by per-lane masks, and the z slab is the
         // band kernels' work, so z-slab tiles are plain here too.
-        const bool y_plain = P1 == 0 || ((j0 - 1 > P1 || !front1) && (j0 + TY - 1 < ny - P1 - 1 || !back1));
+        const bool y_plain = p.P[1] == 0 || ((j0 - 1 > p.P[1] || !((p.faces >> 2) & 1)) && (j0 + TY - 1 < p.ny - p.P[1] - 1 || !((p.faces >> 3) & 1)));
 
         // y psi by TMA for tiles whose y-slab rows lie on one side (box row r <-> j0-1+r)
-        const bool ye_f = front1 && P1 > 0 && j0 - 1 <= P1 && j0 + TY - 1 >= 1;
-        const bool ye_b = back1 && P1 > 0 && j0 + TY - 1 >= ny - P1 - 1 && j0 - 1 <= ny - 2;
-        const bool yh_f = front1 && P1 > 0 && j0 <= P1 && j0 + TY - 1 >= 1;
-        const bool yh_b = back1 && P1 > 0 && j0 + TY - 1 >= ny - P1 && j0 <= ny - 1;
+        const bool ye_f = ((p.faces >> 2) & 1) && p.P[1] > 0 && j0 - 1 <= p.P[1] && j0 + TY - 1 >= 1;
+        const bool ye_b = ((p.faces >> 3) & 1) && p.P[1] > 0 && j0 + TY - 1 >= p.ny - p.P[1] - 1 && j0 - 1 <= p.ny - 2;
+        const bool yh_f = ((p.faces >> 2) & 1) && p.P[1] > 0 && j0 <= p.P[1] && j0 + TY - 1 >= 1;
+        const bool yh_b = ((p.faces >> 3) & 1) && p.P[1] > 0 && j0 + TY - 1 >= p.ny - p.P[1] && j0 <= p.ny - 1;
         const bool ytile = p.xypsi && (ye_f || ye_b || yh_f || yh_b) && !((ye_f || yh_f) && (ye_b || yh_b));
 
         // ---- per-item, per-thread cell description (pair at row j, columns k, k+1) ----
         const int64_t jj = j0 - 1 + er, kk = k0 + eko;
-        const bool row_in = jj >= 0 && jj < ny;
-        const bool in0 = row_in && kk >= 0 && kk < nz, in1 = row_in && kk + 1 >= 0 && kk + 1 < nz;
-        const bool j_lt = jj < ny - 1, j_gt = jj > 0;
-        const bool k0_lt = kk < nz - 1, k1_lt = kk + 1 < nz - 1, k0_gt = kk > 0, k1_gt = kk + 1 > 0;
+        const bool row_in = jj >= 0 && jj < p.ny;
+        const bool in0 = row_in && kk >= 0 && kk < p.nz, in1 = row_in && kk + 1 >= 0 && kk + 1 < p.nz;
+        const bool j_lt = jj < p.ny - 1, j_gt = jj > 0;
+        const bool k0_lt = kk < p.nz - 1, k1_lt = kk + 1 < p.nz - 1, k0_gt = kk > 0, k1_gt = kk + 1 > 0;
         // lanes with a cell outside an update region (grid edges); the i edges are plane-uniform
         const bool emask = !(j_lt && k0_lt && k1_lt), hmask = !(j_gt && k0_gt && k1_gt);
-        const int sye = row_in ? slab_e(jj, P1, ny, front1, back1) : -1;
-        const int syh = row_in ? slab_h(jj, P1, ny, front1, back1) : -1;
+        const int sye = row_in ? slab_e(jj, p.P[1], p.ny, ((p.faces >> 2) & 1), ((p.faces >> 3) & 1)) : -1;
+        const int syh = row_in ? slab_h(jj, p.P[1], p.ny, ((p.faces >> 2) & 1), ((p.faces >> 3) & 1)) : -1;
         // H cells of the z band: left to the band kernel (no psi_h update here)
-        const bool hb0 = p.zfix && in_zband_h(kk, P2, nz, front2, back2);
-        const bool hb1 = p.zfix && in_zband_h(kk + 1, P2, nz, front2, back2);
+        const bool hb0 = p.zfix && in_zband_h(kk, p.P[2], p.nz, ((p.faces >> 4) & 1), ((p.faces >> 5) & 1));
+        const bool hb1 = p.zfix && in_zband_h(kk + 1, p.P[2], p.nz, ((p.faces >> 4) & 1), ((p.faces >> 5) & 1));
 
         auto issue = [&](int64_t q) {
             const int64_t plane = i_start + q;
             const int st = (int)((g0 + q) % NS);
             uint64_t *bar = &bars[st];
             issued_hi = q;
-            if (plane >= nx) {
-                // Past the last plane: H(nx) only feeds E components that are
-                // never updated at i = nx-1; complete the phase without a copy.
+            if (plane >= p.nx) {
+                // Past the last plane: H(p.nx) only feeds E components that are
+                // never updated at i = p.nx-1; complete the phase without a copy.
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
                 return;
             }
@@ -472,10 +449,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             uint64_t *bar = &bars[NS + sl];
             psi_hi = q;
             const int64_t plane = i_start + q;
-            const int xse = plane < nx ? slab_e(plane, P0, nx, front0, back0) : -1;
-            const int xsh = plane < nx ? slab_h(plane, P0, nx, front0, back0) : -1;
+            const int xse = plane < p.nx ? slab_e(plane, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1)) : -1;
+            const int xsh = plane < p.nx ? slab_h(plane, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1)) : -1;
             const bool xm = p.xypsi && (xse >= 0 || xsh >= 0);
-            const bool ym = !xm && ytile && plane < nx;
+            const bool ym = !xm && ytile && plane < p.nx;
             const bool ye = ye_f || ye_b, yh = yh_f || yh_b;
             const uint32_t nbox = xm ? 2u * (xse >= 0) + 2u * (xsh >= 0) : (ym ? 2u * ye + 2u * yh : 0u);
             if (nbox == 0) {
@@ -495,12 +472,12 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 }
             } else {
                 if (ye) {
-                    const int ys = ye_b ? (int)(P1 + (j0 - 1) - (ny - P1 - 1)) : (int)(j0 - 2);
+                    const int ys = ye_b ? (int)(p.P[1] + (j0 - 1) - (p.ny - p.P[1] - 1)) : (int)(j0 - 2);
                     tma_load_3d(sP(sl, 0), &maps.ype[0], bar, kc, ys, xc);
                     tma_load_3d(sP(sl, 1), &maps.ype[1], bar, kc, ys, xc);
                 }
                 if (yh) {
-                    const int ys = yh_b ? (int)(P1 + (j0 - 1) - (ny - P1)) : (int)(j0 - 2);
+                    const int ys = yh_b ? (int)(p.P[1] + (j0 - 1) - (p.ny - p.P[1])) : (int)(j0 - 2);
                     tma_load_3d(sP(sl, 2), &maps.yph[0], bar, kc, ys, xc);
                     tma_load_3d(sP(sl, 3), &maps.yph[1], bar, kc, ys, xc);
                 }
@@ -515,7 +492,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 for (int s = 0; s < p.nsrc; s++) {
                     const int64_t si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
                     if (si >= i_start && si < x1 && sj >= j0 - 1 && sj < j0 + TY && sk >= k0 - 1 && sk < k0 + TZ &&
-                        !(p.zfix && slab_e(sk, P2, nz, front2, back2) >= 0)) {
+                        !(p.zfix && slab_e(sk, p.P[2], p.nz, ((p.faces >> 4) & 1), ((p.faces >> 5) & 1)) >= 0)) {
                         if (n < MAX_LOCAL_SRC) {
                             s_ls_ij[n] = ((uint32_t)si << 16) | (uint32_t)sj;
                             s_ls_kc[n] = (int)(sk << 2) | p.src_comp[s];
@@ -568,8 +545,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             }
 
             // plane-uniform CPML (x) and masks
-            const int sxe = slab_e(i, P0, nx, front0, back0), sxh = slab_h(i, P0, nx, front0, back0);
-            const bool i_lt = i < nx - 1, i_gt = i > 0;
+            const int sxe = slab_e(i, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1)), sxh = slab_h(i, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1));
+            const bool i_lt = i < p.nx - 1, i_gt = i > 0;
             const bool e_plain = tile_plain && i_lt && sxe < 0;
             const bool h_plain = tile_plain && i_gt && sxh < 0;
             // where this plane's x/y psi come from (the choice of issue_psi)
@@ -605,8 +582,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 if (!e_plain) {
                     const bool own = own_row && i >= x0;
                     if (sxe >= 0) {  // x slab: ey -= cey (..dHz/dx..), ez += cez (..dHy/dx..)
-                        const Coef c = tab_coef(tabs, toff0, 2 * P0, 0, sxe);
-                        const int64_t qb = ((int64_t)sxe * ny + jj) * nz + kk;
+                        const Coef c = tab_coef(tabs, 0, 2 * p.P[0], 0, sxe);
+                        const int64_t qb = ((int64_t)sxe * p.ny + jj) * p.nz + kk;
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
@@ -625,8 +602,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         }
                     }
                     if (sye >= 0) {  // y slab: ez -= cez (..dHx/dy..), ex += cex (..dHz/dy..)
-                        const Coef cye = tab_coef(tabs, toff1, 2 * P1, 0, sye);
-                        const int64_t qb = (i * 2 * P1 + sye) * nz + kk;
+                        const Coef cye = tab_coef(tabs, (12 * p.P[0]), 2 * p.P[1], 0, sye);
+                        const int64_t qb = (i * 2 * p.P[1] + sye) * p.nz + kk;
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
@@ -692,8 +669,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                     }
                     if (!h_plain) {
                         if (sxh >= 0) {  // x slab: hy += (..dEz/dx..), hz -= (..dEy/dx..)
-                            const Coef c = tab_coef(tabs, toff0, 2 * P0, 1, sxh);
-                            const int64_t qb = ((int64_t)sxh * ny + jj) * nz + kk;
+                            const Coef c = tab_coef(tabs, 0, 2 * p.P[0], 1, sxh);
+                            const int64_t qb = ((int64_t)sxh * p.ny + jj) * p.nz + kk;
 #pragma unroll
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
@@ -712,8 +689,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             }
                         }
                         if (syh >= 0) {  // y slab: hz += (..dEx/dy..), hx -= (..dEz/dy..)
-                            const Coef cyh = tab_coef(tabs, toff1, 2 * P1, 1, syh);
-                            const int64_t qb = (i * 2 * P1 + syh) * nz + kk;
+                            const Coef cyh = tab_coef(tabs, (12 * p.P[0]), 2 * p.P[1], 1, syh);
+                            const int64_t qb = (i * 2 * p.P[1] + syh) * p.nz + kk;
 #pragma unroll
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
@@ -767,7 +744,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             // Let the copies still in flight land before the CTA's shared
             // memory is released (each wait bounded).
             for (int64_t q = q_abort; q <= issued_hi; q++) {
-                if (i_start_abort + q >= nx) continue;
+                if (i_start_abort + q >= p.nx) continue;
                 const uint32_t G = g0 + (uint32_t)q;
                 mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr);
             }

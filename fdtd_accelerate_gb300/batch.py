@@ -24,8 +24,8 @@ from .solver import YeeSolver
 __all__ = ["BatchSolver", "TILE_CANDIDATES", "tune_cache_path"]
 
 # (tile_y, x_chunk, ctas_per_sm, stages) candidates for the autotuner
-TILE_CANDIDATES = ((8, 128, 0, 3), (8, 64, 0, 3), (8, 32, 0, 3), (4, 64, 0, 4), (16, 64, 0, 3),
-                   (8, 64, 0, 4), (4, 32, 0, 4))
+TILE_CANDIDATES = ((8, 128, 0, 3), (8, 64, 0, 3), (8, 32, 0, 3), (8, 16, 0, 3), (4, 64, 0, 4), (4, 32, 0, 4),
+                   (16, 128, 0, 3), (16, 64, 0, 3), (16, 32, 0, 3), (16, 16, 0, 3), (8, 64, 0, 4))
 
 
 def tune_cache_path():

@@ -124,6 +124,9 @@ struct BatchDesc {
     const TMaps *maps;       // [2*nsims]: tensor maps of grid s, input buffer b
     const int64_t *item_off; // [nsims + 1]
     int32_t stage_bytes;     // pipeline stage size (max over grids)
+    // work queue: [0] next item, [1] CTAs finished; zero between launches (the
+    // last CTA to finish clears both)
+    int32_t *queue;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -357,7 +360,17 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     const int64_t nitems = BATCH ? bd.item_off[bd.nsims] : (int64_t)pk.ntz * pk.nty * pk.nxc;
     int cur_sim = -1;
 
-    for (int64_t gitem = blockIdx.x; gitem < nitems && !aborted; gitem += gridDim.x) {
+    // Batched launches take items from a queue (grids ordered with the longest
+    // items first, so the short ones fill the tail); a single grid walks its
+    // uniform items in a fixed stride.
+    __shared__ int s_item;
+    int64_t gitem = blockIdx.x;
+    if (BATCH) {
+        if (tid == 0) s_item = atomicAdd(&bd.queue[0], 1);
+        __syncthreads();
+        gitem = s_item;
+    }
+    while (gitem < nitems && !aborted) {
         int64_t item = gitem;
         const TMaps *mp = &mk;
         if (BATCH) {
@@ -730,14 +743,30 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 prev_ez = oez;
             }
         }
-        if (!aborted) {
-            g0 += (uint32_t)nplanes;
-            gp0 += (uint32_t)(nplanes - 1);  // one psi phase per iteration
-            issued_hi = -1;
-            psi_hi = -1;
+        if (aborted) break;
+        g0 += (uint32_t)nplanes;
+        gp0 += (uint32_t)(nplanes - 1);  // one psi phase per iteration
+        issued_hi = -1;
+        psi_hi = -1;
+        if (BATCH) {
+            __syncthreads();  // every thread has read s_item
+            if (tid == 0) s_item = atomicAdd(&bd.queue[0], 1);
+            __syncthreads();
+            gitem = s_item;
+        } else {
+            gitem += gridDim.x;
         }
     }
 
+    if (BATCH && tid == 0) {
+        // the last CTA to finish clears the queue for the next launch
+        __threadfence();
+        if (atomicAdd(&bd.queue[1], 1) == (int)gridDim.x - 1) {
+            bd.queue[0] = 0;
+            bd.queue[1] = 0;
+            __threadfence();
+        }
+    }
     if (aborted) {
         if (tid == 0) {
             atomicExch(p.status, FDTD_ERR_TIMEOUT);
@@ -1327,6 +1356,7 @@ struct fdtd_batch_plan {
     int64_t *d_band_e;     // band cell offsets (E, H) of the band kernels
     int64_t *d_band_h;
     int64_t band_e, band_h;  // band cells in all grids
+    int32_t *d_queue;        // work queue of the fused kernel (2 counters)
 };
 
 static size_t batch_ws_layout(int32_t nsims, size_t *off_params, size_t *off_items) {
@@ -1336,8 +1366,9 @@ static size_t batch_ws_layout(int32_t nsims, size_t *off_params, size_t *off_ite
     *off_params = o;
     o += (size_t)2 * nsims * sizeof(Params);
     o = (o + 63) / 64 * 64;
-    *off_items = o;  // work-item offsets, then E and H band cell offsets
+    *off_items = o;  // work-item offsets, then E and H band cell offsets, then the queue
     o += (size_t)3 * (nsims + 1) * sizeof(int64_t);
+    o += 64;
     return o;
 }
 
@@ -1363,10 +1394,19 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     int64_t *boff_e = off.data() + (nsims + 1), *boff_h = off.data() + 2 * (nsims + 1);
     const KernelEntry *ke = nullptr;
     int stage_bytes = 0, tab_bytes = 0;
+    // grids with the longest items (x planes per chunk, then tile rows) come first
+    std::vector<int32_t> order((size_t)nsims);
+    for (int32_t s = 0; s < nsims; s++) order[s] = s;
+    auto item_len = [&](int32_t s) {
+        const int64_t xc = tile && tile->x_chunk ? tile->x_chunk : 128;
+        return std::min<int64_t>(xc, grids[s].nx) * 65536 + std::min<int64_t>(grids[s].ny, 65535);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return item_len(a) > item_len(b); });
     for (int32_t s = 0; s < nsims; s++) {
+        const int32_t u = order[s];
         fdtd_yee_plan *pl = nullptr;
-        const int st = fdtd_yee_plan_create(&pl, &grids[s], &states[s], cpmls ? &cpmls[s] : nullptr,
-                                            srcs ? &srcs[s] : nullptr, tile, status_dev, cur);
+        const int st = fdtd_yee_plan_create(&pl, &grids[u], &states[u], cpmls ? &cpmls[u] : nullptr,
+                                            srcs ? &srcs[u] : nullptr, tile, status_dev, cur);
         if (st != FDTD_OK) return st;
         ke = pl->k;
         stage_bytes = std::max(stage_bytes, pl->base.stage_bytes);
@@ -1391,6 +1431,7 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     cudaError_t e = cudaMemcpy(ws, maps.data(), maps.size() * sizeof(TMaps), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(ws + off_p, params.data(), params.size() * sizeof(Params), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(ws + off_i, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(ws + off_i + off.size() * sizeof(int64_t), 0, 64);
     if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
 
     fdtd_batch_plan *bp = new fdtd_batch_plan();
@@ -1407,6 +1448,7 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     bp->d_band_h = bp->d_off + 2 * (nsims + 1);
     bp->band_e = boff_e[nsims];
     bp->band_h = boff_h[nsims];
+    bp->d_queue = reinterpret_cast<int32_t *>(ws + off_i + off.size() * sizeof(int64_t));
     int dev = 0, nsm = 0, occ = 0, optin = 0;
     cudaFuncAttributes fa;
     e = cudaGetDevice(&dev);
@@ -1442,6 +1484,7 @@ int fdtd_batch_plan_run(fdtd_batch_plan *bp, int64_t t0, int64_t nsteps, void *s
         bd.maps = bp->d_maps;
         bd.item_off = bp->d_off;
         bd.stage_bytes = bp->stage_bytes;
+        bd.queue = bp->d_queue;
         bp->k->fn_batch<<<bp->nblocks, bp->k->threads, bp->smem, st>>>(dummy_maps, dummy, bd);
         if (bp->band_e > 0 || bp->band_h > 0) {
             BandBatch d{bp->nsims, bp->cur, t0 + n, bp->d_params, bp->d_band_e};

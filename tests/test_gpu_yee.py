@@ -172,6 +172,9 @@ def _oracle_sim(work_shape, ce, npml, faces, sources, init):
     ((37, 29, 45), 5, (8, 16, 0, 3, 2)),      # L2 promotion variants
     ((40, 40, 200), 4, (8, 16, 0, 4, 1)),
     ((30, 44, 70), 14, (16, 8, 1, 3)),        # z band wider than half a tile
+    ((30, 44, 72), 14, (16, 8, 1, 3)),        # TMA band kernels, 16-wide boxes at their limit
+    ((36, 36, 96), 16, None),                 # TMA band kernels, 32-wide boxes
+    ((33, 21, 64), 6, (8, 16, 0, 3)),         # TMA band kernels, ragged y tiles
 ])
 def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     from fdtd_accelerate_gb300 import configs

@@ -46,11 +46,11 @@ NPML = 12
 # Measured STREAM-style copy bandwidth of this machine's GB300 (GB/s); read
 # from MEASURED_PEAKS.json when present.
 FALLBACK_HBM_GBS = 6790.7
-# DRAM bytes per cell-step of the fused kernel from an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum over one launch / cells);
-# see profiles/k_yee_fused_cpml1024.md (512x512x256 capture of the same workload,
-# scaled by cells: an upper bound at full size, where the CPML fraction is smaller).
-NCU_DRAM_BYTES_PER_CELL = 81.4
+# DRAM bytes per cell-step of one time step (the fused kernel and the two z-band
+# kernels: dram__bytes_read.sum + dram__bytes_write.sum over the three launches of a
+# step / cells), from an ncu launch list of this workload at full size;
+# see profiles/k_yee_fused_cpml1024.md.
+NCU_DRAM_BYTES_PER_CELL = 75.2
 
 
 def algorithmic_bytes_per_step(shape, npml):

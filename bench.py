@@ -486,11 +486,16 @@ def run_adjoint256(args):
     eng.check_status()
     fwd = statistics.mean(t[0] for t in times)
     bwd = statistics.mean(t[1] for t in times)
-    # central differences (FP32 forward, loss accumulated in FP64) at random design cells
+    # central differences at random design cells: the loss of the same discrete
+    # problem evaluated by the FP64 step on the GPU (FP32 forward runs cannot
+    # resolve it: the perturbation moves the loss by 1e-7..1e-5 relative)
+    from fdtd_accelerate_gb300.fp64 import YeeRun64
+    r64 = YeeRun64(w.shape, npml=w.npml, sources=w.sources, monitors=w.monitors, device=dev)
     rng = np.random.default_rng(7)
     cells, errs, g_fd = [], [], []
     h = 1e-3
     ds = w.design
+    t_fd = time.perf_counter()
     with torch.no_grad():
         for _ in range(args.fd_cells):
             c = tuple(int(rng.integers(sl.start, sl.stop)) for sl in ds)
@@ -498,8 +503,8 @@ def run_adjoint256(args):
             for sgn in (1, -1):
                 e2 = eps.clone()
                 e2[c] += sgn * h
-                m2, _ = F.fdtd_run(ce_of(e2), eng)
-                vals.append(float(loss_of(m2)))
+                r64.set_ce(ce_of(e2))
+                vals.append(float((r64.run(w.steps) ** 2).sum()))
             fd = (vals[0] - vals[1]) / (2 * h)
             gc = float(grad[c])
             cells.append(c)
@@ -520,9 +525,10 @@ def run_adjoint256(args):
                                     "median_rel_err": float(np.median(errs)) if errs else None,
                                     "max_rel_err": float(max(errs)) if errs else None,
                                     "max_err_over_max_fd": norm_err,
-                                    "note": "FP32 forward runs: the perturbation changes the loss by g*h/L ~ "
-                                            "1e-7..1e-5, the order of FP32 roundoff, so this bounds noise more "
-                                            "than the gradient; the FP64-loss check is tests/test_gpu_adjoint.py"},
+                                    "seconds": time.perf_counter() - t_fd,
+                                    "how": "dL/deps from the FP32 adjoint against central differences "
+                                           "(h = 1e-3 in eps) of the loss computed by the FP64 step on the GPU "
+                                           "(fdtd_step_unfused_f64) for the same FP32-rounded CE"},
                        "gpu_launches": None})
     print(json.dumps(line), flush=True)
 

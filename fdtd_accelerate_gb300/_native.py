@@ -96,6 +96,8 @@ _SIGS = {
     "fdtd_adjoint_step_noalloc_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P,
                                                 P, C.POINTER(Points), P, P]),
     "fdtd_gather_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
+    "fdtd_step_unfused_f64": (C.c_int, [C.POINTER(Grid), P, P, C.POINTER(Cpml), P, P, C.POINTER(Sources), I64, P]),
+    "fdtd_gather_points_f64": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_add_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_batch_workspace_bytes": (C.c_size_t, [I32]),
     "fdtd_batch_plan_create": (C.c_int, [C.POINTER(P), I32, C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),

@@ -241,6 +241,19 @@ int fdtd_gather_points_f32(const fdtd_grid *g, const fdtd_points *pts, const flo
 int fdtd_add_points_f32(const fdtd_grid *g, const fdtd_points *pts, float *const f[6],
                         const float *vals, void *stream);
 
+/* ---- FP64 step (accuracy checks) --------------------------------------- */
+/* One whole step in FP64, unfused and in place, with the FP32 step's
+ * operation order (update_e, cpml_e, sources, update_h, cpml_h; ch = 0.5).
+ * The CPML tables (fdtd_cpml) and source amplitudes stay FP32 and are widened.
+ * psi arrays: the layouts of fdtd_psi, in double.  No reference counterpart as
+ * one call: the reference's NumPy step run in float64. */
+int fdtd_step_unfused_f64(const fdtd_grid *g, double *const f[6], const double *const ce[3],
+                          const fdtd_cpml *c, double *const psi_e[6], double *const psi_h[6],
+                          const fdtd_sources *src, int64_t t, void *stream);
+/* out[p] = f[comp[p]][i, j, k] in double (NaN for a point outside the grid) */
+int fdtd_gather_points_f64(const fdtd_grid *g, const fdtd_points *pts, const double *const f[6],
+                           double *out, void *stream);
+
 /* ---- 4th-order symplectic stages (in place) --------------------------- */
 int fdtd_symplectic_h_f32(const fdtd_grid *g, float cl,
                           const float *ex, const float *ey, const float *ez,

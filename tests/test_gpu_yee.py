@@ -208,6 +208,44 @@ def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
             np.testing.assert_array_equal(_host(fused.cpml.psi_h[q]), sim.psi_h[q], err_msg="psi_h%d" % q)
 
 
+@pytest.mark.parametrize("shape,npml,faces,tile", [
+    ((30, 26, 90), 6, 0x10, None),            # z front face only
+    ((30, 26, 90), 6, 0x20, (8, 16, 0, 3)),   # z back face only
+    ((30, 26, 90), 6, 0x33, (4, 8, 0, 4)),    # x and z faces, 4-row tiles
+    ((26, 30, 60), 8, 0x3F, (16, 8, 1, 3)),   # one z tile holds both z slabs
+    ((30, 26, 90), 7, 0x30, None),            # odd slab width
+])
+def test_fused_z_slab_faces_and_sources(fdtd, shape, npml, faces, tile):
+    """The z-slab CPML (band kernels after the fused kernel) with one or both z
+    faces, and soft sources of every component on E z-slab nodes of both sides
+    (two of them on one cell: list order), equals the oracle bit for bit."""
+    rng = np.random.default_rng(23)
+    ce = [(0.5 / rng.uniform(1.0, 6.0, shape)).astype(np.float32) for _ in range(3)]
+    nsteps = 7
+    t = np.arange(nsteps + 2, dtype=np.float64)
+    nz = shape[2]
+    sources = []
+    for n, (comp, k) in enumerate([("ex", 1), ("ey", npml), ("ez", 2), ("ex", nz - npml - 1), ("ey", nz - 2),
+                                   ("ez", nz - 3), ("ex", 1)]):
+        sources.append((comp, (shape[0] // 2 + n % 3, shape[1] // 2 - n % 2, k), fdtd.gaussian_sine(t, 2.0 + n, 2.0, 0.1)))
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    sim = _oracle_sim(shape, ce, (npml,) * 3, faces, sources, init)
+    sim.step(nsteps)
+    fused = fdtd.YeeSolver(shape, ce=ce, npml=npml, faces=faces, sources=sources, tile=tile)
+    fused.set_fields(**init)
+    assert fused.plan_info()["z_band"] == 1
+    assert fused.plan_info()["launches_per_step"] == 3
+    fused.step(nsteps)
+    torch.cuda.synchronize()
+    fused.check_status()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(fused.fields[k]), sim.f[k], err_msg=k)
+    for q in range(6):
+        if fused.psi_e()[q] is not None:  # axes without a CPML face have no slabs
+            np.testing.assert_array_equal(_host(fused.psi_e()[q]), sim.psi_e[q], err_msg="psi_e%d" % q)
+            np.testing.assert_array_equal(_host(fused.cpml.psi_h[q]), sim.psi_h[q], err_msg="psi_h%d" % q)
+
+
 @pytest.mark.parametrize("tile", [None, (8, 16, 0, 3)])
 def test_fused_line_source_many_per_tile(fdtd, tile):
     """A z line of 90 sources (a tile holds up to 65 of them, plus a second

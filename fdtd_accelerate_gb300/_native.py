@@ -42,8 +42,13 @@ class Sources(C.Structure):
     _fields_ = [("nsrc", I32), ("ijk", P), ("comp", P), ("amp", P), ("namp", I64)]
 
 
+class Drude(C.Structure):
+    _fields_ = [("i0", I64), ("j0", I64), ("k0", I64), ("ni", I64), ("nj", I64), ("nk", I64),
+                ("j", P * 3), ("cja", P * 3), ("cjb", P * 3), ("j2", P * 3)]
+
+
 class YeeState(C.Structure):
-    _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3)]
+    _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3), ("drude", P)]
 
 
 class Tile(C.Structure):
@@ -75,6 +80,7 @@ _SIGS = {
     "fdtd_cpml_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml)] + [P] * 9 + [C.POINTER(Psi), P]),
     "fdtd_cpml_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml)] + [P] * 9 + [C.POINTER(Psi), P]),
     "fdtd_add_sources_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Sources), I64, P, P, P, P]),
+    "fdtd_drude_update_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Drude)] + [P] * 6 + [P]),
     "fdtd_step_unfused_f32": (C.c_int, [C.POINTER(Grid), P, P, P, C.POINTER(Cpml), C.POINTER(Psi),
                                         C.POINTER(Sources), I64, P]),
     "fdtd_symplectic_h_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),

@@ -44,6 +44,16 @@ inline bool all_nonnull(P... p) {
     return ((p != nullptr) && ...);
 }
 
+// Drude box inside the grid, all nine arrays present.
+inline int validate_drude(const Grid &g, const fdtd_drude *d) {
+    if (!d) return FDTD_ERR_ARG;
+    if (d->ni < 1 || d->nj < 1 || d->nk < 1 || d->i0 < 0 || d->j0 < 0 || d->k0 < 0) return FDTD_ERR_SHAPE;
+    if (d->i0 + d->ni > g.nx || d->j0 + d->nj > g.ny || d->k0 + d->nk > g.nz) return FDTD_ERR_SHAPE;
+    for (int q = 0; q < 3; q++)
+        if (!all_nonnull(d->j[q], d->cja[q], d->cjb[q])) return FDTD_ERR_ARG;
+    return FDTD_OK;
+}
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Round-to-nearest arithmetic that the compiler may not contract into FMA:
@@ -51,6 +61,14 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+// Drude ADE on one E value: e' = e - ce*J, J = cja*J + cjb*e'
+// (kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c:71-78); returns e', sets jn.
+__device__ __forceinline__ float drude_cell(float e, float ce, float j, float cja, float cjb, float &jn) {
+    const float en = fsub(e, fmul(ce, j));
+    jn = fadd(fmul(cja, j), fmul(cjb, en));
+    return en;
+}
 
 // ((a - b) - c) + d : the grouping NumPy uses for `a - b - c + d`.
 __device__ __forceinline__ float curl4(float a, float b, float c, float d) {

@@ -112,6 +112,13 @@ struct Params {
     // nbsrc < 0: more than MAX_BAND_SRC of them, the band kernel scans the list
     int32_t nbsrc;
     int32_t bsrc[MAX_BAND_SRC];
+    // Drude box (drude = 1): cells [i0, i0+ni) x [j0, j0+nj) x [k0, k0+nk); dense J, CJA, CJB;
+    // J is read from dj_in and written to dj_out (ping-pong like E-psi)
+    int32_t drude;
+    int64_t dbox[6];  // i0, j0, k0, ni, nj, nk
+    const float *dj_in[3];
+    float *dj_out[3];
+    const float *dcja[3], *dcjb[3];
 };
 
 // Many independent grids advanced by one launch: work items of all grids are
@@ -385,9 +392,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             mp = &bd.maps[2 * lo + bd.cur];
             if (lo != cur_sim) {
                 __syncthreads();  // every thread is done with the previous grid's parameters
-                if (tid < (int)(sizeof(Params) / 4))
-                    reinterpret_cast<int32_t *>(&s_p)[tid] =
-                        reinterpret_cast<const int32_t *>(&bd.params[2 * lo + bd.cur])[tid];
+                for (int w = tid; w < (int)(sizeof(Params) / 4); w += blockDim.x)
+                    reinterpret_cast<int32_t *>(&s_p)[w] =
+                        reinterpret_cast<const int32_t *>(&bd.params[2 * lo + bd.cur])[w];
                 __syncthreads();
                 if (tid == 0) {
                     s_p.t = bd.t;
@@ -422,6 +429,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const bool yh_f = ((p.faces >> 2) & 1) && p.P[1] > 0 && j0 <= p.P[1] && j0 + TY - 1 >= 1;
         const bool yh_b = ((p.faces >> 3) & 1) && p.P[1] > 0 && j0 + TY - 1 >= p.ny - p.P[1] && j0 <= p.ny - 1;
         const bool ytile = p.xypsi && (ye_f || ye_b || yh_f || yh_b) && !((ye_f || yh_f) && (ye_b || yh_b));
+        // the item's E region (planes i_start..x1-1, rows j0-1.., columns k0-1..) meets the Drude box
+        const bool dtile = p.drude && i_start < p.dbox[0] + p.dbox[3] && x1 > p.dbox[0] &&
+                           j0 - 1 < p.dbox[1] + p.dbox[4] && j0 + TY > p.dbox[1] &&
+                           k0 - 1 < p.dbox[2] + p.dbox[5] && k0 + TZ > p.dbox[2];
 
         // ---- per-item, per-thread cell description (pair at row j, columns k, k+1) ----
         const int64_t jj = j0 - 1 + er, kk = k0 + eko;
@@ -527,7 +538,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             if (nplanes > 1) issue_psi(0);
         }
         const int nls = s_nls;
-        const bool tile_plain = y_plain && nls == 0;
+        const bool tile_plain = y_plain && nls == 0 && !dtile;
 
         float2 prev_ey = make_float2(0.f, 0.f), prev_ez = make_float2(0.f, 0.f);
         float2 oex = prev_ey, oey = prev_ey, oez = prev_ey;  // own E_new pair
@@ -594,6 +605,25 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 }
                 if (!e_plain) {
                     const bool own = own_row && i >= x0;
+                    if (dtile && i >= p.dbox[0] && i < p.dbox[0] + p.dbox[3] && jj >= p.dbox[1] &&
+                        jj < p.dbox[1] + p.dbox[4]) {  // Drude ADE, before the CPML terms
+                        const int64_t jb = ((i - p.dbox[0]) * p.dbox[4] + (jj - p.dbox[1])) * p.dbox[5] - p.dbox[2];
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            const int64_t k = kk + e;
+                            if (!(e ? in1 : in0) || k < p.dbox[2] || k >= p.dbox[2] + p.dbox[5]) continue;
+                            float jn;
+                            set(ex, e, drude_cell(get(ex, e), get(cex, e), p.dj_in[0][jb + k], p.dcja[0][jb + k],
+                                                  p.dcjb[0][jb + k], jn));
+                            if (own) p.dj_out[0][jb + k] = jn;
+                            set(ey, e, drude_cell(get(ey, e), get(cey, e), p.dj_in[1][jb + k], p.dcja[1][jb + k],
+                                                  p.dcjb[1][jb + k], jn));
+                            if (own) p.dj_out[1][jb + k] = jn;
+                            set(ez, e, drude_cell(get(ez, e), get(cez, e), p.dj_in[2][jb + k], p.dcja[2][jb + k],
+                                                  p.dcjb[2][jb + k], jn));
+                            if (own) p.dj_out[2][jb + k] = jn;
+                        }
+                    }
                     if (sxe >= 0) {  // x slab: ey -= cey (..dHz/dx..), ez += cez (..dHy/dx..)
                         const Coef c = tab_coef(tabs, 0, 2 * p.P[0], 0, sxe);
                         const int64_t qb = ((int64_t)sxe * p.ny + jj) * p.nz + kk;
@@ -1054,6 +1084,7 @@ struct fdtd_yee_plan {
     Params base;
     float *f[2][6];
     float *psi_e[2][6];
+    float *dj[2][3];  // Drude J buffers
 };
 
 // 3-D FP32 tensor map: dims (n0 fastest, n1, n2), element strides s1, s2,
@@ -1151,6 +1182,21 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
         for (int q = 0; q < 6; q++) p.psi_h[q] = s->psi_h[q];
     }
     for (int q = 0; q < 3; q++) p.in_ce[q] = s->ce[q];
+    if (s->drude) {
+        const int st = validate_drude(g, s->drude);
+        if (st != FDTD_OK) { delete pl; return st; }
+        const fdtd_drude &d = *s->drude;
+        p.drude = 1;
+        const int64_t box[6] = {d.i0, d.j0, d.k0, d.ni, d.nj, d.nk};
+        for (int q = 0; q < 6; q++) p.dbox[q] = box[q];
+        for (int q = 0; q < 3; q++) {
+            if (!d.j2[q]) { delete pl; return FDTD_ERR_ARG; }
+            pl->dj[0][q] = d.j[q];
+            pl->dj[1][q] = d.j2[q];
+            p.dcja[q] = d.cja[q];
+            p.dcjb[q] = d.cjb[q];
+        }
+    }
     // the z slab (when a z face has CPML) is finished by the band kernels
     p.zfix = (p.P[2] > 0 && ((p.faces >> 4) & 3)) ? 1 : 0;
     if (src && src->nsrc > 0) {
@@ -1292,6 +1338,10 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
             p.psi_e_in[q] = pl->psi_e[in][q];
             p.psi_e_out[q] = pl->psi_e[outb][q];
         }
+        for (int q = 0; q < 3; q++) {
+            p.dj_in[q] = pl->dj[in][q];
+            p.dj_out[q] = pl->dj[outb][q];
+        }
         p.t = t0 + n;
         BatchDesc bd{};
         pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
@@ -1418,6 +1468,10 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
                 p.psi_e_in[q] = pl->psi_e[b][q];
                 p.psi_e_out[q] = pl->psi_e[1 - b][q];
                 p.in[q] = pl->f[b][q];
+            }
+            for (int q = 0; q < 3; q++) {
+                p.dj_in[q] = pl->dj[b][q];
+                p.dj_out[q] = pl->dj[1 - b][q];
             }
             params[2 * s + b] = p;
             maps[2 * s + b] = pl->maps[b];

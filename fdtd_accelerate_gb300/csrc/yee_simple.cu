@@ -230,6 +230,24 @@ __global__ void k_cpml_h_z(Grid g, CpmlAxis A, float *hx, float *hy, const float
 }
 
 // Soft sources, sequential in list order (duplicates accumulate in order).
+// Drude ADE on the box of d, one thread per box cell (z fastest).
+__global__ void __launch_bounds__(kBlockZ)
+k_drude_e(Grid g, fdtd_drude d, float *ex, float *ey, float *ez, const float *cex, const float *cey,
+          const float *cez) {
+    const int64_t t = (int64_t)blockIdx.x * kBlockZ + threadIdx.x;
+    if (t >= d.ni * d.nj * d.nk) return;
+    const int64_t k = t % d.nk, j = (t / d.nk) % d.nj, i = t / (d.nk * d.nj);
+    const int64_t c = (d.i0 + i) * g.sx + (d.j0 + j) * g.sy + d.k0 + k;
+    float *E[3] = {ex, ey, ez};
+    const float *CE[3] = {cex, cey, cez};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        float jn;
+        E[q][c] = drude_cell(E[q][c], CE[q][c], d.j[q][t], d.cja[q][t], d.cjb[q][t], jn);
+        d.j[q][t] = jn;
+    }
+}
+
 __global__ void k_sources(Grid g, fdtd_sources src, int64_t t, float *ex, float *ey, float *ez) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (t < 0 || t >= src.namp) return;
@@ -406,6 +424,18 @@ int fdtd_add_sources_f32(const fdtd_grid *gp, const fdtd_sources *src, int64_t t
     FDTD_TRY(validate_sources(g, src));
     if (src->nsrc == 0) return FDTD_OK;
     k_sources<<<1, 32, 0, as_stream(stream)>>>(g, *src, t, ex, ey, ez);
+    return check_launch();
+}
+
+int fdtd_drude_update_e_f32(const fdtd_grid *gp, const fdtd_drude *d, float *ex, float *ey, float *ez,
+                            const float *cex, const float *cey, const float *cez, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!all_nonnull(ex, ey, ez, cex, cey, cez)) return FDTD_ERR_ARG;
+    FDTD_TRY(validate_drude(g, d));
+    const int64_t n = d->ni * d->nj * d->nk;
+    k_drude_e<<<(unsigned)((n + kBlockZ - 1) / kBlockZ), kBlockZ, 0, as_stream(stream)>>>(g, *d, ex, ey, ez, cex,
+                                                                                         cey, cez);
     return check_launch();
 }
 

@@ -32,7 +32,7 @@ def padded_nz(nz, align=4):
 
 class YeeSolver:
     def __init__(self, shape, ce=None, npml=0, faces=0x3F, cpml_params=None, sources=(),
-                 device="cuda", tile=None, z_align=4):
+                 device="cuda", tile=None, z_align=4, drude=None):
         nx, ny, nz = (int(v) for v in shape)
         self.shape = (nx, ny, nz)
         self.device = torch.device(device)
@@ -49,11 +49,27 @@ class YeeSolver:
         self.cpml = CpmlLayer(self.shape, npml, faces, device=dev, double_buffer_e=True,
                               **(cpml_params or {}))
         self.sources = PointSources(self.shape, sources, device=dev)
+        # optional Drude region (DrudeAde), applied after the E update, before the CPML
+        if drude is not None and (tuple(drude.grid_shape) != self.shape or drude.J.device != self._state.device):
+            raise ValueError("the Drude region belongs to a %s grid on %s" % (drude.grid_shape, drude.J.device))
+        self.drude = drude
+        self._drude_struct = drude.struct(both_buffers=True) if drude is not None else None
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.cur = 0
+        self._cur = 0
         self.tstep = 1
         self.tile = tile
         self._plan = None
+
+    @property
+    def cur(self):
+        """Index of the state buffer holding the current fields (and E-psi, J)."""
+        return self._cur
+
+    @cur.setter
+    def cur(self, value):
+        self._cur = int(value)
+        if self.drude is not None:
+            self.drude.cur = self._cur
 
     # ------------------------------------------------------------------ views
     def _views(self, b):
@@ -107,6 +123,7 @@ class YeeSolver:
             s.psi_h[q] = h.data_ptr() if h is not None else None
         for q in range(3):
             s.ce[q] = self._ce[q].data_ptr()
+        s.drude = C.addressof(self._drude_struct) if self._drude_struct is not None else None
         return s
 
     def plan(self):
@@ -152,9 +169,24 @@ class YeeSolver:
         with torch.cuda.device(self.device):
             stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
             for _ in range(n):
-                N.call("fdtd_step_unfused_f32", C.byref(g), f, ce, None,
-                       C.byref(cp) if self.cpml.active else None, C.byref(psi),
-                       C.byref(src), int(self.tstep), stream)
+                if self._drude_struct is None:
+                    N.call("fdtd_step_unfused_f32", C.byref(g), f, ce, None,
+                           C.byref(cp) if self.cpml.active else None, C.byref(psi),
+                           C.byref(src), int(self.tstep), stream)
+                else:
+                    # the reference-shaped calls in the order of
+                    # kuFDTD/v0.2.0/dim3/cpu/test/030-drude-cpml.py:88-95
+                    E, H = list(f)[:3], list(f)[3:]
+                    d = self.drude.struct()
+                    N.call("fdtd_update_e_f32", C.byref(g), *E, *H, *ce, stream)
+                    N.call("fdtd_drude_update_e_f32", C.byref(g), C.byref(d), *E, *ce, stream)
+                    if self.cpml.active:
+                        N.call("fdtd_cpml_e_f32", C.byref(g), C.byref(cp), *E, *H, *ce, C.byref(psi), stream)
+                    N.call("fdtd_add_sources_f32", C.byref(g), C.byref(src), int(self.tstep), *E, stream)
+                    N.call("fdtd_update_h_f32", C.byref(g), *E, *H, None, None, None, stream)
+                    if self.cpml.active:
+                        N.call("fdtd_cpml_h_f32", C.byref(g), C.byref(cp), *E, *H, None, None, None,
+                               C.byref(psi), stream)
                 self.tstep += 1
 
     def check_status(self):

@@ -25,6 +25,10 @@
  *                          kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c:238-263
  *   fdtd_add_sources_f32   2nd_order-Yee/CUDA/fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:352-363
  *                          updateSrc; KEMP/v0.7_pml/fdtd3d/naive/incident_direct.py:52-70
+ *   fdtd_drude_update_e_f32  kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c:14-93
+ *                          drude_ade.update_e (Ncore, Nx, Ny, Nz, idx0,
+ *                          spaceNyz, spaceNz, Ex..CEz, Jx..CJBz): the box and
+ *                          strides travel in fdtd_drude / fdtd_grid
  *   fdtd_step_unfused_f32  one time step in the order of
  *                          fdtd3d_201_..._100000tstep.cu:718-742
  *   fdtd_yee_plan_*        the same step, fused into one pass per step
@@ -92,6 +96,25 @@ typedef struct {
     int64_t namp;
 } fdtd_sources;
 
+/* Drude dispersive region (auxiliary differential equation): a sub-box of
+ * ni x nj x nk cells starting at cell (i0, j0, k0) of the E arrays, with
+ * dense (ni, nj, nk) device arrays per component: j = polarisation current
+ * (state, updated in place), cja and cjb = its coefficients.  After the E
+ * update and before its CPML correction, per cell and component:
+ *   e' = e - ce*J;  e = e';  J = cja*J + cjb*e'
+ * Replaces kuFDTD DrudeAde (kuFDTD/v0.2.0/dim3/cpu/matter.py:222-314,
+ * kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c:14-93).  j2: a second J buffer for
+ * the fused step, which reads J from buffer `cur` (j when cur = 0, j2 when
+ * cur = 1, as the fields) and writes the other (neighbouring tiles recompute
+ * halo cells from the old J); unused by fdtd_drude_update_e_f32 (in place
+ * on j). */
+typedef struct {
+    int64_t i0, j0, k0, ni, nj, nk;
+    float *j[3];
+    const float *cja[3], *cjb[3];
+    float *j2[3];
+} fdtd_drude;
+
 const char *fdtd_status_string(int status);
 int fdtd_last_cuda_error(void);
 
@@ -118,6 +141,10 @@ int fdtd_cpml_h_f32(const fdtd_grid *g, const fdtd_cpml *c,
                     const fdtd_psi *psi, void *stream);
 int fdtd_add_sources_f32(const fdtd_grid *g, const fdtd_sources *src, int64_t t,
                          float *ex, float *ey, float *ez, void *stream);
+/* Drude ADE on the box of d (in place on E and d->j); call it between
+ * fdtd_update_e_f32 and fdtd_cpml_e_f32. */
+int fdtd_drude_update_e_f32(const fdtd_grid *g, const fdtd_drude *d, float *ex, float *ey, float *ez,
+                            const float *cex, const float *cey, const float *cez, void *stream);
 
 /* One whole step, unfused (update_e, cpml_e, sources, update_h, cpml_h),
  * in place.  c and src may be NULL. */
@@ -135,6 +162,7 @@ typedef struct {
     float *psi_e[2][6];
     float *psi_h[6];
     const float *ce[3];
+    const fdtd_drude *drude;  /* NULL: no dispersive region */
 } fdtd_yee_state;
 
 /* Launch shape of the fused kernel (0 = default): tile height in y (4, 8

@@ -16,6 +16,8 @@ Artefacts
                                 (Python extension, Py3 init shim).
   ref_symp_dielectric*.so       4th_order-Symplectic/Python-C/dielectric.c
                                 (Python extension, Py3 init shim).
+  ref_drude_ade*.so             kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c
+                                (Python extension, Py3 init shim).
 """
 import os
 import platform
@@ -32,6 +34,7 @@ KEMP_SRC = "KEMP/v0.7_pml/fdtd3d/cpu/src/core.c"
 KUFDTD_CPML = "kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c"
 KUFDTD_INC = "kuFDTD/v0.2.0/dim3/cpu/core"
 SYMP_SRC = "4th_order-Symplectic/Python-C/dielectric.c"
+KUFDTD_DRUDE = "kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c"
 
 
 def available():
@@ -102,7 +105,8 @@ def build(verbose=False):
     shim = os.path.join(HERE, "ref_pymod_shim.c")
     for name, src, old_init, extra in (
             ("ref_cpml_non_kappa", KUFDTD_CPML, "initcpml_non_kappa", ["-I" + os.path.join(REF, KUFDTD_INC)]),
-            ("ref_symp_dielectric", SYMP_SRC, "initdielectric", [])):
+            ("ref_symp_dielectric", SYMP_SRC, "initdielectric", []),
+            ("ref_drude_ade", KUFDTD_DRUDE, "initdrude_ade", ["-I" + os.path.join(REF, KUFDTD_INC)])):
         jobs.append(["gcc", "-O2", "-fPIC", "-shared", "-w", "-I" + pyinc, "-I" + npinc, *extra,
                      '-DREF_SRC="%s"' % os.path.join(REF, src),
                      '-DSHIM_NAME="%s"' % name, "-DSHIM_INIT=PyInit_" + name,

@@ -27,6 +27,9 @@
  *                            (F += -/+ c*((1/kappa-1)*dF + psi), ds = 1)
  *   soft source              2nd_order-Yee/CUDA/fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:352-363
  *                            and KEMP/v0.7_pml/fdtd3d/naive/incident_direct.py:52-70
+ *   Drude ADE (E pass)       kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c:48-93
+ *                            (e' = e - ce*J; J = cja*J + cjb*e', per
+ *                            component, on a sub-box of the E arrays)
  *   4th-order stages         4th_order-Symplectic/PyCUDA/100-base.py:10-44
  *                            (index ranges of the CUDA kernels; grouping of
  *                            4th_order-Symplectic/Python-C/dielectric.c:35-89)
@@ -576,6 +579,39 @@ void FN(symp_h_scalar)(const int64_t *g, REAL cl, REAL ch, const REAL *ex, const
                     REAL n = ((ey[c] - ey[c - sx]) - ex[c]) + ex[c - sy];
                     REAL f = ((ey[c + sx] - ey[c - 2 * sx]) - ex[c + sy]) + ex[c - 2 * sy];
                     hz[c] = hz[c] - cc * (c27 * n - f);
+                }
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Drude ADE, kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c:48-93: on the sub-box   */
+/* of ni x nj x nk cells starting at (i0, j0, k0) of the E arrays; J, cja,   */
+/* cjb are dense (ni, nj, nk) arrays.  Per cell and component:               */
+/*   e' = e - ce*J;  e = e';  J = cja*J + cjb*e'                              */
+/* ------------------------------------------------------------------------ */
+void FN(drude_e)(const int64_t *g, const int64_t *box, REAL *ex, REAL *ey, REAL *ez,
+                 const REAL *cex, const REAL *cey, const REAL *cez,
+                 REAL *jx, REAL *jy, REAL *jz, const REAL *cjax, const REAL *cjay, const REAL *cjaz,
+                 const REAL *cjbx, const REAL *cjby, const REAL *cjbz)
+{
+    GRID;
+    const int64_t i0 = box[0], j0 = box[1], k0 = box[2], ni = box[3], nj = box[4], nk = box[5];
+    REAL *E[3] = {ex, ey, ez}, *J[3] = {jx, jy, jz};
+    const REAL *CE[3] = {cex, cey, cez}, *CA[3] = {cjax, cjay, cjaz}, *CB[3] = {cjbx, cjby, cjbz};
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int64_t i = 0; i < ni; i++)
+        for (int64_t j = 0; j < nj; j++)
+            for (int64_t k = 0; k < nk; k++) {
+                const int64_t ji = (i * nj + j) * nk + k;
+                const int64_t ei = (i0 + i) * sx + (j0 + j) * sy + (k0 + k);
+                for (int q = 0; q < 3; q++) {
+                    const REAL f = J[q][ji];
+                    const REAL t = CE[q][ei] * f;
+                    const REAL e = E[q][ei] - t;
+                    E[q][ei] = e;
+                    const REAL a = CA[q][ji] * f;
+                    const REAL b = CB[q][ji] * e;
+                    J[q][ji] = a + b;
                 }
             }
 }

@@ -14,7 +14,8 @@ from . import build as _build
 
 __all__ = ["update_e", "update_h", "pbc_e", "pbc_h", "cpml_e", "cpml_h",
            "add_points", "symp_h", "symp_e", "cpml_tables", "pulse",
-           "OracleSim", "lib", "symp_h_scalar", "symp_cpml_e", "symp_cpml_h", "symp_stage_tables"]
+           "OracleSim", "lib", "symp_h_scalar", "symp_cpml_e", "symp_cpml_h", "symp_stage_tables",
+           "drude_e", "drude_coefficients"]
 
 _LIBS = {}
 
@@ -173,6 +174,38 @@ def pulse(n, t0=150.0, width=30.0, freq=0.05):
     return math.sin(2.0 * math.pi * freq * n) * math.exp(-0.5 * ((n - t0) / width) ** 2)
 
 
+def drude_e(box, ex, ey, ez, cex, cey, cez, J, CJA, CJB):
+    """Drude ADE on the sub-box box = (i0, j0, k0) of the E arrays
+    (kuFDTD drude_ade.c update_e); J, CJA, CJB: 3 dense arrays each, shape
+    (ni, nj, nk), of the E arrays' dtype.  J is updated in place."""
+    _check(ex, ey, ez, cex, cey, cez)
+    kind, _ = _kind(ex)
+    ni, nj, nk = J[0].shape
+    for a in (*J, *CJA, *CJB):
+        if a.dtype != ex.dtype or a.shape != (ni, nj, nk) or not a.flags.c_contiguous:
+            raise ValueError("J, CJA, CJB must be C-contiguous (ni, nj, nk) arrays of the field dtype")
+    i0, j0, k0 = (int(v) for v in box)
+    if i0 < 0 or j0 < 0 or k0 < 0 or i0 + ni > ex.shape[0] or j0 + nj > ex.shape[1] or k0 + nk > ex.shape[2]:
+        raise ValueError("Drude box outside the grid")
+    b = (C.c_int64 * 6)(i0, j0, k0, ni, nj, nk)
+    getattr(lib(kind), "orc_drude_e_" + kind)(_grid(ex), b, *map(_p, (ex, ey, ez, cex, cey, cez)),
+                                              *map(_p, J), *map(_p, CJA), *map(_p, CJB))
+
+
+def drude_coefficients(pfreq, gamma, dt=0.5):
+    """CJA = (2 - gamma dt)/(2 + gamma dt), CJB = 4 (dt pfreq)^2/(2 + gamma dt), in
+    float32 array arithmetic as kuFDTD/v0.2.0/dim3/cpu/matter.py:198-208 (and
+    268-278) evaluates them on its 'f' arrays."""
+    g = np.asarray(gamma, np.float32)
+    w = np.asarray(pfreq, np.float32)
+    g, w = np.broadcast_arrays(g, w)
+    dt32 = np.float32(dt)
+    tmp = np.float32(2) + g * dt32
+    cja = (np.float32(2) - g * dt32) / tmp
+    cjb = np.float32(4) * (dt32 * w) ** 2 / tmp
+    return cja.astype(np.float32), cjb.astype(np.float32)
+
+
 class OracleSim:
     """Whole-step oracle: state in NumPy arrays, canonical step order.
 
@@ -183,7 +216,10 @@ class OracleSim:
     amplitude table is indexed by the 1-based step number.
     """
 
-    def __init__(self, fields, npml=(0, 0, 0), faces=0x3F, tables=None, sources=()):
+    def __init__(self, fields, npml=(0, 0, 0), faces=0x3F, tables=None, sources=(), drude=None):
+        # drude: optional (box (i0, j0, k0), J[3], CJA[3], CJB[3]) applied after update_e
+        # (kuFDTD/v0.2.0/dim3/cpu/test/030-drude-cpml.py:88-92 step order)
+        self.drude = drude
         self.f = fields
         ex = fields["ex"]
         self.dtype = ex.dtype
@@ -210,6 +246,9 @@ class OracleSim:
         pml = any(self.npml)
         for _ in range(n):
             update_e(*E, *H, *CE)
+            if self.drude is not None:
+                box, J, CJA, CJB = self.drude
+                drude_e(box, *E, *CE, J, CJA, CJB)
             if pml:
                 cpml_e(self.npml, self.faces, self.tables, *E, *H, *CE, self.psi_e)
             for comp, (i, j, k), amp in self.sources:

@@ -262,13 +262,63 @@ def symp_c(rng):
     return out
 
 
+def drude_kufdtd(rng):
+    """kuFDTD drude_ade.update_e (kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c) on a
+    sub-box of the E arrays, three calls in a row (J carries over)."""
+    sys.path.insert(0, build_ref.OUT)
+    import ref_drude_ade as ref
+    import oracle
+    out = {}
+    n = 0
+    # (full grid, box origin, box shape); the reference's k loop takes 4 cells at a time
+    for shape, org, box in (((9, 10, 13), (2, 3, 4), (4, 5, 8)), ((6, 7, 12), (0, 0, 0), (6, 7, 12))):
+        nx, ny, nz = shape
+        E = [rng.standard_normal(shape).astype(F32) for _ in range(3)]
+        CE = [rng.random(shape, dtype=F32) for _ in range(3)]
+        J = [(0.1 * rng.standard_normal(box)).astype(F32) for _ in range(3)]
+        CA, CB = [], []
+        for _ in range(3):
+            a, b = oracle.drude_coefficients(rng.uniform(0.05, 0.4, box).astype(F32),
+                                             rng.uniform(0.0, 0.2, box).astype(F32))
+            CA.append(a)
+            CB.append(b)
+        tag = "c%d_" % n
+        out[tag + "meta"] = np.array([*org, *box])
+        for q, k in enumerate(("ex", "ey", "ez")):
+            out[tag + "in_" + k] = E[q].copy()
+            out[tag + "in_c" + k] = CE[q]
+            out[tag + "in_j" + k[1]] = J[q].copy()
+            out[tag + "in_cja" + k[1]] = CA[q]
+            out[tag + "in_cjb" + k[1]] = CB[q]
+        idx0 = (org[0] * ny + org[1]) * nz + org[2]
+        for _ in range(3):
+            ref.update_e(1, box[0], box[1], box[2], idx0, ny * nz, nz, *E, *CE, *J, *CA, *CB)
+        for q, k in enumerate(("ex", "ey", "ez")):
+            out[tag + "out_" + k] = E[q]
+            out[tag + "out_j" + k[1]] = J[q]
+        n += 1
+    out["ncases"] = np.array(n)
+    return out
+
+
+CASES = (("yee_numpy", yee_numpy), ("kemp_core", kemp_core), ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c),
+         ("drude_kufdtd", drude_kufdtd))
+
+
 def main():
     if not build_ref.build():
         raise SystemExit("reference checkout or x86_64 host not available")
+    # one generator per case, seeded by its position, so a case can be
+    # regenerated alone (python make_golden.py drude_kufdtd) without touching the others;
+    # the first four keep the single shared stream they were made with
+    only = set(sys.argv[1:])
     rng = np.random.default_rng(20261203)
-    for name, fn in (("yee_numpy", yee_numpy), ("kemp_core", kemp_core),
-                     ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c)):
+    for pos, (name, fn) in enumerate(CASES):
+        if pos >= 4:
+            rng = np.random.default_rng(20261203 + pos)
         data = fn(rng)
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **data)
         print("wrote", path, os.path.getsize(path), "bytes")

@@ -88,3 +88,19 @@ def test_error_mapping():
         N.check(N.FDTD_ERR_UNSUPPORTED, "f")
     with pytest.raises(RuntimeError):
         N.check(N.FDTD_ERR_CUDA, "f")
+
+
+def test_drude_validation_before_cuda(lib):
+    """A Drude box outside the grid or missing arrays is rejected on the host."""
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(8, 9, 10, 90, 10)
+    fake = [C.c_void_p(256 * (q + 1)) for q in range(6)]   # never dereferenced
+    d = N.Drude(2, 3, 4, 4, 4, 4)
+    assert lib.fdtd_drude_update_e_f32(C.byref(g), C.byref(d), *fake, None) == N.FDTD_ERR_ARG  # no J arrays
+    for q in range(3):
+        d.j[q] = d.cja[q] = d.cjb[q] = 512 * (q + 1)
+    d.k0 = 7                                                # 7 + 4 > 10
+    assert lib.fdtd_drude_update_e_f32(C.byref(g), C.byref(d), *fake, None) == N.FDTD_ERR_SHAPE
+    d.k0, d.ni = 4, 0
+    assert lib.fdtd_drude_update_e_f32(C.byref(g), C.byref(d), *fake, None) == N.FDTD_ERR_SHAPE
+    assert lib.fdtd_drude_update_e_f32(C.byref(g), None, *fake, None) == N.FDTD_ERR_ARG

@@ -118,6 +118,46 @@ def test_oracle_symplectic_matches_reference_c_bit_exact(golden_dir):
                                           err_msg="case %d %s" % (n, NAMES[q]))
 
 
+def _drude_case(g, n):
+    t = "c%d_" % n
+    m = g[t + "meta"]
+    E = [g[t + "in_" + k].copy() for k in ("ex", "ey", "ez")]
+    CE = [g[t + "in_c" + k] for k in ("ex", "ey", "ez")]
+    J = [g[t + "in_j" + a].copy() for a in "xyz"]
+    CA = [g[t + "in_cja" + a] for a in "xyz"]
+    CB = [g[t + "in_cjb" + a] for a in "xyz"]
+    return t, tuple(int(v) for v in m[:3]), E, CE, J, CA, CB
+
+
+def test_oracle_drude_matches_kufdtd_bit_exact(golden_dir):
+    """Reference kuFDTD drude_ade.update_e (three calls, J carried over) on a
+    sub-box and on the whole grid (tests/golden/drude_kufdtd.npz)."""
+    g = np.load(os.path.join(golden_dir, "drude_kufdtd.npz"))
+    for n in range(int(g["ncases"])):
+        t, org, E, CE, J, CA, CB = _drude_case(g, n)
+        for _ in range(3):
+            oracle.drude_e(org, *E, *CE, J, CA, CB)
+        for q, k in enumerate(("ex", "ey", "ez")):
+            np.testing.assert_array_equal(E[q], g[t + "out_" + k], err_msg="case %d %s" % (n, k))
+            np.testing.assert_array_equal(J[q], g[t + "out_j" + k[1]], err_msg="case %d J%s" % (n, k[1]))
+
+
+def test_drude_coefficients_float32_arithmetic():
+    """CJA, CJB as kuFDTD matter.py:198-208 evaluates them on float32 arrays."""
+    rng = np.random.default_rng(4)
+    w = rng.uniform(0.01, 0.5, (5, 6)).astype(np.float32)
+    gam = rng.uniform(0.0, 0.3, (5, 6)).astype(np.float32)
+    cja, cjb = oracle.drude_coefficients(w, gam, 0.5)
+    assert cja.dtype == np.float32 and cjb.dtype == np.float32
+    tmp = (2 + gam * np.float32(0.5)).astype(np.float32)
+    np.testing.assert_array_equal(cja, ((2 - gam * np.float32(0.5)) / tmp).astype(np.float32))
+    np.testing.assert_array_equal(cjb, (4 * (np.float32(0.5) * w) ** 2 / tmp).astype(np.float32))
+    # no dispersion: J stays zero, E untouched
+    cja0, cjb0 = oracle.drude_coefficients(np.zeros(3, np.float32), np.zeros(3, np.float32))
+    np.testing.assert_array_equal(cja0, np.ones(3, np.float32))
+    np.testing.assert_array_equal(cjb0, np.zeros(3, np.float32))
+
+
 def test_oracle_fp64_matches_fp32_roughly():
     rng = np.random.default_rng(1)
     shape = (10, 11, 12)

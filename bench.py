@@ -16,6 +16,8 @@ Other workloads (each prints its own line; the default is the headline):
                          64 sequential single-grid solves
   --workload adjoint256  gradient run at 256x256x128, 3000 steps: backward /
                          forward cost and central differences at 32 cells
+  --workload drude512    512^3 with a 256^3 Drude (ADE) box, 12-cell CPML,
+                         beside the same grid without it
 
 --impl reference times the reference's CPU path on the host cores: the
 reference's own C cannot be built on the benchmark host (SSE intrinsics,
@@ -405,6 +407,62 @@ def run_symp512(args):
     print(json.dumps(line), flush=True)
 
 
+def run_drude512(args):
+    """512^3 vacuum, 12-cell CPML, a centred 256^3 Drude box (gold-like: eps_inf 9.0685,
+    wp dt = 0.075, gamma dt = 0.0019, the parameters of kuFDTD/v0.2.0/dim3/cpu/test/
+    030-drude-cpml.py in the step's normalised units), one Ez dipole; the same grid without
+    the Drude box is timed beside it."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    dev = torch.device("cuda", 0)
+    shape, npml, box0, box = (512, 512, 512), 12, (128, 128, 128), (256, 256, 256)
+    dt = 0.5
+    eps_inf, wp, gamma = 9.0685, 0.075 / dt, 0.00192 / dt
+    t = np.arange(args.warmup + args.steps + 2, dtype=np.float64)
+    src = [("ez", (256, 256, 64), np.sin(2 * np.pi * 0.05 * t) * np.exp(-0.5 * ((t - 150.0) / 30.0) ** 2))]
+    stream = torch.cuda.current_stream(dev)
+    results = {}
+    for with_drude in (False, True):
+        ce = torch.full((3,) + shape, 0.5, dtype=torch.float32, device=dev)
+        d = None
+        if with_drude:
+            sl = tuple(slice(o, o + n) for o, n in zip(box0, box))
+            ce[(slice(None),) + sl] = float(np.float32(0.5) / np.float32(eps_inf))
+            d = F.DrudeAde(shape, box0, box, device=dev)
+            d.set_coeff(wp, gamma, dt)
+        s = F.YeeSolver(shape, ce=ce, npml=npml, sources=src, device=dev, drude=d, tile=args.tile)
+        del ce
+        for _ in range(args.warmup):
+            s.step(1)
+        sampler = ClockSampler(0)
+        sampler.start()
+        ms = _timed_steps(torch, stream, lambda: s.step(1), args.steps)
+        clocks = sampler.stop()
+        s.check_status()
+        results[with_drude] = (statistics.mean(ms), clocks, s.plan_info())
+        s.close()
+        del s, d
+        torch.cuda.empty_cache()
+    avg, clocks, info = results[True]
+    cells = int(np.prod(shape))
+    dcells = int(np.prod(box))
+    alg = algorithmic_bytes_per_step(shape, npml) + dcells * 48
+    peak, psrc = measured_peak()
+    achieved = alg / (avg / 1e3) / 1e9
+    line = _base_line("Mcell-updates/s (Yee+CPML+Drude 512^3, 256^3 Drude box, FP32)", cells / (avg / 1e3) / 1e6,
+                      UNIT, args, avg, "f32", "Yee + 12-cell CPML 512x512x512 with a centred 256^3 Drude (ADE) box, "
+                      "gold-like parameters, Ez dipole; state 6.4 GB >> L2",
+                      {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": None, "peak_source": psrc,
+                                    "alg_bytes_per_launch": alg,
+                                    "scope": "one time step: 60 B/cell + 32 B per slab cell + 48 B per Drude "
+                                             "cell (J read+written, CJA, CJB read)"},
+                       "without_drude_ms_per_step": results[False][0],
+                       "clocks": clocks, "gpu_launches": args.steps * info["launches_per_step"]})
+    line["config"]["tile"] = info
+    print(json.dumps(line), flush=True)
+
+
 def run_batched64(args):
     """64 ragged grids in one launch per step (autotuned, graph-captured) against
     the same 64 grids solved one after another with the single-grid path."""
@@ -550,9 +608,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default 200; plain128 1000, symp512 50, batched64 500, adjoint256 3000)")
+                    help="timed steps (default 200; plain128 1000, symp512 50, batched64 500, adjoint256 3000, "
+                         "drude512 100)")
     ap.add_argument("--workload", default="cpml1024",
-                    choices=["cpml1024", "plain128", "symp512", "batched64", "adjoint256"])
+                    choices=["cpml1024", "plain128", "symp512", "batched64", "adjoint256", "drude512"])
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -567,14 +626,14 @@ def main():
         args.warmup = 3
     if args.steps is None:
         args.steps = {"cpml1024": 200, "plain128": 1000, "symp512": 50, "batched64": 500,
-                      "adjoint256": 3000}[args.workload]
+                      "adjoint256": 3000, "drude512": 100}[args.workload]
     if args.workload != "cpml1024":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "workload": args.workload,
                               "unavailable": "the reference arm covers the headline workload only"}), flush=True)
             return
         {"plain128": run_plain128, "symp512": run_symp512, "batched64": run_batched64,
-         "adjoint256": run_adjoint256}[args.workload](args)
+         "adjoint256": run_adjoint256, "drude512": run_drude512}[args.workload](args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

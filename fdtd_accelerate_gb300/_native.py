@@ -47,6 +47,11 @@ class Drude(C.Structure):
                 ("j", P * 3), ("cja", P * 3), ("cjb", P * 3), ("j2", P * 3)]
 
 
+class Tfsf(C.Structure):
+    _fields_ = [("p1", I64 * 3), ("p2", I64 * 3), ("faces", I32), ("axis", I32), ("angle", C.c_double),
+                ("e1d", P), ("h1d", P), ("abc", P), ("amp", P), ("namp", I64)]
+
+
 class YeeState(C.Structure):
     _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3), ("drude", P)]
 
@@ -81,6 +86,8 @@ _SIGS = {
     "fdtd_cpml_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml)] + [P] * 9 + [C.POINTER(Psi), P]),
     "fdtd_add_sources_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Sources), I64, P, P, P, P]),
     "fdtd_drude_update_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Drude)] + [P] * 6 + [P]),
+    "fdtd_tfsf_update_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Tfsf), I64, P, P, P, P]),
+    "fdtd_tfsf_update_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Tfsf), P, P, P, P]),
     "fdtd_step_unfused_f32": (C.c_int, [C.POINTER(Grid), P, P, P, C.POINTER(Cpml), C.POINTER(Psi),
                                         C.POINTER(Sources), I64, P]),
     "fdtd_symplectic_h_f32": (C.c_int, [C.POINTER(Grid), F32] + [P] * 9 + [P]),

@@ -32,7 +32,7 @@ def padded_nz(nz, align=4):
 
 class YeeSolver:
     def __init__(self, shape, ce=None, npml=0, faces=0x3F, cpml_params=None, sources=(),
-                 device="cuda", tile=None, z_align=4, drude=None):
+                 device="cuda", tile=None, z_align=4, drude=None, tfsf=None):
         nx, ny, nz = (int(v) for v in shape)
         self.shape = (nx, ny, nz)
         self.device = torch.device(device)
@@ -52,6 +52,11 @@ class YeeSolver:
         # optional Drude region (DrudeAde), applied after the E update, before the CPML
         if drude is not None and (tuple(drude.grid_shape) != self.shape or drude.J.device != self._state.device):
             raise ValueError("the Drude region belongs to a %s grid on %s" % (drude.grid_shape, drude.J.device))
+        # optional plane-wave source (Tfsf): step_unfused applies it after the
+        # E and H CPML corrections; the fused step does not take it
+        if tfsf is not None and tuple(tfsf.shape) != self.shape:
+            raise ValueError("the TFSF source belongs to a %s grid" % (tfsf.shape,))
+        self.tfsf = tfsf
         self.drude = drude
         self._drude_struct = drude.struct(both_buffers=True) if drude is not None else None
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -148,6 +153,8 @@ class YeeSolver:
                          "launches_per_step"), list(info)))
 
     def step(self, n=1):
+        if self.tfsf is not None:
+            raise NotImplementedError("the fused step has no TFSF face corrections; use step_unfused")
         """Advance n steps with the fused kernel (one launch per step)."""
         plan = self.plan()
         L = N.lib()
@@ -169,7 +176,7 @@ class YeeSolver:
         with torch.cuda.device(self.device):
             stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
             for _ in range(n):
-                if self._drude_struct is None:
+                if self._drude_struct is None and self.tfsf is None:
                     N.call("fdtd_step_unfused_f32", C.byref(g), f, ce, None,
                            C.byref(cp) if self.cpml.active else None, C.byref(psi),
                            C.byref(src), int(self.tstep), stream)
@@ -177,16 +184,23 @@ class YeeSolver:
                     # the reference-shaped calls in the order of
                     # kuFDTD/v0.2.0/dim3/cpu/test/030-drude-cpml.py:88-95
                     E, H = list(f)[:3], list(f)[3:]
-                    d = self.drude.struct()
                     N.call("fdtd_update_e_f32", C.byref(g), *E, *H, *ce, stream)
-                    N.call("fdtd_drude_update_e_f32", C.byref(g), C.byref(d), *E, *ce, stream)
+                    if self.drude is not None:
+                        d = self.drude.struct()
+                        N.call("fdtd_drude_update_e_f32", C.byref(g), C.byref(d), *E, *ce, stream)
                     if self.cpml.active:
                         N.call("fdtd_cpml_e_f32", C.byref(g), C.byref(cp), *E, *H, *ce, C.byref(psi), stream)
+                    if self.tfsf is not None:
+                        self.tfsf.ensure_steps(self.tstep)
+                        t = self.tfsf.struct()
+                        N.call("fdtd_tfsf_update_e_f32", C.byref(g), C.byref(t), int(self.tstep), *E, stream)
                     N.call("fdtd_add_sources_f32", C.byref(g), C.byref(src), int(self.tstep), *E, stream)
                     N.call("fdtd_update_h_f32", C.byref(g), *E, *H, None, None, None, stream)
                     if self.cpml.active:
                         N.call("fdtd_cpml_h_f32", C.byref(g), C.byref(cp), *E, *H, None, None, None,
                                C.byref(psi), stream)
+                    if self.tfsf is not None:
+                        N.call("fdtd_tfsf_update_h_f32", C.byref(g), C.byref(t), *H, stream)
                 self.tstep += 1
 
     def check_status(self):

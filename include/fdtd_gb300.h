@@ -29,6 +29,8 @@
  *                          drude_ade.update_e (Ncore, Nx, Ny, Nz, idx0,
  *                          spaceNyz, spaceNz, Ex..CEz, Jx..CJBz): the box and
  *                          strides travel in fdtd_drude / fdtd_grid
+ *   fdtd_tfsf_update_{e,h}_f32  kuFDTD/v0.2.0/dim3/tfsf.py Tfsf.updateE(tstep) /
+ *                          updateH() (Fdtd1d + TfsfFace + TfsfIncNormal)
  *   fdtd_step_unfused_f32  one time step in the order of
  *                          fdtd3d_201_..._100000tstep.cu:718-742
  *   fdtd_yee_plan_*        the same step, fused into one pass per step
@@ -115,6 +117,24 @@ typedef struct {
     float *j2[3];
 } fdtd_drude;
 
+/* Total-field/scattered-field plane wave at normal incidence (kuFDTD Tfsf,
+ * kuFDTD/v0.2.0/dim3/tfsf.py:14-244).  p1, p2: corners of the total-field
+ * box as set_space leaves them (p2 = the given pt2 + 1); faces: bit f on for
+ * face f = x front, x back, y front, y back, z front, z back; axis: the
+ * propagation axis 0..2; angle: polarisation angle (radians).  The 1-D
+ * auxiliary grid lives in device arrays e1d, h1d of n1d = p2[axis] -
+ * p1[axis] + 11 floats and abc[4] (two-step delay of both ends), zeroed by
+ * the caller; amp[t] (t < namp) = sin(w dt t) is the hard source written
+ * to e1d[3] in step t. */
+typedef struct {
+    int64_t p1[3], p2[3];
+    int32_t faces, axis;
+    double angle;
+    float *e1d, *h1d, *abc;
+    const float *amp;
+    int64_t namp;
+} fdtd_tfsf;
+
 const char *fdtd_status_string(int status);
 int fdtd_last_cuda_error(void);
 
@@ -141,6 +161,14 @@ int fdtd_cpml_h_f32(const fdtd_grid *g, const fdtd_cpml *c,
                     const fdtd_psi *psi, void *stream);
 int fdtd_add_sources_f32(const fdtd_grid *g, const fdtd_sources *src, int64_t t,
                          float *ex, float *ey, float *ez, void *stream);
+/* TFSF: the 1-D E step (tfsf.py:26-38) of step t, then E += 0.5 * incident H
+ * on every enabled face (tfsf.py:234-237); call it after fdtd_cpml_e_f32.
+ * The H form: the 1-D H step, then H += 0.5 * incident E (tfsf.py:240-244);
+ * call it after fdtd_cpml_h_f32.  The box must lie inside the grid with one
+ * cell to spare on each side (the E faces sit at p1-1 and p2). */
+int fdtd_tfsf_update_e_f32(const fdtd_grid *g, const fdtd_tfsf *t, int64_t tstep, float *ex, float *ey, float *ez,
+                           void *stream);
+int fdtd_tfsf_update_h_f32(const fdtd_grid *g, const fdtd_tfsf *t, float *hx, float *hy, float *hz, void *stream);
 /* Drude ADE on the box of d (in place on E and d->j); call it between
  * fdtd_update_e_f32 and fdtd_cpml_e_f32. */
 int fdtd_drude_update_e_f32(const fdtd_grid *g, const fdtd_drude *d, float *ex, float *ey, float *ez,

@@ -15,7 +15,7 @@ from . import build as _build
 __all__ = ["update_e", "update_h", "pbc_e", "pbc_h", "cpml_e", "cpml_h",
            "add_points", "symp_h", "symp_e", "cpml_tables", "pulse",
            "OracleSim", "lib", "symp_h_scalar", "symp_cpml_e", "symp_cpml_h", "symp_stage_tables",
-           "drude_e", "drude_coefficients"]
+           "drude_e", "drude_coefficients", "TfsfNormal"]
 
 _LIBS = {}
 
@@ -206,6 +206,112 @@ def drude_coefficients(pfreq, gamma, dt=0.5):
     return cja.astype(np.float32), cjb.astype(np.float32)
 
 
+class TfsfNormal:
+    """Total-field/scattered-field plane wave at normal incidence, restated from
+    kuFDTD/v0.2.0/dim3/tfsf.py (test infrastructure only).
+
+    pt1, pt2: corners of the total-field box as Tfsf.set_space receives them
+    (None -> 1 / n-2), faces: 6 flags (x front, x back, y front, ... as
+    apply_direction 'fb'), axis 0..2: propagation axis, angle: polarisation
+    angle, wdt: wfreq*dt (the source phase step).  Arrays are float32; NumPy
+    1.x casting as in 2009 (scalar coefficients taken to float32).
+
+      Fdtd1d                 tfsf.py:14-40 (E, H of N+10 cells, Mur-like
+                             two-step delay at both ends, hard source E[3])
+      faces                  tfsf.py:140-186 (calc_face_list)
+      incident coefficients  tfsf.py:189-231 (calc_inc_list)
+      updateE / updateH      tfsf.py:234-244, TfsfFace tfsf.py:68-89
+    """
+
+    def __init__(self, shape, pt1, pt2, faces, axis, angle, wdt):
+        n3 = list(shape)
+        p1 = [1 if v is None else int(v) for v in pt1]
+        p2 = [n3[a] - 2 if v is None else int(v) for a, v in enumerate(pt2)]
+        p2 = [v + 1 for v in p2]
+        self.p1, self.p2, self.axis, self.faces = p1, p2, int(axis), [bool(f) for f in faces]
+        N = p2[axis] - p1[axis] + 1
+        self.E = np.zeros(N + 10, np.float32)
+        self.H = np.zeros(N + 10, np.float32)
+        self.abc = [np.float32(0)] * 4   # f1, f2, b1, b2
+        self.wdt = float(wdt)
+        si, co = np.float32(math.sin(angle)), np.float32(math.cos(angle))
+        # (ce1, ce2, ch1, ch2, sE1, sE2, sH1, sH2) of Inc1..Inc6; slice ids 1..5 of tfsf.py:195-199
+        zero = np.float32(0)
+        self.incs = [(-si, co, co, si, 1, 1, 2, 2), (si, -co, -co, -si, 5, 5, 5, 5),
+                     (zero, si, zero, -co, 4, 3, 3, 4), (zero, -si, zero, co, 4, 3, 3, 4),
+                     (-co, zero, -si, zero, 3, 4, 4, 3), (co, zero, si, zero, 3, 4, 4, 3)]
+        order = {0: [0, 1, 2, 3, 4, 5], 1: [4, 5, 0, 1, 2, 3], 2: [2, 3, 4, 5, 0, 1]}[self.axis]
+        self.face_inc = order   # face f (xf, xb, yf, yb, zf, zb) uses Inc order[f]
+
+    def _sl1d(self, sid):
+        i1, i2 = 5, self.p2[self.axis] - self.p1[self.axis] + 5
+        return {1: slice(i1 - 1, i1), 2: slice(i1, i1 + 1), 3: slice(i1, i2), 4: slice(i1, i2 + 1),
+                5: slice(i2, i2 + 1)}[sid]
+
+    def update_e1d(self, tstep):
+        E, H = self.E, self.H
+        E[1:-1] -= np.float32(0.5) * (H[2:] - H[1:-1])
+        E[0] = self.abc[0]
+        self.abc[0] = self.abc[1]
+        self.abc[1] = E[1]
+        E[-1] = self.abc[2]
+        self.abc[2] = self.abc[3]
+        self.abc[3] = E[-2]
+        E[3] = np.float32(math.sin(self.wdt * tstep))
+
+    def update_h1d(self):
+        self.H[1:] -= np.float32(0.5) * (self.E[1:] - self.E[:-1])
+
+    def _faces(self, f):
+        """(e1, e2, h1, h2) component names and their index tuples (tfsf.py:140-186)."""
+        (i1, j1, k1), (i2, j2, k2) = self.p1, self.p2
+        sx, sxp, sy, syp, sz, szp = (slice(i1, i2), slice(i1, i2 + 1), slice(j1, j2), slice(j1, j2 + 1),
+                                      slice(k1, k2), slice(k1, k2 + 1))
+        return [
+            (("ey", "ez", "hy", "hz"), ((i1 - 1, syp, sz), (i1 - 1, sy, szp), (i1, sy, szp), (i1, syp, sz))),
+            (("ey", "ez", "hy", "hz"), ((i2, syp, sz), (i2, sy, szp), (i2, sy, szp), (i2, syp, sz))),
+            (("ez", "ex", "hz", "hx"), ((sx, j1 - 1, szp), (sxp, j1 - 1, sz), (sxp, j1, sz), (sx, j1, szp))),
+            (("ez", "ex", "hz", "hx"), ((sx, j2, szp), (sxp, j2, sz), (sxp, j2, sz), (sx, j2, szp))),
+            (("ex", "ey", "hx", "hy"), ((sxp, sy, k1 - 1), (sx, syp, k1 - 1), (sx, syp, k1), (sxp, sy, k1))),
+            (("ex", "ey", "hx", "hy"), ((sxp, sy, k2), (sx, syp, k2), (sx, syp, k2), (sxp, sy, k2))),
+        ][f]
+
+    def _inc(self, f, eh):
+        """The two incident arrays of face f for E (eh=0: the face's E update reads
+        the 1-D H) or H (eh=1), broadcast to the face slices (newaxis of tfsf.py:201-214)."""
+        ce1, ce2, ch1, ch2, sE1, sE2, sH1, sH2 = self.incs[self.face_inc[f]]
+        if eh == 0:
+            c1, c2, a1, a2 = ch1, ch2, self.H[self._sl1d(sH1)], self.H[self._sl1d(sH2)]
+        else:
+            c1, c2, a1, a2 = ce1, ce2, self.E[self._sl1d(sE1)], self.E[self._sl1d(sE2)]
+        newaxis = {0: [0, 0, 1, 1, 1, 1], 1: [1, 1, 0, 0, 0, 0], 2: [0, 0, 0, 0, 0, 0]}[self.axis][f]
+        ex = [slice(None)]
+        ex.insert(newaxis, None)
+        return (c1 * a1)[tuple(ex)], (c2 * a2)[tuple(ex)]
+
+    def update_e(self, fields, tstep):
+        """tfsf.py:234-237: 1-D E step, then E += 0.5 * incident H on every face."""
+        self.update_e1d(tstep)
+        for f in range(6):
+            if not self.faces[f]:
+                continue
+            names, idx = self._faces(f)
+            h1, h2 = self._inc(f, 0)
+            fields[names[0]][idx[0]] += np.float32(0.5) * h1
+            fields[names[1]][idx[1]] += np.float32(0.5) * h2
+
+    def update_h(self, fields):
+        """tfsf.py:240-244: 1-D H step, then H += 0.5 * incident E on every face."""
+        self.update_h1d()
+        for f in range(6):
+            if not self.faces[f]:
+                continue
+            names, idx = self._faces(f)
+            e1, e2 = self._inc(f, 1)
+            fields[names[2]][idx[2]] += np.float32(0.5) * e1
+            fields[names[3]][idx[3]] += np.float32(0.5) * e2
+
+
 class OracleSim:
     """Whole-step oracle: state in NumPy arrays, canonical step order.
 
@@ -216,10 +322,13 @@ class OracleSim:
     amplitude table is indexed by the 1-based step number.
     """
 
-    def __init__(self, fields, npml=(0, 0, 0), faces=0x3F, tables=None, sources=(), drude=None):
+    def __init__(self, fields, npml=(0, 0, 0), faces=0x3F, tables=None, sources=(), drude=None, tfsf=None):
         # drude: optional (box (i0, j0, k0), J[3], CJA[3], CJB[3]) applied after update_e
-        # (kuFDTD/v0.2.0/dim3/cpu/test/030-drude-cpml.py:88-92 step order)
+        # (kuFDTD/v0.2.0/dim3/cpu/test/030-drude-cpml.py:88-92 step order);
+        # tfsf: optional TfsfNormal applied after cpml_e and after cpml_h
+        # (kuFDTD/v0.2.0/dim3/cpu/test/200-dielectric-cpml-output-tfsf.py:72-78), point sources after it
         self.drude = drude
+        self.tfsf = tfsf
         self.f = fields
         ex = fields["ex"]
         self.dtype = ex.dtype
@@ -251,12 +360,16 @@ class OracleSim:
                 drude_e(box, *E, *CE, J, CJA, CJB)
             if pml:
                 cpml_e(self.npml, self.faces, self.tables, *E, *H, *CE, self.psi_e)
+            if self.tfsf is not None:
+                self.tfsf.update_e(f, self.tstep)
             for comp, (i, j, k), amp in self.sources:
                 arr = f[comp]
                 arr[i, j, k] = arr[i, j, k] + np.asarray(amp[self.tstep], dtype=self.dtype)
             update_h(*E, *H, *CH)
             if pml:
                 cpml_h(self.npml, self.faces, self.tables, *E, *H, self.psi_h, *CH)
+            if self.tfsf is not None:
+                self.tfsf.update_h(f)
             self.tstep += 1
 
 

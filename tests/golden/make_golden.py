@@ -301,8 +301,77 @@ def drude_kufdtd(rng):
     return out
 
 
+def _reference_tfsf_module():
+    """kuFDTD/v0.2.0/dim3/tfsf.py executed in place under Python 3: its
+    imports (kufdtd.common: scipy as sc, light_velocity) are provided by a stub
+    module, and three Python-2 idioms are mapped when the text is compiled
+    (xrange -> range, `is` between strings -> ==, list indices -> tuples)."""
+    import types
+    common = types.ModuleType("kufdtd.common")
+
+    class SC:
+        zeros = staticmethod(np.zeros)
+        sin = staticmethod(np.sin)
+        cos = staticmethod(np.cos)
+        sqrt = staticmethod(np.sqrt)
+        newaxis = None
+        pi = np.pi
+    common.sc = SC
+    common.light_velocity = 2.99792458e8
+    pkg = types.ModuleType("kufdtd")
+    pkg.common = common
+    sys.modules.setdefault("kufdtd", pkg)
+    sys.modules.setdefault("kufdtd.common", common)
+    path = os.path.join(build_ref.REF, "kuFDTD/v0.2.0/dim3/tfsf.py")
+    src = open(path).read()
+    src = src.replace("from kufdtd.common import *", "from kufdtd.common import sc, light_velocity")
+    src = src.replace(" is '", " == '").replace("' is ", "' == ").replace("[s.sl_expand]", "[tuple(s.sl_expand)]")
+    ns = {"xrange": range}
+    exec(compile(src, path, "exec"), ns)
+    return ns
+
+
+def tfsf_kufdtd(rng):
+    """kuFDTD Tfsf.updateE/updateH from zero fields (no 3-D update in between,
+    so only face cells change), polarisation angle 0 (coefficients 0 and +-1:
+    the result does not depend on the NumPy version's scalar casting), every
+    propagation axis, all faces and a subset."""
+    ns = _reference_tfsf_module()
+
+    class Space:
+        pass
+    out = {}
+    n = 0
+    shape = (18, 16, 14)
+    for axis in "xyz":
+        for apply in (("fb", "fb", "fb"), ("f", "b", "fb")):
+            S = Space()
+            S.Nx, S.Ny, S.Nz = shape
+            S.dx = 1.0
+            S.dt = 0.5 / 2.99792458e8          # w dt = 2 pi 0.5 / wavelength (in cells)
+            f0 = {k: np.zeros(shape, F32) for k in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+            for k, v in f0.items():
+                setattr(S, k, v.copy())
+            T = ns["Tfsf"]((5, 4, 3), (12, 11, 10), apply, 10.0, ["normal", axis], 0.0)
+            T.set_space(S)
+            for t in range(1, 13):
+                T.updateE(t)
+                T.updateH()
+            tag = "c%d_" % n
+            out[tag + "meta"] = np.array(["xyz".index(axis)] + [int("f" in a) * 1 + int("b" in a) * 2 for a in apply])
+            for k in f0:
+                out[tag + "out_" + k.lower()] = getattr(S, k)
+            out[tag + "e1d"] = T.space1d.E
+            out[tag + "h1d"] = T.space1d.H
+            n += 1
+    out["ncases"] = np.array(n)
+    out["pt"] = np.array([[5, 4, 3], [12, 11, 10]])
+    out["wdt"] = np.array(2 * np.pi * 2.99792458e8 / 10.0 * (0.5 / 2.99792458e8))
+    return out
+
+
 CASES = (("yee_numpy", yee_numpy), ("kemp_core", kemp_core), ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c),
-         ("drude_kufdtd", drude_kufdtd))
+         ("drude_kufdtd", drude_kufdtd), ("tfsf_kufdtd", tfsf_kufdtd))
 
 
 def main():

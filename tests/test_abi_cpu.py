@@ -104,3 +104,22 @@ def test_drude_validation_before_cuda(lib):
     d.k0, d.ni = 4, 0
     assert lib.fdtd_drude_update_e_f32(C.byref(g), C.byref(d), *fake, None) == N.FDTD_ERR_SHAPE
     assert lib.fdtd_drude_update_e_f32(C.byref(g), None, *fake, None) == N.FDTD_ERR_ARG
+
+
+def test_tfsf_validation_before_cuda(lib):
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(20, 20, 20, 400, 20)
+    fake = [C.c_void_p(256 * (q + 1)) for q in range(3)]
+    t = N.Tfsf()
+    for a in range(3):
+        t.p1[a], t.p2[a] = 5, 12
+    t.faces, t.axis = 0x3F, 0
+    assert lib.fdtd_tfsf_update_e_f32(C.byref(g), C.byref(t), 1, *fake, None) == N.FDTD_ERR_ARG  # no 1-D arrays
+    t.e1d = t.h1d = t.abc = t.amp = 4096
+    t.namp = 8
+    t.p2[2] = 20                                            # p2 must stay below n
+    assert lib.fdtd_tfsf_update_e_f32(C.byref(g), C.byref(t), 1, *fake, None) == N.FDTD_ERR_SHAPE
+    t.p2[2] = 12
+    assert lib.fdtd_tfsf_update_e_f32(C.byref(g), C.byref(t), 8, *fake, None) == N.FDTD_ERR_ARG  # past the table
+    t.axis = 3
+    assert lib.fdtd_tfsf_update_h_f32(C.byref(g), C.byref(t), *fake, None) == N.FDTD_ERR_ARG

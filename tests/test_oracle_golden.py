@@ -185,3 +185,25 @@ def test_cpml_tables_shape_and_range(npml):
     # front slab is the mirror of the back slab
     np.testing.assert_allclose(t["b_e"][:npml][::-1], t["b_e"][npml:])
     np.testing.assert_allclose(t["b_h"][:npml][::-1], t["b_h"][npml:])
+
+
+def test_oracle_tfsf_matches_kufdtd_bit_exact(golden_dir):
+    """Reference kuFDTD Tfsf (executed in place by tests/golden/make_golden.py),
+    12 updateE/updateH pairs from zero fields, every axis, all faces and a subset."""
+    g = np.load(os.path.join(golden_dir, "tfsf_kufdtd.npz"))
+    p1, p2 = [tuple(int(v) for v in r) for r in g["pt"]]
+    shape = g["c0_out_ex"].shape
+    for n in range(int(g["ncases"])):
+        t = "c%d_" % n
+        m = g[t + "meta"]
+        axis, apply = int(m[0]), m[1:]
+        faces = [bool(apply[a] & (1 if s == 0 else 2)) for a in range(3) for s in range(2)]
+        ref = oracle.TfsfNormal(shape, p1, p2, faces, axis, 0.0, float(g["wdt"]))
+        f = {k: np.zeros(shape, np.float32) for k in NAMES}
+        for step in range(1, 13):
+            ref.update_e(f, step)
+            ref.update_h(f)
+        for k in NAMES:
+            np.testing.assert_array_equal(f[k], g[t + "out_" + k], err_msg="case %d %s" % (n, k))
+        np.testing.assert_array_equal(ref.E, g[t + "e1d"])
+        np.testing.assert_array_equal(ref.H, g[t + "h1d"])

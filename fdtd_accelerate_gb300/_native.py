@@ -53,7 +53,8 @@ class Tfsf(C.Structure):
 
 
 class YeeState(C.Structure):
-    _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3), ("drude", P)]
+    _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3), ("drude", P),
+                ("tfsf", P)]
 
 
 class Tile(C.Structure):

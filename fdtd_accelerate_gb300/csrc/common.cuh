@@ -44,6 +44,14 @@ inline bool all_nonnull(P... p) {
     return ((p != nullptr) && ...);
 }
 
+// TFSF helpers (tfsf.cu): validation, 1-D grid length, the fused-step table
+// and the 1-D steps (which: 0 = E step of step t, 1 = H step, 2 = H step then
+// the E step of step t).
+int validate_tfsf(const Grid &g, const fdtd_tfsf *t);
+int64_t tfsf_n1d(const fdtd_tfsf *t);
+void tfsf_table(const fdtd_tfsf *t, float coef[2][6][2], int32_t ix[2][6][2], int32_t *vo);
+int tfsf_launch_1d(const fdtd_tfsf *t, int which, int64_t step, cudaStream_t st);
+
 // Drude box inside the grid, all nine arrays present.
 inline int validate_drude(const Grid &g, const fdtd_drude *d) {
     if (!d) return FDTD_ERR_ARG;

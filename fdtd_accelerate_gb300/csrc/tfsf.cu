@@ -164,6 +164,54 @@ __global__ void __launch_bounds__(kTfsfBlock) k_tfsf_h1d(float *h, const float *
     for (int64_t i = 1 + threadIdx.x; i < n; i += blockDim.x) h[i] = fsub(h[i], fmul(0.5f, fsub(e[i], e[i - 1])));
 }
 
+// The 1-D H step of step t followed by the 1-D E step of step t+1 (one block;
+// between two fused steps).
+__global__ void __launch_bounds__(kTfsfBlock)
+k_tfsf_he1d(float *e, float *h, float *abc, int64_t n, const float *amp, int64_t t_next) {
+    for (int64_t i = 1 + threadIdx.x; i < n; i += blockDim.x) h[i] = fsub(h[i], fmul(0.5f, fsub(e[i], e[i - 1])));
+    __syncthreads();
+    for (int64_t i = 1 + threadIdx.x; i < n - 1; i += blockDim.x) e[i] = fsub(e[i], fmul(0.5f, fsub(h[i + 1], h[i])));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        e[0] = abc[0];
+        abc[0] = abc[1];
+        abc[1] = e[1];
+        e[n - 1] = abc[2];
+        abc[2] = abc[3];
+        abc[3] = e[n - 2];
+        e[3] = amp[t_next];
+    }
+}
+
+// Fused-step form: coefficient and 1-D index of every (half, face, slot) and
+// the offset of the varying index (tfsf.py:189-231).
+void tfsf_table(const fdtd_tfsf *t, float coef[2][6][2], int32_t ix[2][6][2], int32_t *vo) {
+    for (int eh = 0; eh < 2; eh++) {
+        const TfsfHalf h = tfsf_half(t, eh);
+        int n = 0;
+        for (int f = 0; f < 6; f++)
+            for (int q = 0; q < 2; q++) {
+                coef[eh][f][q] = 0.f;
+                ix[eh][f][q] = 0;
+                if (!((t->faces >> f) & 1)) continue;
+                const TfsfSlice &s = h.s[n++];
+                coef[eh][f][q] = s.coef;
+                ix[eh][f][q] = s.vary ? -1 : s.idx;
+            }
+    }
+    *vo = 5 - (int32_t)t->p1[t->axis];
+}
+
+// which: 0 = 1-D E step of step t, 1 = 1-D H step, 2 = H step then E step of step t
+int tfsf_launch_1d(const fdtd_tfsf *t, int which, int64_t step, cudaStream_t st) {
+    if (which != 1 && (step < 0 || step >= t->namp)) return FDTD_ERR_ARG;
+    const int64_t n = tfsf_n1d(t);
+    if (which == 0) k_tfsf_e1d<<<1, kTfsfBlock, 0, st>>>(t->e1d, t->h1d, t->abc, n, t->amp, step);
+    else if (which == 1) k_tfsf_h1d<<<1, kTfsfBlock, 0, st>>>(t->h1d, t->e1d, n);
+    else k_tfsf_he1d<<<1, kTfsfBlock, 0, st>>>(t->e1d, t->h1d, t->abc, n, t->amp, step);
+    return check_launch();
+}
+
 // face corrections of slices first, first+1 (one face: two components);
 // blockIdx.y picks the slice, threads run over its cells
 __global__ void __launch_bounds__(kTfsfBlock)

@@ -119,6 +119,14 @@ struct Params {
     const float *dj_in[3];
     float *dj_out[3];
     const float *dcja[3], *dcjb[3];
+    // TFSF plane wave (tfsf = 1): box corners tp1, tp2 (p2 = pt2 + 1), face bits, axis;
+    // incident table per half (0: E faces read th1d, 1: H faces read te1d), face, slot:
+    // coefficient and 1-D index (tix >= 0: fixed; < 0: coordinate along the axis + tvo)
+    int32_t tfsf, tfaces, taxis, tvo;
+    int32_t tp1[3], tp2[3];
+    float tcoef[2][6][2];
+    int32_t tix[2][6][2];
+    const float *te1d, *th1d;
 };
 
 // Many independent grids advanced by one launch: work items of all grids are
@@ -260,6 +268,59 @@ __device__ __forceinline__ float corr(float &psi, const Coef &c, float d) {
 __device__ __forceinline__ Coef tab_coef(const float *tabs, int base, int n2, int eh, int s) {
     const float *t = tabs + base + eh * 3 * n2;
     return Coef{t[s], t[n2 + s], t[2 * n2 + s]};
+}
+
+// TFSF correction of one face slot: v += 0.5 (c * F1d[idx]) (kuFDTD/v0.2.0/dim3/tfsf.py:79-89)
+__device__ __forceinline__ void tfsf_add(const Params &p, int half, int f, int slot, const float *f1d, int64_t ax,
+                                         float &v) {
+    const int32_t ix = p.tix[half][f][slot];
+    const float c = p.tcoef[half][f][slot];
+    v = fadd(v, fmul(0.5f, fmul(c, f1d[ix >= 0 ? (int64_t)ix : ax + p.tvo])));
+}
+__device__ __forceinline__ bool tin(int64_t x, int32_t lo, int32_t hi) { return x >= lo && x <= hi; }
+
+// E component q (0 ex, 1 ey, 2 ez) at (i, j, k): the face slices of tfsf.py:154-186 that
+// contain it (disjoint for E); returns true when one applied
+__device__ __forceinline__ bool tfsf_e_comp(const Params &p, int q, int64_t i, int64_t j, int64_t k, float &v) {
+    const int32_t i1 = p.tp1[0], j1 = p.tp1[1], k1 = p.tp1[2], i2 = p.tp2[0], j2 = p.tp2[1], k2 = p.tp2[2];
+    const int64_t ax = p.taxis == 0 ? i : (p.taxis == 1 ? j : k);
+    const float *h1 = p.th1d;
+    int f = -1, slot = 0;
+    if (q == 0) {         // ex: y faces (slot e2), z faces (slot e1)
+        if (tin(i, i1, i2) && tin(k, k1, k2 - 1) && (j == j1 - 1 || j == j2)) { f = j == j2 ? 3 : 2; slot = 1; }
+        else if (tin(i, i1, i2) && tin(j, j1, j2 - 1) && (k == k1 - 1 || k == k2)) { f = k == k2 ? 5 : 4; slot = 0; }
+    } else if (q == 1) {  // ey: x faces (e1), z faces (e2)
+        if (tin(j, j1, j2) && tin(k, k1, k2 - 1) && (i == i1 - 1 || i == i2)) { f = i == i2 ? 1 : 0; slot = 0; }
+        else if (tin(i, i1, i2 - 1) && tin(j, j1, j2) && (k == k1 - 1 || k == k2)) { f = k == k2 ? 5 : 4; slot = 1; }
+    } else {              // ez: x faces (e2), y faces (e1)
+        if (tin(j, j1, j2 - 1) && tin(k, k1, k2) && (i == i1 - 1 || i == i2)) { f = i == i2 ? 1 : 0; slot = 1; }
+        else if (tin(i, i1, i2 - 1) && tin(k, k1, k2) && (j == j1 - 1 || j == j2)) { f = j == j2 ? 3 : 2; slot = 0; }
+    }
+    if (f < 0 || !((p.tfaces >> f) & 1)) return false;
+    tfsf_add(p, 0, f, slot, h1, ax, v);
+    return true;
+}
+
+// H component q at (i, j, k): up to two faces on the box edges, applied in face order
+__device__ __forceinline__ bool tfsf_h_comp(const Params &p, int q, int64_t i, int64_t j, int64_t k, float &v) {
+    const int32_t i1 = p.tp1[0], j1 = p.tp1[1], k1 = p.tp1[2], i2 = p.tp2[0], j2 = p.tp2[1], k2 = p.tp2[2];
+    const int64_t ax = p.taxis == 0 ? i : (p.taxis == 1 ? j : k);
+    const float *e1 = p.te1d;
+    int fa = -1, sa = 0, fb = -1, sb = 0;
+    if (q == 0) {         // hx: y faces (h2), then z faces (h1)
+        if (tin(i, i1, i2 - 1) && tin(k, k1, k2) && (j == j1 || j == j2)) { fa = j == j2 ? 3 : 2; sa = 1; }
+        if (tin(i, i1, i2 - 1) && tin(j, j1, j2) && (k == k1 || k == k2)) { fb = k == k2 ? 5 : 4; sb = 0; }
+    } else if (q == 1) {  // hy: x faces (h1), then z faces (h2)
+        if (tin(j, j1, j2 - 1) && tin(k, k1, k2) && (i == i1 || i == i2)) { fa = i == i2 ? 1 : 0; sa = 0; }
+        if (tin(i, i1, i2) && tin(j, j1, j2 - 1) && (k == k1 || k == k2)) { fb = k == k2 ? 5 : 4; sb = 1; }
+    } else {              // hz: x faces (h2), then y faces (h1)
+        if (tin(j, j1, j2) && tin(k, k1, k2 - 1) && (i == i1 || i == i2)) { fa = i == i2 ? 1 : 0; sa = 1; }
+        if (tin(i, i1, i2) && tin(k, k1, k2 - 1) && (j == j1 || j == j2)) { fb = j == j2 ? 3 : 2; sb = 0; }
+    }
+    bool any = false;
+    if (fa >= 0 && ((p.tfaces >> fa) & 1)) { tfsf_add(p, 1, fa, sa, e1, ax, v); any = true; }
+    if (fb >= 0 && ((p.tfaces >> fb) & 1)) { tfsf_add(p, 1, fb, sb, e1, ax, v); any = true; }
+    return any;
 }
 
 template <int TY, int NS, bool BATCH>
@@ -538,7 +599,13 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             if (nplanes > 1) issue_psi(0);
         }
         const int nls = s_nls;
-        const bool tile_plain = y_plain && nls == 0 && !dtile;
+        // the item's E/H region meets a TFSF face (E faces at p1-1 and p2, H faces at p1 and p2)
+        // and is not strictly inside the box
+        const bool ttile = p.tfsf && i_start <= p.tp2[0] && x1 - 1 >= p.tp1[0] - 1 && j0 - 1 <= p.tp2[1] &&
+                           j0 + TY - 1 >= p.tp1[1] - 1 && k0 - 1 <= p.tp2[2] && k0 + TZ - 1 >= p.tp1[2] - 1 &&
+                           !(i_start > p.tp1[0] && x1 - 1 < p.tp2[0] && j0 - 1 > p.tp1[1] && j0 + TY - 1 < p.tp2[1] &&
+                             k0 - 1 > p.tp1[2] && k0 + TZ - 1 < p.tp2[2]);
+        const bool tile_plain = y_plain && nls == 0 && !dtile && !ttile;
 
         float2 prev_ey = make_float2(0.f, 0.f), prev_ez = make_float2(0.f, 0.f);
         float2 oex = prev_ey, oey = prev_ey, oez = prev_ey;  // own E_new pair
@@ -664,6 +731,18 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             }
                         }
                     }
+                    if (ttile) {  // TFSF: E += 0.5 (c * H1d), after the CPML terms, before the sources
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (!(e ? in1 : in0)) continue;
+                            float v = get(ex, e);
+                            if (tfsf_e_comp(p, 0, i, jj, kk + e, v)) set(ex, e, v);
+                            v = get(ey, e);
+                            if (tfsf_e_comp(p, 1, i, jj, kk + e, v)) set(ey, e, v);
+                            v = get(ez, e);
+                            if (tfsf_e_comp(p, 2, i, jj, kk + e, v)) set(ez, e, v);
+                        }
+                    }
                     const uint32_t ij_here = ((uint32_t)i << 16) | (uint32_t)jj;
                     for (int s = 0; s < nls; s++) {  // soft sources, list order
                         if (s_ls_ij[s] != ij_here) continue;
@@ -750,6 +829,18 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                                     set(hx, e, fsub(get(hx, e), fmul(0.5f, tc)));
                                 }
                             }
+                        }
+                    }
+                    if (ttile) {  // TFSF: H += 0.5 (c * E1d), after the CPML terms
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            if (!(e ? in1 : in0)) continue;
+                            float v = get(hx, e);
+                            if (tfsf_h_comp(p, 0, i, jj, kk + e, v)) set(hx, e, v);
+                            v = get(hy, e);
+                            if (tfsf_h_comp(p, 1, i, jj, kk + e, v)) set(hy, e, v);
+                            v = get(hz, e);
+                            if (tfsf_h_comp(p, 2, i, jj, kk + e, v)) set(hz, e, v);
                         }
                     }
                     const int64_t gi = i * p.sx + jj * p.sy + kk;
@@ -1085,6 +1176,8 @@ struct fdtd_yee_plan {
     float *f[2][6];
     float *psi_e[2][6];
     float *dj[2][3];  // Drude J buffers
+    bool has_tfsf;
+    fdtd_tfsf tfsf;   // plane-wave source (1-D grid arrays owned by the caller)
 };
 
 // 3-D FP32 tensor map: dims (n0 fastest, n1, n2), element strides s1, s2,
@@ -1196,6 +1289,30 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
             p.dcja[q] = d.cja[q];
             p.dcjb[q] = d.cjb[q];
         }
+    }
+    if (s->tfsf) {
+        const int st = validate_tfsf(g, s->tfsf);
+        if (st != FDTD_OK) { delete pl; return st; }
+        const fdtd_tfsf &t = *s->tfsf;
+        // the box's face cells (p1-1 .. p2) stay clear of the CPML slabs and of the
+        // z band, which the band kernels finish after the fused kernel
+        const int64_t n3[3] = {g.nx, g.ny, g.nz};
+        for (int a = 0; a < 3; a++) {
+            const int64_t P = c ? c->npml[a] : 0;
+            if (P > 0 && (t.p1[a] - 1 < P + 2 || t.p2[a] + 1 > n3[a] - P - 2)) { delete pl; return FDTD_ERR_UNSUPPORTED; }
+        }
+        pl->has_tfsf = true;
+        pl->tfsf = t;
+        p.tfsf = 1;
+        p.tfaces = t.faces;
+        p.taxis = t.axis;
+        for (int a = 0; a < 3; a++) {
+            p.tp1[a] = (int32_t)t.p1[a];
+            p.tp2[a] = (int32_t)t.p2[a];
+        }
+        tfsf_table(&t, p.tcoef, p.tix, &p.tvo);
+        p.te1d = t.e1d;
+        p.th1d = t.h1d;
     }
     // the z slab (when a z face has CPML) is finished by the band kernels
     p.zfix = (p.P[2] > 0 && ((p.faces >> 4) & 3)) ? 1 : 0;
@@ -1330,6 +1447,13 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
 int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *stream) {
     if (!pl || nsteps < 0) return FDTD_ERR_ARG;
     cudaStream_t st = as_stream(stream);
+    // TFSF: the 1-D E step of each step runs before its fused kernel (whose E
+    // faces read the 1-D H of the previous step, H faces the new 1-D E), the
+    // 1-D H step after it
+    if (pl->has_tfsf && nsteps > 0) {
+        if (t0 + nsteps - 1 >= pl->tfsf.namp || t0 < 0) return FDTD_ERR_ARG;
+        FDTD_TRY(tfsf_launch_1d(&pl->tfsf, 0, t0, st));
+    }
     for (int64_t n = 0; n < nsteps; n++) {
         const int in = pl->cur, outb = 1 - pl->cur;
         Params p = pl->base;
@@ -1352,6 +1476,7 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
             k_zband_h<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(p);
         }
         FDTD_TRY(check_launch());
+        if (pl->has_tfsf) FDTD_TRY(tfsf_launch_1d(&pl->tfsf, n + 1 < nsteps ? 2 : 1, t0 + n + 1, st));
         pl->cur = outb;
     }
     return FDTD_OK;
@@ -1375,7 +1500,7 @@ int fdtd_yee_plan_info(const fdtd_yee_plan *pl, int32_t *info, int32_t n) {
     info[5] = pl->smem;
     if (n >= 8) {
         info[6] = pl->base.zfix;                  // 1: z slab on the band kernels
-        info[7] = pl->base.zfix ? 3 : 1;          // kernel launches per step
+        info[7] = (pl->base.zfix ? 3 : 1) + (pl->has_tfsf ? 1 : 0);  // kernel launches per step
     }
     return FDTD_OK;
 }
@@ -1452,6 +1577,8 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
         return std::min<int64_t>(xc, grids[s].nx) * 65536 + std::min<int64_t>(grids[s].ny, 65535);
     };
     std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return item_len(a) > item_len(b); });
+    for (int32_t s = 0; s < nsims; s++)
+        if (states[s].tfsf) return FDTD_ERR_UNSUPPORTED;  // plane waves: single-grid plans only
     for (int32_t s = 0; s < nsims; s++) {
         const int32_t u = order[s];
         fdtd_yee_plan *pl = nullptr;

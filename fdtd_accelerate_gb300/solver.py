@@ -52,8 +52,8 @@ class YeeSolver:
         # optional Drude region (DrudeAde), applied after the E update, before the CPML
         if drude is not None and (tuple(drude.grid_shape) != self.shape or drude.J.device != self._state.device):
             raise ValueError("the Drude region belongs to a %s grid on %s" % (drude.grid_shape, drude.J.device))
-        # optional plane-wave source (Tfsf): step_unfused applies it after the
-        # E and H CPML corrections; the fused step does not take it
+        # optional plane-wave source (Tfsf), applied after the E and H CPML
+        # corrections (before the point sources) by both steps
         if tfsf is not None and tuple(tfsf.shape) != self.shape:
             raise ValueError("the TFSF source belongs to a %s grid" % (tfsf.shape,))
         self.tfsf = tfsf
@@ -129,6 +129,8 @@ class YeeSolver:
         for q in range(3):
             s.ce[q] = self._ce[q].data_ptr()
         s.drude = C.addressof(self._drude_struct) if self._drude_struct is not None else None
+        self._tfsf_struct = self.tfsf.struct() if self.tfsf is not None else None
+        s.tfsf = C.addressof(self._tfsf_struct) if self._tfsf_struct is not None else None
         return s
 
     def plan(self):
@@ -154,7 +156,11 @@ class YeeSolver:
 
     def step(self, n=1):
         if self.tfsf is not None:
-            raise NotImplementedError("the fused step has no TFSF face corrections; use step_unfused")
+            # the plan holds the source table's address: a longer table needs a new plan
+            old = self.tfsf.amp.data_ptr()
+            self.tfsf.ensure_steps(self.tstep + n)
+            if self.tfsf.amp.data_ptr() != old:
+                self.close()
         """Advance n steps with the fused kernel (one launch per step)."""
         plan = self.plan()
         L = N.lib()

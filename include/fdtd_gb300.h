@@ -191,6 +191,8 @@ typedef struct {
     float *psi_h[6];
     const float *ce[3];
     const fdtd_drude *drude;  /* NULL: no dispersive region */
+    const fdtd_tfsf *tfsf;    /* NULL: no plane wave; else the fused step applies it (box
+                                 faces at least P+2 cells away from every CPML slab) */
 } fdtd_yee_state;
 
 /* Launch shape of the fused kernel (0 = default): tile height in y (4, 8

@@ -39,9 +39,12 @@ def _tables(npml):
     ((40, 34, 36), 6, (10, 9, 9), (29, 24, 26), ("fb", "fb", "fb"), "y", 0.6),
     ((40, 34, 36), 6, (10, 9, 9), (29, 24, 26), ("fb", "fb", "fb"), "z", 1.1),
     ((30, 33, 40), 0, (3, None, 5), (25, None, 30), ("f", "", "fb"), "z", 0.3),   # open y, PEC walls
-    ((36, 30, 31), 5, (8, 7, 7), (27, 22, 23), ("b", "fb", "f"), "x", 2.0),
+    ((36, 30, 31), 5, (8, 8, 8), (27, 21, 22), ("b", "fb", "f"), "x", 2.0),
 ])
-def test_unfused_step_with_tfsf_bit_exact(F, shape, npml, pt1, pt2, apply, axis, angle):
+@pytest.mark.parametrize("fused", [False, True])
+def test_step_with_tfsf_bit_exact(F, shape, npml, pt1, pt2, apply, axis, angle, fused):
+    """Unfused (reference-shaped calls) and fused step with the plane wave,
+    CPML and a point source inside the box, against the oracle."""
     rng = np.random.default_rng(17)
     ce = [(0.5 / rng.uniform(1.0, 3.0, shape)).astype(np.float32) for _ in range(3)]
     init = {k: (0.05 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
@@ -59,15 +62,19 @@ def test_unfused_step_with_tfsf_bit_exact(F, shape, npml, pt1, pt2, apply, axis,
     sim.step(nsteps)
     s = F.YeeSolver(shape, ce=ce, npml=npml, sources=sources, tfsf=src)
     s.set_fields(**init)
-    s.step_unfused(nsteps)
+    if fused:
+        s.step(5)
+        s.step(nsteps - 5)          # two plan runs: the 1-D grid carries over
+        assert s.plan_info()["launches_per_step"] == (4 if npml else 2)
+    else:
+        s.step_unfused(nsteps)
     torch.cuda.synchronize()
+    s.check_status()
     for k in NAMES:
         np.testing.assert_array_equal(_host(s.fields[k]), sim.f[k], err_msg=k)
     np.testing.assert_array_equal(_host(src.e1d), ref.E)
     np.testing.assert_array_equal(_host(src.h1d), ref.H)
     np.testing.assert_array_equal(_host(src.abc), np.array(ref.abc, np.float32))
-    with pytest.raises(NotImplementedError):
-        s.step(1)
 
 
 def test_tfsf_plane_wave_stays_in_the_box(F):
@@ -86,6 +93,20 @@ def test_tfsf_plane_wave_stays_in_the_box(F):
     out[p1[0] - 2:p2[0] + 3, p1[1] - 2:p2[1] + 3, p1[2] - 2:p2[2] + 3] = False
     assert inside > 0.5
     assert e[out].max() < 1e-5 * inside
+
+
+def test_fused_plan_refusals(F):
+    """A box whose faces come within P+2 cells of a CPML slab, and a plane wave
+    in a batched plan, are refused (the unfused step still takes the first)."""
+    shape = (40, 34, 36)
+    src = F.Tfsf(shape, (7, 9, 9), (29, 24, 26))        # x front face at 6 < P + 2
+    s = F.YeeSolver(shape, npml=6, tfsf=src)
+    with pytest.raises(NotImplementedError):           # FDTD_ERR_UNSUPPORTED
+        s.step(1)
+    s.step_unfused(2)
+    src2 = F.Tfsf(shape, (10, 9, 9), (29, 24, 26))
+    with pytest.raises(NotImplementedError):
+        F.BatchSolver([F.YeeSolver(shape, npml=6, tfsf=src2), F.YeeSolver((20, 20, 20))]).step(1)
 
 
 def test_tfsf_arguments(F):

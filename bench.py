@@ -18,6 +18,8 @@ Other workloads (each prints its own line; the default is the headline):
                          forward cost and central differences at 32 cells
   --workload drude512    512^3 with a 256^3 Drude (ADE) box, 12-cell CPML,
                          beside the same grid without it
+  --workload tfsf512     512^3 with a TFSF plane wave on the box 64..447,
+                         12-cell CPML, beside the same grid without it
 
 --impl reference times the reference's CPU path on the host cores: the
 reference's own C cannot be built on the benchmark host (SSE intrinsics,
@@ -463,6 +465,54 @@ def run_drude512(args):
     print(json.dumps(line), flush=True)
 
 
+def run_tfsf512(args):
+    """512^3 vacuum, 12-cell CPML, a plane wave (TFSF, normal incidence along x,
+    wavelength 40 cells, polarisation 0.3 rad) on the box 64..447 in every axis; the
+    same grid without the plane wave is timed beside it."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    dev = torch.device("cuda", 0)
+    shape, npml, lo, hi = (512, 512, 512), 12, 64, 447
+    stream = torch.cuda.current_stream(dev)
+    results = {}
+    for with_tfsf in (False, True):
+        src = None
+        if with_tfsf:
+            src = F.Tfsf(shape, (lo,) * 3, (hi,) * 3, wavelength=40.0, propagation_direction=("normal", "x"),
+                         polarization_angle=0.3, steps=args.warmup + args.steps + 4, device=dev)
+        s = F.YeeSolver(shape, npml=npml, device=dev, tfsf=src, tile=args.tile)
+        for _ in range(args.warmup):
+            s.step(1)
+        sampler = ClockSampler(0)
+        sampler.start()
+        ms = _timed_steps(torch, stream, lambda: s.step(1), args.steps)
+        clocks = sampler.stop()
+        s.check_status()
+        results[with_tfsf] = (statistics.mean(ms), clocks, s.plan_info())
+        s.close()
+        del s, src
+        torch.cuda.empty_cache()
+    avg, clocks, info = results[True]
+    cells = int(np.prod(shape))
+    side = hi - lo + 2
+    face_cells = 6 * side * side
+    alg = algorithmic_bytes_per_step(shape, npml) + face_cells * 2 * 2 * 8
+    peak, psrc = measured_peak()
+    achieved = alg / (avg / 1e3) / 1e9
+    line = _base_line("Mcell-updates/s (Yee+CPML+TFSF plane wave 512^3, FP32)", cells / (avg / 1e3) / 1e6,
+                      UNIT, args, avg, "f32", "Yee + 12-cell CPML 512x512x512, vacuum, TFSF plane wave on the box "
+                      "64..447 (x incidence, wavelength 40 cells); state 6.4 GB >> L2",
+                      {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": None, "peak_source": psrc,
+                                    "alg_bytes_per_launch": alg,
+                                    "scope": "one time step (fused kernel, band kernels, 1-D grid kernel): "
+                                             "60 B/cell + 32 B per slab cell + 16 B per TFSF face cell and half"},
+                       "without_tfsf_ms_per_step": results[False][0],
+                       "clocks": clocks, "gpu_launches": args.steps * info["launches_per_step"]})
+    line["config"]["tile"] = info
+    print(json.dumps(line), flush=True)
+
+
 def run_batched64(args):
     """64 ragged grids in one launch per step (autotuned, graph-captured) against
     the same 64 grids solved one after another with the single-grid path."""
@@ -609,9 +659,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
                     help="timed steps (default 200; plain128 1000, symp512 50, batched64 500, adjoint256 3000, "
-                         "drude512 100)")
+                         "drude512 100, tfsf512 100)")
     ap.add_argument("--workload", default="cpml1024",
-                    choices=["cpml1024", "plain128", "symp512", "batched64", "adjoint256", "drude512"])
+                    choices=["cpml1024", "plain128", "symp512", "batched64", "adjoint256", "drude512", "tfsf512"])
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -626,14 +676,14 @@ def main():
         args.warmup = 3
     if args.steps is None:
         args.steps = {"cpml1024": 200, "plain128": 1000, "symp512": 50, "batched64": 500,
-                      "adjoint256": 3000, "drude512": 100}[args.workload]
+                      "adjoint256": 3000, "drude512": 100, "tfsf512": 100}[args.workload]
     if args.workload != "cpml1024":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "workload": args.workload,
                               "unavailable": "the reference arm covers the headline workload only"}), flush=True)
             return
         {"plain128": run_plain128, "symp512": run_symp512, "batched64": run_batched64,
-         "adjoint256": run_adjoint256, "drude512": run_drude512}[args.workload](args)
+         "adjoint256": run_adjoint256, "drude512": run_drude512, "tfsf512": run_tfsf512}[args.workload](args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

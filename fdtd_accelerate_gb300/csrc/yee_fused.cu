@@ -275,55 +275,92 @@ __device__ __forceinline__ void tfsf_add(const Params &p, int half, int f, int s
                                          float &v) {
     const int32_t ix = p.tix[half][f][slot];
     const float c = p.tcoef[half][f][slot];
-    v = fadd(v, fmul(0.5f, fmul(c, f1d[ix >= 0 ? (int64_t)ix : ax + p.tvo])));
+    // the 1-D grid is read-only inside the fused kernel: read-only data cache
+    v = fadd(v, fmul(0.5f, fmul(c, __ldg(f1d + (ix >= 0 ? (int64_t)ix : ax + p.tvo)))));
 }
 __device__ __forceinline__ bool tin(int64_t x, int32_t lo, int32_t hi) { return x >= lo && x <= hi; }
 
-// E component q (0 ex, 1 ey, 2 ez) at (i, j, k): the face slices of tfsf.py:154-186 that
-// contain it (disjoint for E); returns true when one applied
-__device__ __forceinline__ bool tfsf_e_comp(const Params &p, int q, int64_t i, int64_t j, int64_t k, float &v) {
-    const int32_t i1 = p.tp1[0], j1 = p.tp1[1], k1 = p.tp1[2], i2 = p.tp2[0], j2 = p.tp2[1], k2 = p.tp2[2];
-    const int64_t ax = p.taxis == 0 ? i : (p.taxis == 1 ? j : k);
-    const float *h1 = p.th1d;
-    int f = -1, slot = 0;
-    if (q == 0) {         // ex: y faces (slot e2), z faces (slot e1)
-        if (tin(i, i1, i2) && tin(k, k1, k2 - 1) && (j == j1 - 1 || j == j2)) { f = j == j2 ? 3 : 2; slot = 1; }
-        else if (tin(i, i1, i2) && tin(j, j1, j2 - 1) && (k == k1 - 1 || k == k2)) { f = k == k2 ? 5 : 4; slot = 0; }
-    } else if (q == 1) {  // ey: x faces (e1), z faces (e2)
-        if (tin(j, j1, j2) && tin(k, k1, k2 - 1) && (i == i1 - 1 || i == i2)) { f = i == i2 ? 1 : 0; slot = 0; }
-        else if (tin(i, i1, i2 - 1) && tin(j, j1, j2) && (k == k1 - 1 || k == k2)) { f = k == k2 ? 5 : 4; slot = 1; }
-    } else {              // ez: x faces (e2), y faces (e1)
-        if (tin(j, j1, j2 - 1) && tin(k, k1, k2) && (i == i1 - 1 || i == i2)) { f = i == i2 ? 1 : 0; slot = 1; }
-        else if (tin(i, i1, i2 - 1) && tin(k, k1, k2) && (j == j1 - 1 || j == j2)) { f = j == j2 ? 3 : 2; slot = 0; }
+// Per item and lane: for each cell e of the pair, component and face family
+// (the two face axes that can correct that component, in face order), a
+// 2-bit code from the cell's (j, k): 0 none, 1 front face, 2 back face, 3 one of
+// the two x faces (decided per plane).  Layout: bit (e*12 + (comp*2 + fam)*2).
+// E (tfsf.py:154-186 e1/e2 slices): ex (y face, z face), ey (x face, z face),
+// ez (x face, y face); H: hx (y, z), hy (x, z), hz (x, y).
+__device__ __forceinline__ uint32_t tfsf_lane_codes(const Params &p, int eh, int64_t j, int64_t k0c, bool in0,
+                                                    bool in1) {
+    const int32_t j1 = p.tp1[1], k1 = p.tp1[2], j2 = p.tp2[1], k2 = p.tp2[2];
+    const int32_t f = p.tfaces;
+    auto code = [&](bool cand, bool back, int face_front) -> uint32_t {
+        if (!cand) return 0;
+        const int face = face_front + (back ? 1 : 0);
+        return ((f >> face) & 1) ? (back ? 2u : 1u) : 0u;
+    };
+    uint32_t m = 0;
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        if (!(e ? in1 : in0)) continue;
+        const int64_t k = k0c + e;
+        uint32_t c[6];
+        if (eh == 0) {
+            const int32_t je0 = j1 - 1, ke0 = k1 - 1;  // E faces at p1-1 and p2
+            c[0] = code((j == je0 || j == j2) && tin(k, k1, k2 - 1), j == j2, 2);     // ex, y face
+            c[1] = code((k == ke0 || k == k2) && tin(j, j1, j2 - 1), k == k2, 4);     // ex, z face
+            c[2] = tin(j, j1, j2) && tin(k, k1, k2 - 1) ? 3u : 0u;                    // ey, x face
+            c[3] = code((k == ke0 || k == k2) && tin(j, j1, j2), k == k2, 4);         // ey, z face
+            c[4] = tin(j, j1, j2 - 1) && tin(k, k1, k2) ? 3u : 0u;                    // ez, x face
+            c[5] = code((j == je0 || j == j2) && tin(k, k1, k2), j == j2, 2);         // ez, y face
+        } else {                                       // H faces at p1 and p2
+            c[0] = code((j == j1 || j == j2) && tin(k, k1, k2), j == j2, 2);          // hx, y face
+            c[1] = code((k == k1 || k == k2) && tin(j, j1, j2), k == k2, 4);          // hx, z face
+            c[2] = tin(j, j1, j2 - 1) && tin(k, k1, k2) ? 3u : 0u;                    // hy, x face
+            c[3] = code((k == k1 || k == k2) && tin(j, j1, j2 - 1), k == k2, 4);      // hy, z face
+            c[4] = tin(j, j1, j2) && tin(k, k1, k2 - 1) ? 3u : 0u;                    // hz, x face
+            c[5] = code((j == j1 || j == j2) && tin(k, k1, k2 - 1), j == j2, 2);      // hz, y face
+        }
+#pragma unroll
+        for (int q = 0; q < 6; q++) m |= c[q] << (e * 12 + q * 2);
     }
-    if (f < 0 || !((p.tfaces >> f) & 1)) return false;
-    tfsf_add(p, 0, f, slot, h1, ax, v);
-    return true;
+    return m;
 }
 
-// H component q at (i, j, k): up to two faces on the box edges, applied in face order
-__device__ __forceinline__ bool tfsf_h_comp(const Params &p, int q, int64_t i, int64_t j, int64_t k, float &v) {
-    const int32_t i1 = p.tp1[0], j1 = p.tp1[1], k1 = p.tp1[2], i2 = p.tp2[0], j2 = p.tp2[1], k2 = p.tp2[2];
+// Apply the TFSF terms of one cell (codes = its 12 bits) to the three
+// components of the E (eh = 0) or H (eh = 1) field just updated at plane i.
+// Slot and face of each family as tfsf.py:154-186; the x faces of E at p1-1 and
+// p2, of H at p1 and p2; for H the two families apply in face order.
+__device__ __forceinline__ void tfsf_apply(const Params &p, int eh, uint32_t codes, int64_t i, int64_t j, int64_t k,
+                                           float &vx, float &vy, float &vz) {
+    const int32_t i1 = p.tp1[0], i2 = p.tp2[0];
     const int64_t ax = p.taxis == 0 ? i : (p.taxis == 1 ? j : k);
-    const float *e1 = p.te1d;
-    int fa = -1, sa = 0, fb = -1, sb = 0;
-    if (q == 0) {         // hx: y faces (h2), then z faces (h1)
-        if (tin(i, i1, i2 - 1) && tin(k, k1, k2) && (j == j1 || j == j2)) { fa = j == j2 ? 3 : 2; sa = 1; }
-        if (tin(i, i1, i2 - 1) && tin(j, j1, j2) && (k == k1 || k == k2)) { fb = k == k2 ? 5 : 4; sb = 0; }
-    } else if (q == 1) {  // hy: x faces (h1), then z faces (h2)
-        if (tin(j, j1, j2 - 1) && tin(k, k1, k2) && (i == i1 || i == i2)) { fa = i == i2 ? 1 : 0; sa = 0; }
-        if (tin(i, i1, i2) && tin(j, j1, j2 - 1) && (k == k1 || k == k2)) { fb = k == k2 ? 5 : 4; sb = 1; }
-    } else {              // hz: x faces (h2), then y faces (h1)
-        if (tin(j, j1, j2) && tin(k, k1, k2 - 1) && (i == i1 || i == i2)) { fa = i == i2 ? 1 : 0; sa = 1; }
-        if (tin(i, i1, i2) && tin(k, k1, k2 - 1) && (j == j1 || j == j2)) { fb = j == j2 ? 3 : 2; sb = 0; }
+    const float *f1d = eh == 0 ? p.th1d : p.te1d;
+    const bool xf = eh == 0 ? i == i1 - 1 : i == i1, xb = i == i2;  // x face planes
+    const bool xface = (xf && (p.tfaces & 1)) || (xb && ((p.tfaces >> 1) & 1));
+    const int xid = xf ? 0 : 1;
+    // x-range of the y and z families: [i1, i2] or [i1, i2-1] per component
+    const bool ir = tin(i, i1, i2), irm = tin(i, i1, i2 - 1);
+    const uint32_t c0 = codes & 3, c1 = (codes >> 2) & 3, c2 = (codes >> 4) & 3, c3 = (codes >> 6) & 3,
+                   c4 = (codes >> 8) & 3, c5 = (codes >> 10) & 3;
+    if (eh == 0) {
+        if (c0 && ir) tfsf_add(p, 0, 2 + (int)c0 - 1, 1, f1d, ax, vx);      // ex += y face (slot e2)
+        if (c1 && ir) tfsf_add(p, 0, 4 + (int)c1 - 1, 0, f1d, ax, vx);      // ex += z face (e1)
+        if (c2 && xface) tfsf_add(p, 0, xid, 0, f1d, ax, vy);               // ey += x face (e1)
+        if (c3 && irm) tfsf_add(p, 0, 4 + (int)c3 - 1, 1, f1d, ax, vy);     // ey += z face (e2)
+        if (c4 && xface) tfsf_add(p, 0, xid, 1, f1d, ax, vz);               // ez += x face (e2)
+        if (c5 && irm) tfsf_add(p, 0, 2 + (int)c5 - 1, 0, f1d, ax, vz);     // ez += y face (e1)
+    } else {
+        if (c0 && irm) tfsf_add(p, 1, 2 + (int)c0 - 1, 1, f1d, ax, vx);     // hx += y face (h2)
+        if (c1 && irm) tfsf_add(p, 1, 4 + (int)c1 - 1, 0, f1d, ax, vx);     //    then z face (h1)
+        if (c2 && xface) tfsf_add(p, 1, xid, 0, f1d, ax, vy);               // hy += x face (h1)
+        if (c3 && ir) tfsf_add(p, 1, 4 + (int)c3 - 1, 1, f1d, ax, vy);      //    then z face (h2)
+        if (c4 && xface) tfsf_add(p, 1, xid, 1, f1d, ax, vz);               // hz += x face (h2)
+        if (c5 && ir) tfsf_add(p, 1, 2 + (int)c5 - 1, 0, f1d, ax, vz);      //    then y face (h1)
     }
-    bool any = false;
-    if (fa >= 0 && ((p.tfaces >> fa) & 1)) { tfsf_add(p, 1, fa, sa, e1, ax, v); any = true; }
-    if (fb >= 0 && ((p.tfaces >> fb) & 1)) { tfsf_add(p, 1, fb, sb, e1, ax, v); any = true; }
-    return any;
 }
 
-template <int TY, int NS, bool BATCH>
+// EXT: 0 = neither the Drude box nor the TFSF faces are compiled in, 1 = the
+// Drude box, 2 = both.  A plan launches the smallest variant its grid needs:
+// code a step does not use still costs it registers and instruction-cache
+// space (the plain step ran 3.5 % slower with both compiled in).
+template <int TY, int NS, bool BATCH, int EXT>
 __global__ void __launch_bounds__(Layout<TY, NS>::THREADS, Layout<TY, NS>::MINB)
 k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk, const __grid_constant__ BatchDesc bd) {
     using L = Layout<TY, NS>;
@@ -491,7 +528,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         const bool yh_b = ((p.faces >> 3) & 1) && p.P[1] > 0 && j0 + TY - 1 >= p.ny - p.P[1] && j0 <= p.ny - 1;
         const bool ytile = p.xypsi && (ye_f || ye_b || yh_f || yh_b) && !((ye_f || yh_f) && (ye_b || yh_b));
         // the item's E region (planes i_start..x1-1, rows j0-1.., columns k0-1..) meets the Drude box
-        const bool dtile = p.drude && i_start < p.dbox[0] + p.dbox[3] && x1 > p.dbox[0] &&
+        const bool dtile = EXT >= 1 && p.drude && i_start < p.dbox[0] + p.dbox[3] && x1 > p.dbox[0] &&
                            j0 - 1 < p.dbox[1] + p.dbox[4] && j0 + TY > p.dbox[1] &&
                            k0 - 1 < p.dbox[2] + p.dbox[5] && k0 + TZ > p.dbox[2];
 
@@ -599,13 +636,20 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             if (nplanes > 1) issue_psi(0);
         }
         const int nls = s_nls;
-        // the item's E/H region meets a TFSF face (E faces at p1-1 and p2, H faces at p1 and p2)
-        // and is not strictly inside the box
-        const bool ttile = p.tfsf && i_start <= p.tp2[0] && x1 - 1 >= p.tp1[0] - 1 && j0 - 1 <= p.tp2[1] &&
-                           j0 + TY - 1 >= p.tp1[1] - 1 && k0 - 1 <= p.tp2[2] && k0 + TZ - 1 >= p.tp1[2] - 1 &&
-                           !(i_start > p.tp1[0] && x1 - 1 < p.tp2[0] && j0 - 1 > p.tp1[1] && j0 + TY - 1 < p.tp2[1] &&
-                             k0 - 1 > p.tp1[2] && k0 + TZ - 1 < p.tp2[2]);
-        const bool tile_plain = y_plain && nls == 0 && !dtile && !ttile;
+        // TFSF faces in this item (E faces at p1-1 and p2, H faces at p1 and p2): the tile's
+        // rows and columns meet the box's y/z extent [p1-1, p2], and then either hold a y or
+        // z face row/column (all planes of the box's x extent) or, per plane, an x face plane
+        const bool t_rows = EXT >= 2 && p.tfsf && j0 - 1 <= p.tp2[1] && j0 + TY - 1 >= p.tp1[1] - 1 &&
+                            k0 - 1 <= p.tp2[2] && k0 + TZ - 1 >= p.tp1[2] - 1;
+        auto holds = [](int64_t lo, int64_t hi, int64_t v) { return v >= lo && v <= hi; };
+        const bool t_yz = t_rows && i_start <= p.tp2[0] && x1 - 1 >= p.tp1[0] - 1 &&
+                          (holds(j0 - 1, j0 + TY - 1, p.tp1[1] - 1) || holds(j0 - 1, j0 + TY - 1, p.tp1[1]) ||
+                           holds(j0 - 1, j0 + TY - 1, p.tp2[1]) || holds(k0 - 1, k0 + TZ - 1, p.tp1[2] - 1) ||
+                           holds(k0 - 1, k0 + TZ - 1, p.tp1[2]) || holds(k0 - 1, k0 + TZ - 1, p.tp2[2]));
+        // TFSF face codes of the pair (E, H), zero outside the box's faces
+        const uint32_t tcode_e = t_rows ? tfsf_lane_codes(p, 0, jj, kk, in0, in1) : 0u;
+        const uint32_t tcode_h = t_rows && h_active ? tfsf_lane_codes(p, 1, jj, kk, in0, in1) : 0u;
+        const bool tile_plain = y_plain && nls == 0 && !dtile;
 
         float2 prev_ey = make_float2(0.f, 0.f), prev_ez = make_float2(0.f, 0.f);
         float2 oex = prev_ey, oey = prev_ey, oez = prev_ey;  // own E_new pair
@@ -638,8 +682,11 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             // plane-uniform CPML (x) and masks
             const int sxe = slab_e(i, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1)), sxh = slab_h(i, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1));
             const bool i_lt = i < p.nx - 1, i_gt = i > 0;
-            const bool e_plain = tile_plain && i_lt && sxe < 0;
-            const bool h_plain = tile_plain && i_gt && sxh < 0;
+            // plane-uniform: TFSF corrections on this plane
+            const bool ttile = t_rows && ((t_yz && i >= p.tp1[0] - 1 && i <= p.tp2[0]) ||
+                                          i == p.tp1[0] - 1 || i == p.tp1[0] || i == p.tp2[0]);
+            const bool e_plain = tile_plain && i_lt && sxe < 0 && !ttile;
+            const bool h_plain = tile_plain && i_gt && sxh < 0 && !ttile;
             // where this plane's x/y psi come from (the choice of issue_psi)
             const bool xm = p.xypsi && (sxe >= 0 || sxh >= 0);
             const bool ym = !xm && ytile;
@@ -731,17 +778,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             }
                         }
                     }
-                    if (ttile) {  // TFSF: E += 0.5 (c * H1d), after the CPML terms, before the sources
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {
-                            if (!(e ? in1 : in0)) continue;
-                            float v = get(ex, e);
-                            if (tfsf_e_comp(p, 0, i, jj, kk + e, v)) set(ex, e, v);
-                            v = get(ey, e);
-                            if (tfsf_e_comp(p, 1, i, jj, kk + e, v)) set(ey, e, v);
-                            v = get(ez, e);
-                            if (tfsf_e_comp(p, 2, i, jj, kk + e, v)) set(ez, e, v);
-                        }
+                    if (ttile && tcode_e) {  // TFSF: E += 0.5 (c * H1d), after the CPML terms, before the sources
+                        tfsf_apply(p, 0, tcode_e & 0xfff, i, jj, kk, ex.x, ey.x, ez.x);
+                        tfsf_apply(p, 0, tcode_e >> 12, i, jj, kk + 1, ex.y, ey.y, ez.y);
                     }
                     const uint32_t ij_here = ((uint32_t)i << 16) | (uint32_t)jj;
                     for (int s = 0; s < nls; s++) {  // soft sources, list order
@@ -831,17 +870,9 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             }
                         }
                     }
-                    if (ttile) {  // TFSF: H += 0.5 (c * E1d), after the CPML terms
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {
-                            if (!(e ? in1 : in0)) continue;
-                            float v = get(hx, e);
-                            if (tfsf_h_comp(p, 0, i, jj, kk + e, v)) set(hx, e, v);
-                            v = get(hy, e);
-                            if (tfsf_h_comp(p, 1, i, jj, kk + e, v)) set(hy, e, v);
-                            v = get(hz, e);
-                            if (tfsf_h_comp(p, 2, i, jj, kk + e, v)) set(hz, e, v);
-                        }
+                    if (ttile && tcode_h) {  // TFSF: H += 0.5 (c * E1d), after the CPML terms
+                        tfsf_apply(p, 1, tcode_h & 0xfff, i, jj, kk, hx.x, hy.x, hz.x);
+                        tfsf_apply(p, 1, tcode_h >> 12, i, jj, kk + 1, hx.y, hy.y, hz.y);
                     }
                     const int64_t gi = i * p.sx + jj * p.sy + kk;
                     if (in1) {
@@ -1145,13 +1176,16 @@ typedef void (*FusedKernel)(const TMaps, const Params, const BatchDesc);
 
 struct KernelEntry {
     int ty, ns, threads, stage, enew, psiring;
-    FusedKernel fn, fn_batch;
+    FusedKernel fn[3];        // single grid, EXT = 0, 1, 2
+    FusedKernel fn_batch[2];  // batched, EXT = 0, 1 (batched plans take no plane wave)
 };
 
 template <int TY, int NS>
 static KernelEntry entry() {
     return KernelEntry{TY, NS, Layout<TY, NS>::THREADS, Layout<TY, NS>::STAGE, Layout<TY, NS>::ENEW,
-                       Layout<TY, NS>::PSIRING, k_yee_fused<TY, NS, false>, k_yee_fused<TY, NS, true>};
+                       Layout<TY, NS>::PSIRING,
+                       {k_yee_fused<TY, NS, false, 0>, k_yee_fused<TY, NS, false, 1>, k_yee_fused<TY, NS, false, 2>},
+                       {k_yee_fused<TY, NS, true, 0>, k_yee_fused<TY, NS, true, 1>}};
 }
 
 // Tile heights and pipeline depths compiled in (the autotuner picks among them).
@@ -1166,6 +1200,7 @@ static const KernelEntry *find_kernel(int ty, int ns) {
 struct fdtd_yee_plan {
     Grid g;
     const KernelEntry *k;
+    FusedKernel fn;  // the kernel variant launched (with or without the Drude / TFSF code)
     int smem;
     int x_chunk;
     int64_t nitems;
@@ -1424,18 +1459,19 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     }
     const int tab_bytes = 6 * 2 * (p.P[0] + p.P[1] + p.P[2]) * 4;
     pl->smem = ns * p.stage_bytes + ke->enew + 128 /*barriers*/ + ke->psiring + tab_bytes + 128 /*align slack*/;
+    pl->fn = ke->fn[p.tfsf ? 2 : (p.drude ? 1 : 0)];
     int dev = 0, nsm = 0, occ = 0, optin = 0;
     cudaFuncAttributes fa;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)ke->fn);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)pl->fn);
     if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
     const int max_dyn = optin - (int)fa.sharedSizeBytes;
     if (pl->smem > max_dyn) { delete pl; return FDTD_ERR_UNSUPPORTED; }
     // the attribute is an upper bound; every plan of this kernel fits under it
-    e = cudaFuncSetAttribute((const void *)ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+    e = cudaFuncSetAttribute((const void *)pl->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)ke->fn, ke->threads, pl->smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)pl->fn, ke->threads, pl->smem);
     if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
     if (occ < 1) { delete pl; return FDTD_ERR_UNSUPPORTED; }
     if (tile && tile->ctas_per_sm > 0) occ = std::min(occ, (int)tile->ctas_per_sm);
@@ -1468,7 +1504,7 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
         }
         p.t = t0 + n;
         BatchDesc bd{};
-        pl->k->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
+        pl->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
         if (p.zfix) {
             for (int q = 0; q < 6; q++) p.in[q] = pl->f[in][q];
             const int64_t ne = zband_e_cells(p), nh = zband_h_cells(p);
@@ -1520,6 +1556,7 @@ int fdtd_yee_plan_destroy(fdtd_yee_plan *pl) {
 struct fdtd_batch_plan {
     int32_t nsims;
     const KernelEntry *k;
+    FusedKernel fn;  // batched variant launched (with the Drude code when a grid has a Drude box)
     int smem;
     int nblocks;
     int cur;
@@ -1569,6 +1606,7 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     int64_t *boff_e = off.data() + (nsims + 1), *boff_h = off.data() + 2 * (nsims + 1);
     const KernelEntry *ke = nullptr;
     int stage_bytes = 0, tab_bytes = 0;
+    bool any_drude = false;
     // grids with the longest items (x planes per chunk, then tile rows) come first
     std::vector<int32_t> order((size_t)nsims);
     for (int32_t s = 0; s < nsims; s++) order[s] = s;
@@ -1587,6 +1625,7 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
         if (st != FDTD_OK) return st;
         ke = pl->k;
         stage_bytes = std::max(stage_bytes, pl->base.stage_bytes);
+        any_drude = any_drude || pl->base.drude;
         tab_bytes = std::max(tab_bytes, 6 * 2 * (pl->base.P[0] + pl->base.P[1] + pl->base.P[2]) * 4);
         for (int b = 0; b < 2; b++) {
             Params p = pl->base;
@@ -1634,14 +1673,15 @@ int fdtd_batch_plan_create(fdtd_batch_plan **out, int32_t nsims, const fdtd_grid
     cudaFuncAttributes fa;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)ke->fn_batch);
+    bp->fn = ke->fn_batch[any_drude ? 1 : 0];
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)bp->fn);
     if (e != cudaSuccess) { set_cuda_error(e); delete bp; return FDTD_ERR_CUDA; }
     const int max_dyn = optin - (int)fa.sharedSizeBytes;
     if (bp->smem > max_dyn) { delete bp; return FDTD_ERR_UNSUPPORTED; }
-    e = cudaFuncSetAttribute((const void *)ke->fn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+    e = cudaFuncSetAttribute((const void *)bp->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)ke->fn_batch, ke->threads, bp->smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)bp->fn, ke->threads, bp->smem);
     if (e != cudaSuccess) { set_cuda_error(e); delete bp; return FDTD_ERR_CUDA; }
     if (occ < 1) { delete bp; return FDTD_ERR_UNSUPPORTED; }
     if (tile && tile->ctas_per_sm > 0) occ = std::min(occ, (int)tile->ctas_per_sm);
@@ -1666,7 +1706,7 @@ int fdtd_batch_plan_run(fdtd_batch_plan *bp, int64_t t0, int64_t nsteps, void *s
         bd.item_off = bp->d_off;
         bd.stage_bytes = bp->stage_bytes;
         bd.queue = bp->d_queue;
-        bp->k->fn_batch<<<bp->nblocks, bp->k->threads, bp->smem, st>>>(dummy_maps, dummy, bd);
+        bp->fn<<<bp->nblocks, bp->k->threads, bp->smem, st>>>(dummy_maps, dummy, bd);
         if (bp->band_e > 0 || bp->band_h > 0) {
             BandBatch d{bp->nsims, bp->cur, t0 + n, bp->d_params, bp->d_band_e};
             if (bp->band_e > 0) k_zband_e_batch<<<(unsigned)((bp->band_e + 127) / 128), 128, 0, st>>>(d);

@@ -12,11 +12,12 @@ from .api import update_e, update_h, update_pbc_e, update_pbc_h
 from .cpml import CpmlLayer, cpml_tables
 from .drude import DrudeAde, drude_coefficients
 from .tfsf import Tfsf
+from .output import Output
 from .solver import YeeSolver
 from .sources import PointSources, gaussian_sine
 
 __all__ = ["update_e", "update_h", "update_pbc_e", "update_pbc_h", "CpmlLayer", "cpml_tables", "DrudeAde",
-           "drude_coefficients", "Tfsf",
+           "drude_coefficients", "Tfsf", "Output",
            "YeeSolver", "BatchSolver", "YeeAdjoint", "fdtd_run", "PointSources", "gaussian_sine", "build"]
 
 

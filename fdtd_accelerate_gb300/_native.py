@@ -52,6 +52,10 @@ class Tfsf(C.Structure):
                 ("e1d", P), ("h1d", P), ("abc", P), ("amp", P), ("namp", I64)]
 
 
+class Output(C.Structure):
+    _fields_ = [("form", I32), ("p1", I64 * 3), ("p2", I64 * 3), ("step", I64 * 3)]
+
+
 class YeeState(C.Structure):
     _fields_ = [("f", (P * 6) * 2), ("psi_e", (P * 6) * 2), ("psi_h", P * 6), ("ce", P * 3), ("drude", P),
                 ("tfsf", P)]
@@ -88,6 +92,7 @@ _SIGS = {
     "fdtd_add_sources_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Sources), I64, P, P, P, P]),
     "fdtd_drude_update_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Drude)] + [P] * 6 + [P]),
     "fdtd_tfsf_update_e_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Tfsf), I64, P, P, P, P]),
+    "fdtd_output_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Output), P, P, I64, P]),
     "fdtd_tfsf_update_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Tfsf), P, P, P, P]),
     "fdtd_step_unfused_f32": (C.c_int, [C.POINTER(Grid), P, P, P, C.POINTER(Cpml), C.POINTER(Psi),
                                         C.POINTER(Sources), I64, P]),

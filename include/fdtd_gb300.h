@@ -31,6 +31,8 @@
  *                          strides travel in fdtd_drude / fdtd_grid
  *   fdtd_tfsf_update_{e,h}_f32  kuFDTD/v0.2.0/dim3/tfsf.py Tfsf.updateE(tstep) /
  *                          updateH() (Fdtd1d + TfsfFace + TfsfIncNormal)
+ *   fdtd_output_f32        kuFDTD/v0.2.0/dim3/output.py Output.get_data()
+ *                          (centred fields, Poynting vector, square/sum/sqrt)
  *   fdtd_step_unfused_f32  one time step in the order of
  *                          fdtd3d_201_..._100000tstep.cu:718-742
  *   fdtd_yee_plan_*        the same step, fused into one pass per step
@@ -135,6 +137,16 @@ typedef struct {
     int64_t namp;
 } fdtd_tfsf;
 
+/* Field output on the region p1..p2 (inclusive) sampled every step cells
+ * (kuFDTD Output, kuFDTD/v0.2.0/dim3/output.py:14-212): the fields averaged
+ * to the cell centres, then per form = family*16 + kind*4 + comp with family
+ * 0 E, 1 H, 2 Poynting S and kind 0 |v|, 1 |v|^2, 2 v[comp], 3 v[comp]^2
+ * (dataforms 'e', 'e2', 'ex', 'ex2', 'h', ..., 's', 's2', 'sx', 'sx2'). */
+typedef struct {
+    int32_t form;
+    int64_t p1[3], p2[3], step[3];
+} fdtd_output;
+
 const char *fdtd_status_string(int status);
 int fdtd_last_cuda_error(void);
 
@@ -169,6 +181,11 @@ int fdtd_add_sources_f32(const fdtd_grid *g, const fdtd_sources *src, int64_t t,
 int fdtd_tfsf_update_e_f32(const fdtd_grid *g, const fdtd_tfsf *t, int64_t tstep, float *ex, float *ey, float *ez,
                            void *stream);
 int fdtd_tfsf_update_h_f32(const fdtd_grid *g, const fdtd_tfsf *t, float *hx, float *hy, float *hz, void *stream);
+/* Output of o into out (C order, n[a] = (p2[a]-p1[a])/step[a] + 1 per axis,
+ * out_len >= their product); the region needs p2 + 1 <= n - 1 on every axis
+ * (the averages read the next node). */
+int fdtd_output_f32(const fdtd_grid *g, const fdtd_output *o, const float *const f[6], float *out, int64_t out_len,
+                    void *stream);
 /* Drude ADE on the box of d (in place on E and d->j); call it between
  * fdtd_update_e_f32 and fdtd_cpml_e_f32. */
 int fdtd_drude_update_e_f32(const fdtd_grid *g, const fdtd_drude *d, float *ex, float *ey, float *ez,

@@ -15,7 +15,7 @@ from . import build as _build
 __all__ = ["update_e", "update_h", "pbc_e", "pbc_h", "cpml_e", "cpml_h",
            "add_points", "symp_h", "symp_e", "cpml_tables", "pulse",
            "OracleSim", "lib", "symp_h_scalar", "symp_cpml_e", "symp_cpml_h", "symp_stage_tables",
-           "drude_e", "drude_coefficients", "TfsfNormal"]
+           "drude_e", "drude_coefficients", "TfsfNormal", "output_data"]
 
 _LIBS = {}
 
@@ -310,6 +310,51 @@ class TfsfNormal:
             e1, e2 = self._inc(f, 1)
             fields[names[2]][idx[2]] += np.float32(0.5) * e1
             fields[names[3]][idx[3]] += np.float32(0.5) * e2
+
+
+def output_data(fields, dataform, pt1, pt2, step=(1, 1, 1)):
+    """kuFDTD Output.get_data() restated in NumPy (kuFDTD/v0.2.0/dim3/output.py:
+    set_space 33-46, centred data 167-178, square/sum/sqrt 181-195, Poynting
+    198-211); fields: dict ex..hz of float32 (nx, ny, nz) arrays."""
+    d = dataform.lower()
+    n = fields["ex"].shape
+    p1 = [1 if v is None else int(v) for v in pt1]
+    p2 = [n[a] - 2 if v is None else int(v) for a, v in enumerate(pt2)]
+    (i1, j1, k1), (i2, j2, k2) = p1, p2
+    sl = (slice(i1, i2 + 1), slice(j1, j2 + 1), slice(k1, k2 + 1))
+    up = lambda a: tuple(slice(x.start + 1, x.stop + 1) if q == a else x for q, x in enumerate(sl))
+    up2 = lambda a, b: tuple(slice(x.start + 1, x.stop + 1) if q in (a, b) else x for q, x in enumerate(sl))
+    st = tuple(slice(None, None, int(v)) for v in step)
+    def ce(q):
+        E = fields["e" + "xyz"[q]]
+        return (0.5 * (E[sl] + E[up(q)]))[st]
+    def ch(q):
+        H = fields["h" + "xyz"[q]]
+        a, b = [(1, 2), (0, 2), (0, 1)][q]
+        return (0.25 * (H[sl] + H[up(a)] + H[up(b)] + H[up2(a, b)]))[st]
+    if d[0] in "eh":
+        cen = ce if d[0] == "e" else ch
+        if len(d) >= 2 and d[1] in "xyz":
+            v = cen("xyz".index(d[1]))
+            out = v ** 2 if d.endswith("2") and len(d) == 3 else v
+        else:
+            tot = 0
+            for q in range(3):
+                tot = tot + cen(q) ** 2
+            out = np.sqrt(tot) if len(d) == 1 else tot
+    else:
+        ex, ey, ez, hx, hy, hz = ce(0), ce(1), ce(2), ch(0), ch(1), ch(2)
+        S = [ey * hz - ez * hy, ez * hx - ex * hz, ex * hy - ey * hx]
+        if len(d) >= 2 and d[1] in "xyz":
+            v = S["xyz".index(d[1])]
+            out = v ** 2 if len(d) == 3 else v
+        else:
+            tot = 0
+            for q in range(3):
+                tot = tot + S[q] ** 2
+            out = np.sqrt(tot) if len(d) == 1 else tot
+    ds = tuple(0 if p2[a] == p1[a] else slice(None) for a in range(3))
+    return out[ds]
 
 
 class OracleSim:

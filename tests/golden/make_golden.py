@@ -370,8 +370,68 @@ def tfsf_kufdtd(rng):
     return out
 
 
+def output_kufdtd(rng):
+    """kuFDTD Output.get_data() (kuFDTD/v0.2.0/dim3/output.py, executed in place
+    with the same stub module as the TFSF case) for every dataform on a region
+    with a spatial step, and on a plane (pt1 == pt2 on one axis)."""
+    import types
+    common = types.ModuleType("kufdtd.common")
+
+    class SC:
+        sqrt = staticmethod(np.sqrt)
+    common.sc = SC
+
+    def list_replace(lst, index, content):       # kuFDTD/v0.2.0/common.py:32-39
+        out = list(lst)
+        out[index] = content
+        return out
+    common.list_replace = list_replace
+    pkg = types.ModuleType("kufdtd")
+    pkg.common = common
+    saved = {k: sys.modules.get(k) for k in ("kufdtd", "kufdtd.common")}
+    sys.modules["kufdtd"], sys.modules["kufdtd.common"] = pkg, common
+    path = os.path.join(build_ref.REF, "kuFDTD/v0.2.0/dim3/output.py")
+    src = open(path).read().replace("from kufdtd.common import *", "from kufdtd.common import sc, list_replace")
+    src = src.replace("[s.data_slice]", "[tuple(s.data_slice)]").replace("[ e_sl[0] ]", "[ tuple(e_sl[0]) ]")
+    src = src.replace("[ e_sl[1] ]", "[ tuple(e_sl[1]) ]")
+    for q in range(4):
+        src = src.replace("[ h_sl[%d] ]" % q, "[ tuple(h_sl[%d]) ]" % q)
+    ns = {"xrange": range}
+    exec(compile(src, path, "exec"), ns)
+    for k, v in saved.items():
+        if v is None:
+            sys.modules.pop(k, None)
+        else:
+            sys.modules[k] = v
+
+    class Space:
+        pass
+    shape = (12, 11, 10)
+    S = Space()
+    S.Nx, S.Ny, S.Nz = shape
+    f = {k: rng.standard_normal(shape).astype(F32) for k in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+    for k, v in f.items():
+        setattr(S, k, v)
+    out = {"in_" + k.lower(): v for k, v in f.items()}
+    n = 0
+    forms = ns["Output"]("e", (1, 1, 1), (2, 2, 2)).__class__   # the class, for the form list below
+    for dform in ("e", "e2", "ex", "ey", "ez", "ex2", "ey2", "ez2", "h", "h2", "hx", "hy", "hz", "hx2", "hy2",
+                  "hz2", "s", "s2", "sx", "sy", "sz", "sx2", "sy2", "sz2"):
+        for pt1, pt2, step in (((2, 1, None), (9, None, 8), (2, 1, 3)), ((None, 4, 2), (None, 4, 8), (1, 1, 2))):
+            o = forms(dform, pt1, pt2, step)
+            o.set_space(S)
+            tag = "c%d_" % n
+            out[tag + "form"] = np.array(dform)
+            out[tag + "pts"] = np.array([[-1 if v is None else v for v in pt1], [-1 if v is None else v for v in pt2],
+                                        list(step)])
+            out[tag + "out"] = np.asarray(o.get_data(), dtype=F32)
+            n += 1
+    out["ncases"] = np.array(n)
+    return out
+
+
 CASES = (("yee_numpy", yee_numpy), ("kemp_core", kemp_core), ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c),
-         ("drude_kufdtd", drude_kufdtd), ("tfsf_kufdtd", tfsf_kufdtd))
+         ("drude_kufdtd", drude_kufdtd), ("tfsf_kufdtd", tfsf_kufdtd), ("output_kufdtd", output_kufdtd))
 
 
 def main():

@@ -123,3 +123,18 @@ def test_tfsf_validation_before_cuda(lib):
     assert lib.fdtd_tfsf_update_e_f32(C.byref(g), C.byref(t), 8, *fake, None) == N.FDTD_ERR_ARG  # past the table
     t.axis = 3
     assert lib.fdtd_tfsf_update_h_f32(C.byref(g), C.byref(t), *fake, None) == N.FDTD_ERR_ARG
+
+
+def test_output_validation_before_cuda(lib):
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(10, 10, 10, 100, 10)
+    f = (C.c_void_p * 6)(*[256 * (q + 1) for q in range(6)])
+    o = N.Output(0)
+    for a in range(3):
+        o.p1[a], o.p2[a], o.step[a] = 1, 8, 1
+    out = C.c_void_p(4096)
+    assert lib.fdtd_output_f32(C.byref(g), C.byref(o), f, out, 10, None) == N.FDTD_ERR_CAPACITY  # 512 cells
+    o.p2[1] = 9                                                # 9 + 1 > n - 1
+    assert lib.fdtd_output_f32(C.byref(g), C.byref(o), f, out, 1000, None) == N.FDTD_ERR_SHAPE
+    o.p2[1], o.form = 8, 3 * 16                                # family 3 does not exist
+    assert lib.fdtd_output_f32(C.byref(g), C.byref(o), f, out, 1000, None) == N.FDTD_ERR_ARG

@@ -207,3 +207,22 @@ def test_oracle_tfsf_matches_kufdtd_bit_exact(golden_dir):
             np.testing.assert_array_equal(f[k], g[t + "out_" + k], err_msg="case %d %s" % (n, k))
         np.testing.assert_array_equal(ref.E, g[t + "e1d"])
         np.testing.assert_array_equal(ref.H, g[t + "h1d"])
+
+
+def _output_case(g, n):
+    t = "c%d_" % n
+    pts = g[t + "pts"]
+    pt1 = tuple(None if v < 0 else int(v) for v in pts[0])
+    pt2 = tuple(None if v < 0 else int(v) for v in pts[1])
+    return str(g[t + "form"]), pt1, pt2, tuple(int(v) for v in pts[2]), g[t + "out"]
+
+
+def test_oracle_output_matches_kufdtd_bit_exact(golden_dir):
+    """Reference kuFDTD Output.get_data() for all 24 dataforms on a stepped region
+    and on a plane (tests/golden/output_kufdtd.npz)."""
+    g = np.load(os.path.join(golden_dir, "output_kufdtd.npz"))
+    fields = {k: g["in_" + k] for k in NAMES}
+    for n in range(int(g["ncases"])):
+        form, pt1, pt2, step, ref = _output_case(g, n)
+        np.testing.assert_array_equal(oracle.output_data(fields, form, pt1, pt2, step), ref,
+                                      err_msg="case %d %s" % (n, form))

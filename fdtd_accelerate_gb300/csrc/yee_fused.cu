@@ -49,7 +49,8 @@ constexpr int al128(int b) { return (b + 127) / 128 * 128; }
 
 // Shared-memory layout of one CTA for tile height TY and NS pipeline stages.
 // Warps 0..TY-1 own rows j0..j0+TY-1 (E and H); warp TY recomputes E_new on
-// the halo row j0-1; warp TY+1 recomputes E_new on the halo column k0-1.
+// the halo row j0-1; warp TY+1 recomputes E_new on the halo column k0-1;
+// lane 0 of warp TY+2 is the producer (mbarrier waits, TMA issue).
 template <int TY, int NS>
 struct Layout {
     static constexpr int HR = TY + 2, ER = TY + 1;
@@ -57,16 +58,20 @@ struct Layout {
     static constexpr int HBOXB = al128(HBOX * 4), EBOXB = al128(EBOX * 4);
     static constexpr int STAGE = 3 * HBOXB + 6 * EBOXB;  // H(3), E(3), CE(3)
     static constexpr uint32_t TX = 3 * HBOX * 4 + 6 * EBOX * 4;
+    // a stage completes on two barriers: H (needed one plane early, as H(i+1))
+    // and E + CE (needed on its own plane only)
+    static constexpr uint32_t TX_H = 3 * HBOX * 4, TX_E = 6 * EBOX * 4;
     static constexpr int NR = TY + 1;
     static constexpr int ENEWC = NR * NCW;  // floats per component
-    static constexpr int THREADS = (TY + 2) * 32;
+    // TY row warps, the halo-row warp, the halo-column warp, the producer warp
+    static constexpr int THREADS = (TY + 3) * 32;
     static constexpr int ENEW = al128(3 * ENEWC * 4);
     // psi ring: 2 slots x 4 boxes (E psi 1, 2 and H psi 1, 2 of one axis)
     static constexpr int PSIRING = 2 * 4 * EBOXB;
     static constexpr uint32_t PSI_TX = EBOX * 4;
     static constexpr int SMEM = NS * STAGE + ENEW + 128 /*barriers*/ + PSIRING + 128 /*align slack*/;
     // CTAs per SM the register budget is sized for (shared memory may allow fewer)
-    static constexpr int MINB = TY == 4 ? 4 : (TY == 8 ? 2 : 1);
+    static constexpr int MINB = TY == 4 ? 3 : (TY == 8 ? 2 : 1);
 };
 
 struct TMaps {
@@ -368,6 +373,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     // iteration holds two planes: fewer than 3 stages would wait on a plane
     // that is only issued after the wait.
     static_assert(NS >= 3, "the fused pipeline needs at least 3 stages");
+    static_assert((2 * NS + 2) * 8 <= 128, "the mbarriers live in 128 bytes");
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -396,7 +402,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     // column: lane r <= TY computes the pair at k0-2, k0-1 of row r (only the
     // k0-1 value is used).  H phase: warps 0..TY-1, own pairs.
     const bool col_warp = warp == TY + 1;
-    const bool e_active = !col_warp || lane <= TY;
+    // producer: lane 0 of warp TY+2 waits on the mbarriers and issues the TMA
+    // copies, so that no stencil warp carries that work on its critical path
+    const bool producer = tid == (TY + 2) * 32;
+    const bool e_active = warp <= TY || (col_warp && lane <= TY);
     const bool h_active = warp < TY;
     const int er = warp < TY ? warp + 1 : (warp == TY ? 0 : lane);
     const int eko = col_warp ? -2 : 2 * lane;  // pair start relative to k0
@@ -432,7 +441,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     };
 
     if (tid == 0) {
-        for (int s = 0; s < NS + 2; s++) mbar_init(&bars[s], 1);  // stages, then the 2 psi slots
+        // stage H barriers, stage E+CE barriers, then the 2 psi slots
+        for (int s = 0; s < 2 * NS + 2; s++) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         if (!BATCH) {
@@ -549,26 +559,28 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         auto issue = [&](int64_t q) {
             const int64_t plane = i_start + q;
             const int st = (int)((g0 + q) % NS);
-            uint64_t *bar = &bars[st];
+            uint64_t *bar = &bars[st], *bare = &bars[NS + st];
             issued_hi = q;
             if (plane >= p.nx) {
                 // Past the last plane: H(p.nx) only feeds E components that are
-                // never updated at i = p.nx-1; complete the phase without a copy.
+                // never updated at i = p.nx-1; complete the phases without a copy.
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bare)) : "memory");
                 return;
             }
-            mbar_arrive_expect_tx(bar, L::TX);
+            mbar_arrive_expect_tx(bar, L::TX_H);
+            mbar_arrive_expect_tx(bare, L::TX_E);
             const int kc = (int)(k0 - 4), jc = (int)(j0 - 1), xc = (int)plane;
             for (int c = 0; c < 3; c++) tma_load_3d(sH(st, c), &maps.h[c], bar, kc, jc, xc);
-            for (int c = 0; c < 3; c++) tma_load_3d(sE(st, c), &maps.e[c], bar, kc, jc, xc);
-            for (int c = 0; c < 3; c++) tma_load_3d(sC(st, c), &maps.ce[c], bar, kc, jc, xc);
+            for (int c = 0; c < 3; c++) tma_load_3d(sE(st, c), &maps.e[c], bare, kc, jc, xc);
+            for (int c = 0; c < 3; c++) tma_load_3d(sC(st, c), &maps.ce[c], bare, kc, jc, xc);
         };
         // psi boxes of plane q into ring slot (gp0+q)&1: the x slab's on x-slab
         // planes, else the y slab's in y-slab tiles; otherwise a bare arrive
         auto issue_psi = [&](int64_t q) {
             const uint32_t Gp = gp0 + (uint32_t)q;
             const int sl = (int)(Gp & 1);
-            uint64_t *bar = &bars[NS + sl];
+            uint64_t *bar = &bars[2 * NS + sl];
             psi_hi = q;
             const int64_t plane = i_start + q;
             const int xse = plane < p.nx ? slab_e(plane, p.P[0], p.nx, (p.faces & 1), ((p.faces >> 1) & 1)) : -1;
@@ -631,7 +643,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             s_nls = n;
         }
         __syncthreads();  // previous item finished by every thread; source list ready
-        if (tid == 0) {
+        if (producer) {
             for (int64_t q = 0; q < NS && q < nplanes; q++) issue(q);
             if (nplanes > 1) issue_psi(0);
         }
@@ -660,21 +672,23 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             const uint32_t par = (G / NS) & 1, par1 = ((G + 1) / NS) & 1;
             const uint32_t Gp = gp0 + (uint32_t)q;
             const int psl = (int)(Gp & 1);
-            // One thread waits for the copies; the barrier then releases the CTA
-            // (the mbarrier acquire by tid 0 plus bar.sync order the TMA writes
-            // before every thread's reads).
-            if (tid == 0 &&
+            // The producer waits for the copies; the barrier then releases the CTA
+            // (its mbarrier acquire plus bar.sync order the TMA writes before
+            // every thread's reads).  Plane q+1 is needed for its H only:
+            // its E and CE have one more iteration to arrive.
+            if (producer &&
                 (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status) ||
-                 !mbar_wait_bounded(&bars[NS + psl], (Gp >> 1) & 1, p.status)))
+                 !mbar_wait_bounded(&bars[NS + st], par, p.status) ||
+                 !mbar_wait_bounded(&bars[2 * NS + psl], (Gp >> 1) & 1, p.status)))
                 s_abort = 1;
-            __syncthreads();  // (A) planes q, q+1 visible; iteration q-1 finished everywhere
+            __syncthreads();  // (A) H of planes q, q+1, E and CE of q visible; iteration q-1 finished everywhere
             if (s_abort) {
                 aborted = true;
                 q_abort = q;
                 i_start_abort = i_start;
                 break;
             }
-            if (tid == 0) {
+            if (producer) {
                 if (q >= 1 && q - 1 + NS < nplanes) issue(q - 1 + NS);  // reuse plane q-1's stage
                 if (q + 2 < nplanes) issue_psi(q + 1);                  // reuse plane q-1's psi slot
             }
@@ -920,7 +934,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
         }
     }
     if (aborted) {
-        if (tid == 0) {
+        if (producer) {
             atomicExch(p.status, FDTD_ERR_TIMEOUT);
             // Let the copies still in flight land before the CTA's shared
             // memory is released (each wait bounded).
@@ -928,10 +942,11 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                 if (i_start_abort + q >= p.nx) continue;
                 const uint32_t G = g0 + (uint32_t)q;
                 mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr);
+                mbar_wait_bounded(&bars[NS + G % NS], (G / NS) & 1, nullptr);
             }
             for (int64_t q = q_abort; q <= psi_hi; q++) {
                 const uint32_t Gp = gp0 + (uint32_t)q;
-                mbar_wait_bounded(&bars[NS + (Gp & 1)], (Gp >> 1) & 1, nullptr);
+                mbar_wait_bounded(&bars[2 * NS + (Gp & 1)], (Gp >> 1) & 1, nullptr);
             }
         }
         __syncthreads();

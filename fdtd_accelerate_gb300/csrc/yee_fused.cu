@@ -988,12 +988,15 @@ __host__ __device__ __forceinline__ int64_t zband_h_cells(const Params &p) {
 // E band cell number t of grid p at step tstep.  All loads come first, then
 // the arithmetic, then the stores: a store could alias a later load as far as
 // the compiler knows, so loads placed after stores would not be overlapped.
-__device__ __forceinline__ void zband_e_cell(const Params &p, int64_t tstep, int64_t t) {
+// E band cells per (i, j) row: the front slab's nodes, then the back slab's
+__device__ __forceinline__ int zband_e_row(const Params &p) {
+    return (((p.faces >> 4) & 1) ? p.P[2] : 0) + (((p.faces >> 5) & 1) ? p.P[2] : 0);
+}
+
+// E band cell kb of row (i, j)
+__device__ __forceinline__ void zband_e_at(const Params &p, int64_t tstep, int64_t i, int64_t j, int kb) {
     const int P = p.P[2];
-    const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
-    const int nf = front ? P : 0, nb = back ? P : 0, nk = nf + nb;
-    const int kb = (int)(t % nk);
-    const int64_t j = (t / nk) % p.ny, i = t / ((int64_t)nk * p.ny);
+    const int nf = ((p.faces >> 4) & 1) ? P : 0;
     const int64_t k = kb < nf ? 1 + kb : p.nz - P - 1 + (kb - nf);
     const int sz = kb < nf ? kb : P + (kb - nf);
     const int64_t c = i * p.sx + j * p.sy + k, qz = (i * p.ny + j) * 2 * P + sz;
@@ -1033,17 +1036,27 @@ __device__ __forceinline__ void zband_e_cell(const Params &p, int64_t tstep, int
     }
 }
 
-// H band cell number t of grid p: H recomputed from the input buffer and the
+// E band cell number t of grid p (rows of zband_e_row cells, z fastest)
+__device__ __forceinline__ void zband_e_cell(const Params &p, int64_t tstep, int64_t t) {
+    const int nk = zband_e_row(p);
+    zband_e_at(p, tstep, t / ((int64_t)nk * p.ny), (t / nk) % p.ny, (int)(t % nk));
+}
+
+// H band cells per (i, j) row: k = 1 .. P+1 (front), then bstart .. nz-1 (back)
+__device__ __forceinline__ int zband_h_row(const Params &p) {
+    const int64_t fend = ((p.faces >> 4) & 1) ? p.P[2] + 1 : 0;
+    return (int)(fend + (p.nz - zband_h_start(p)));
+}
+
+// H band cell kb of row (i, j): H recomputed from the input buffer and the
 // final E, with its curl, then the x, y and z CPML terms (in-kernel order)
-__device__ __forceinline__ void zband_h_cell(const Params &p, int64_t t) {
+__device__ __forceinline__ void zband_h_at(const Params &p, int64_t i, int64_t j, int kb) {
     const int P = p.P[2];
     const int front = (p.faces >> 4) & 1, back = (p.faces >> 5) & 1;
     const int64_t nz = p.nz, ny = p.ny, nx = p.nx;
     const int64_t fend = front ? P + 1 : 0;          // front band: k = 1 .. fend
     const int64_t bstart = zband_h_start(p);         // back band: k = bstart .. nz-1
-    const int nf = (int)fend, nk = nf + (int)(nz - bstart);
-    const int kb = (int)(t % nk);
-    const int64_t j = (t / nk) % ny, i = t / ((int64_t)nk * ny);
+    const int nf = (int)fend;
     const int64_t k = kb < nf ? 1 + kb : bstart + (kb - nf);
     const int64_t c = i * p.sx + j * p.sy + k;
     const int f0 = p.faces & 1, b0 = (p.faces >> 1) & 1, f1 = (p.faces >> 2) & 1, b1 = (p.faces >> 3) & 1;
@@ -1117,14 +1130,26 @@ __device__ __forceinline__ void zband_h_cell(const Params &p, int64_t t) {
     }
 }
 
+// H band cell number t of grid p (rows of zband_h_row cells, z fastest)
+__device__ __forceinline__ void zband_h_cell(const Params &p, int64_t t) {
+    const int nk = zband_h_row(p);
+    zband_h_at(p, t / ((int64_t)nk * p.ny), (t / nk) % p.ny, (int)(t % nk));
+}
+
+// Single-grid band kernels: a warp per (i, j) row (grid (ceil(ny/4), nx),
+// 4 warps a block), lanes over the row's band cells -- no index division.
 __global__ void __launch_bounds__(128) k_zband_e(const __grid_constant__ Params p) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < zband_e_cells(p)) zband_e_cell(p, p.t, t);
+    const int64_t j = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5), i = blockIdx.y;
+    if (j >= p.ny) return;
+    const int nk = zband_e_row(p);
+    for (int kb = threadIdx.x & 31; kb < nk; kb += 32) zband_e_at(p, p.t, i, j, kb);
 }
 
 __global__ void __launch_bounds__(128) k_zband_h(const __grid_constant__ Params p) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < zband_h_cells(p)) zband_h_cell(p, t);
+    const int64_t j = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5), i = blockIdx.y;
+    if (j >= p.ny) return;
+    const int nk = zband_h_row(p);
+    for (int kb = threadIdx.x & 31; kb < nk; kb += 32) zband_h_at(p, i, j, kb);
 }
 
 // Batched band kernels: the band cells of all grids numbered consecutively
@@ -1522,9 +1547,9 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
         pl->fn<<<pl->nblocks, pl->k->threads, pl->smem, st>>>(pl->maps[in], p, bd);
         if (p.zfix) {
             for (int q = 0; q < 6; q++) p.in[q] = pl->f[in][q];
-            const int64_t ne = zband_e_cells(p), nh = zband_h_cells(p);
-            k_zband_e<<<(unsigned)((ne + 127) / 128), 128, 0, st>>>(p);
-            k_zband_h<<<(unsigned)((nh + 127) / 128), 128, 0, st>>>(p);
+            const dim3 rows((unsigned)((p.ny + 3) / 4), (unsigned)p.nx);
+            k_zband_e<<<rows, 128, 0, st>>>(p);
+            k_zband_h<<<rows, 128, 0, st>>>(p);
         }
         FDTD_TRY(check_launch());
         if (pl->has_tfsf) FDTD_TRY(tfsf_launch_1d(&pl->tfsf, n + 1 < nsteps ? 2 : 1, t0 + n + 1, st));

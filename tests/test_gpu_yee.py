@@ -175,6 +175,7 @@ def _oracle_sim(work_shape, ce, npml, faces, sources, init):
     ((30, 44, 72), 14, (16, 8, 1, 3)),        # TMA band kernels, 16-wide boxes at their limit
     ((36, 36, 96), 16, None),                 # TMA band kernels, 32-wide boxes
     ((33, 21, 64), 6, (8, 16, 0, 3)),         # TMA band kernels, ragged y tiles
+    ((24, 20, 192), 5, None),                 # three z tiles, sources in the middle one
 ])
 def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     from fdtd_accelerate_gb300 import configs
@@ -214,6 +215,10 @@ def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
     ((30, 26, 90), 6, 0x33, (4, 8, 0, 4)),    # x and z faces, 4-row tiles
     ((26, 30, 60), 8, 0x3F, (16, 8, 1, 3)),   # one z tile holds both z slabs
     ((30, 26, 90), 7, 0x30, None),            # odd slab width
+    ((20, 18, 192), 8, 0x3F, None),           # three z tiles
+    ((20, 18, 256), 6, 0x20, (8, 16, 0, 3)),  # back face only, four z tiles
+    ((20, 18, 140), 6, 0x3F, (4, 8, 0, 4)),   # short last z tile
+    ((20, 18, 135), 6, 0x3F, None),           # last z tile of 7 cells, all of them in the H band
 ])
 def test_fused_z_slab_faces_and_sources(fdtd, shape, npml, faces, tile):
     """The z-slab CPML (band kernels after the fused kernel) with one or both z

@@ -103,6 +103,8 @@ _SIGS = {
                                    + [C.POINTER(Psi), P]),
     "fdtd_symplectic_cpml_h_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), F32, F32] + [P] * 9
                                    + [C.POINTER(Psi), P]),
+    "fdtd_symplectic_stage_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), I32, F32, F32, C.POINTER(P * 6),
+                                            C.POINTER(P * 3), C.POINTER(Psi), P]),
     "fdtd_yee_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
                                        C.POINTER(Sources), C.POINTER(Tile), P, I32]),
     "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),

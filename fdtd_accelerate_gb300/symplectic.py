@@ -182,6 +182,7 @@ class SymplecticSolver:
         self.max_steps = max_steps
         self.tstep = 1
         self._src = None
+        self._stage_args = None
         self._build_sources(max(max_steps, 1))
 
     def _build_sources(self, nsteps):
@@ -204,6 +205,50 @@ class SymplecticSolver:
             self.fields[k].copy_(torch.as_tensor(v, dtype=torch.float32, device=self.device))
 
     def step(self, n=1):
+        """Advance n steps: one launch per stage (the stage update and its CPML
+        slabs together, fdtd_symplectic_stage_f32) and the sources after each E
+        stage.  Fields of 2^31 or more elements (the stage kernel's offsets are
+        32-bit) take the per-call path of step_unfused."""
+        f = self.f
+        if f[0].numel() >= 2 ** 31:
+            return self.step_unfused(n)
+        if self.src_spec and self.tstep + n > self._src_steps:
+            self._build_sources(self.tstep + n)
+        if self._stage_args is None:
+            self._stage_args = self._make_stage_args()
+        g, fptr, ceptr, chptr, chv = self._stage_args
+        with torch.cuda.device(self.device):
+            stream = stream_of(f[0])
+            for _ in range(n):
+                tn = self.tstep
+                for sn in range(4):
+                    self._fused_stage(0, CL[sn], chptr, chv, stream)
+                    self._fused_stage(1, DL[sn], ceptr, 0.0, stream)
+                    if self.src_spec:
+                        self._src.apply(4 * tn + sn, *f[:3])
+                self._fused_stage(0, CL[4], chptr, chv, stream)
+                self.tstep += 1
+
+    def _make_stage_args(self):
+        g = grid_of(self.f[0])
+        fptr = (C.c_void_p * 6)(*(t.data_ptr() for t in self.f))
+        ceptr = (C.c_void_p * 3)(*(t.data_ptr() for t in self.ce))
+        if isinstance(self.ch, float):
+            chptr, chv = None, self.ch
+        else:
+            chptr, chv = (C.c_void_p * 3)(*(t.data_ptr() for t in self.ch)), 0.0
+        return g, fptr, ceptr, chptr, chv
+
+    def _fused_stage(self, e_or_h, coef, cptr, chv, stream):
+        g, fptr = self._stage_args[0], self._stage_args[1]
+        cp = C.byref(self.cpml._structs[coef]) if self.cpml.active else None
+        psi = C.byref(self.cpml._psi) if self.cpml.active else None
+        N.call("fdtd_symplectic_stage_f32", C.byref(g), cp, int(e_or_h), float(coef), float(chv), fptr,
+               cptr, psi, stream)
+
+    def step_unfused(self, n=1):
+        """The same steps through the reference-shaped calls: update_h /
+        update_e per stage, then the per-axis CPML corrections."""
         nx, ny, nz = self.shape
         f, ce, ch = self.f, self.ce, self.ch
         if self.src_spec and self.tstep + n > self._src_steps:

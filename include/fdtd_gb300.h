@@ -41,6 +41,8 @@
  *   fdtd_symplectic_{h,e}_f32  4th_order-Symplectic/PyCUDA/100-base.py:10-44
  *                          update_h / update_e (stage coefficient argument);
  *                          4th_order-Symplectic/Python-C/dielectric.c:5-96
+ *   fdtd_symplectic_stage_f32  one stage of PyCUDA/100-base.py:124-141 with
+ *                          its CPML slabs in the same launch
  */
 #ifndef FDTD_GB300_H
 #define FDTD_GB300_H
@@ -359,6 +361,20 @@ int fdtd_symplectic_cpml_h_f32(const fdtd_grid *g, const fdtd_cpml *c, float cl,
                                float *hx, float *hy, float *hz,
                                const float *chx, const float *chy, const float *chz,
                                const fdtd_psi *psi, void *stream);
+
+/* One whole stage in one launch: the stage update of fdtd_symplectic_h_f32 /
+ * fdtd_symplectic_h_scalar_f32 (e_or_h = 0, coef = cl) or
+ * fdtd_symplectic_e_f32 (e_or_h = 1, coef = dl) followed, on the slabs of
+ * the enabled faces, by the corrections of fdtd_symplectic_cpml_{h,e}_f32 in
+ * their order (x, y, z), with the same arithmetic (bit-identical results).
+ * f = ex, ey, ez, hx, hy, hz; c = the updated field's coefficient arrays
+ * (ce for E; ch for H, or NULL with ch_scalar).  c (the CPML tables of this
+ * stage) and psi may be NULL: no absorbing slabs.  Replaces the stage loop
+ * body of 4th_order-Symplectic/PyCUDA/100-base.py:124-141 (one kernel per
+ * stage there as well). */
+int fdtd_symplectic_stage_f32(const fdtd_grid *g, const fdtd_cpml *c, int32_t e_or_h, float coef,
+                              float ch_scalar, float *const f[6], const float *const cf[3],
+                              const fdtd_psi *psi, void *stream);
 
 #ifdef __cplusplus
 }

@@ -138,3 +138,35 @@ def test_output_validation_before_cuda(lib):
     assert lib.fdtd_output_f32(C.byref(g), C.byref(o), f, out, 1000, None) == N.FDTD_ERR_SHAPE
     o.p2[1], o.form = 8, 3 * 16                                # family 3 does not exist
     assert lib.fdtd_output_f32(C.byref(g), C.byref(o), f, out, 1000, None) == N.FDTD_ERR_ARG
+
+
+def test_symplectic_stage_validation_before_cuda(lib):
+    """fdtd_symplectic_stage_f32 rejects missing fields, a stage kind other
+    than 0/1, an E stage without ce arrays, partial coefficient arrays, CPML
+    without psi and slabs thicker than the axis allows, all on the host."""
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(20, 20, 20, 400, 20)
+    fake = C.c_void_p(16)  # never dereferenced: every case fails validation first
+    f6 = (C.c_void_p * 6)(*([fake] * 6))
+    c3 = (C.c_void_p * 3)(fake, fake, fake)
+    part = (C.c_void_p * 3)(fake, None, fake)
+    call = lib.fdtd_symplectic_stage_f32
+    assert call(C.byref(g), None, 0, 0.5, 0.03, None, None, None, None) == N.FDTD_ERR_ARG
+    assert call(C.byref(g), None, 2, 0.5, 0.03, f6, c3, None, None) == N.FDTD_ERR_ARG
+    assert call(C.byref(g), None, 1, 0.5, 0.0, f6, None, None, None) == N.FDTD_ERR_ARG
+    assert call(C.byref(g), None, 0, 0.5, 0.0, f6, part, None, None) == N.FDTD_ERR_ARG
+    cp = N.Cpml()
+    for a in range(3):
+        cp.npml[a] = 4
+        for key in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h"):
+            getattr(cp, key)[a] = fake
+    cp.faces = 0x3F
+    assert call(C.byref(g), C.byref(cp), 1, 0.5, 0.0, f6, c3, None, None) == N.FDTD_ERR_ARG
+    psi = N.Psi()
+    for q in range(6):
+        psi.e[q] = fake
+        psi.h[q] = fake
+    cp.npml[1] = 10  # 2P + 2 = 22 > ny = 20
+    assert call(C.byref(g), C.byref(cp), 0, 0.5, 0.03, f6, None, C.byref(psi), None) == N.FDTD_ERR_SHAPE
+    bad = N.Grid(20, 20, 20, 399, 20)
+    assert call(C.byref(bad), None, 0, 0.5, 0.03, f6, None, None, None) == N.FDTD_ERR_SHAPE

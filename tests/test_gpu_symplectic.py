@@ -141,6 +141,38 @@ def test_symplectic_steps_bit_exact_vs_oracle(S, shape, npml, faces):
             np.testing.assert_array_equal(_host(solver.cpml.psi_h[q]), orc.psi_h[q], err_msg="psi_h%d" % q)
 
 
+@pytest.mark.parametrize("shape,npml,faces,ch_arrays", [((30, 26, 34), 5, 0x3F, False),
+                                                        ((24, 28, 20), 4, 0x15, True),
+                                                        ((26, 22, 30), 3, 0x2A, False),
+                                                        ((22, 22, 40), 0, 0x3F, True),
+                                                        ((50, 20, 36), 4, 0x3F, False)])
+def test_symplectic_fused_stages_equal_per_call_path(S, shape, npml, faces, ch_arrays):
+    """One launch per stage (stage update and CPML slabs together) equals the
+    reference-shaped calls (update_h / update_e, then the per-axis CPML
+    corrections) bit for bit, with uniform ch and with ch arrays."""
+    rng = np.random.default_rng(9)
+    ce = [(S.COURANT / 24 / rng.uniform(1.0, 4.0, shape)).astype(np.float32) for _ in range(3)]
+    ch = [(S.COURANT / 24 * rng.uniform(0.8, 1.0, shape)).astype(np.float32) for _ in range(3)] if ch_arrays else None
+    src = [("ez", (shape[0] // 2, shape[1] // 2, shape[2] // 2),
+            lambda t: np.sin(0.3 * t) * np.exp(-0.5 * ((t - 4.0) / 2.0) ** 2))]
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    runs = []
+    for fused in (True, False):
+        s = S.SymplecticSolver(shape, ce=ce, ch=ch, npml=npml, faces=faces, sources=src, max_steps=8)
+        s.set_fields(**init)
+        (s.step if fused else s.step_unfused)(5)
+        runs.append(s)
+    torch.cuda.synchronize()
+    a, b = runs
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)
+    if a.cpml.active:
+        for q in range(6):
+            if a.cpml.psi_e[q] is not None:
+                np.testing.assert_array_equal(_host(a.cpml.psi_e[q]), _host(b.cpml.psi_e[q]), err_msg="psi_e%d" % q)
+                np.testing.assert_array_equal(_host(a.cpml.psi_h[q]), _host(b.cpml.psi_h[q]), err_msg="psi_h%d" % q)
+
+
 def test_symplectic_cpml_absorbs(S):
     """A pulse launched in a CPML box leaves: field energy falls well below the
     PEC box's energy, which stays bounded (the scheme is stable)."""

@@ -112,6 +112,8 @@ _SIGS = {
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
     "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
+    "fdtd_yee_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml), C.POINTER(Sources), P,
+                                    I32, I64, I64, C.POINTER(I32), P]),
     "fdtd_adjoint_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P, P,
                                         C.POINTER(Points), P, P]),
     "fdtd_adjoint_step_noalloc_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P,
@@ -128,6 +130,8 @@ _SIGS = {
     "fdtd_batch_plan_set_current": (C.c_int, [P, I32]),
     "fdtd_batch_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_batch_plan_destroy": (C.c_int, [P]),
+    "fdtd_batched_run_f32": (C.c_int, [I32, C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
+                                       C.POINTER(Sources), P, P, C.c_size_t, I32, I64, I64, C.POINTER(I32), P]),
 }
 
 _lib = None

@@ -1586,6 +1586,18 @@ int fdtd_yee_plan_destroy(fdtd_yee_plan *pl) {
     return FDTD_OK;
 }
 
+int fdtd_yee_step_f32(const fdtd_grid *g, const fdtd_yee_state *st, const fdtd_cpml *c, const fdtd_sources *src,
+                      int32_t *status_dev, int32_t cur, int64_t t0, int64_t nsteps, int32_t *cur_out,
+                      void *stream) {
+    if (nsteps < 0) return FDTD_ERR_ARG;
+    fdtd_yee_plan *pl = nullptr;
+    FDTD_TRY(fdtd_yee_plan_create(&pl, g, st, c, src, nullptr, status_dev, cur));
+    const int r = fdtd_yee_plan_run(pl, t0, nsteps, stream);
+    if (cur_out) *cur_out = pl->cur;
+    fdtd_yee_plan_destroy(pl);  // host-side only: the launches hold copies of everything they use
+    return r;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1781,6 +1793,20 @@ int fdtd_batch_plan_info(const fdtd_batch_plan *bp, int32_t *info, int32_t n) {
 int fdtd_batch_plan_destroy(fdtd_batch_plan *bp) {
     delete bp;
     return FDTD_OK;
+}
+
+int fdtd_batched_run_f32(int32_t nsims, const fdtd_grid *grids, const fdtd_yee_state *states,
+                         const fdtd_cpml *cpmls, const fdtd_sources *srcs, int32_t *status_dev, void *workspace,
+                         size_t workspace_bytes, int32_t cur, int64_t t0, int64_t nsteps, int32_t *cur_out,
+                         void *stream) {
+    if (nsteps < 0) return FDTD_ERR_ARG;
+    fdtd_batch_plan *bp = nullptr;
+    FDTD_TRY(fdtd_batch_plan_create(&bp, nsims, grids, states, cpmls, srcs, nullptr, status_dev, workspace,
+                                    workspace_bytes, cur));
+    const int r = fdtd_batch_plan_run(bp, t0, nsteps, stream);
+    if (cur_out) *cur_out = fdtd_batch_plan_current(bp);
+    fdtd_batch_plan_destroy(bp);  // the launches read the caller's workspace, not the plan
+    return r;
 }
 
 }  // extern "C"

@@ -35,7 +35,8 @@
  *                          (centred fields, Poynting vector, square/sum/sqrt)
  *   fdtd_step_unfused_f32  one time step in the order of
  *                          fdtd3d_201_..._100000tstep.cu:718-742
- *   fdtd_yee_plan_*        the same step, fused into one pass per step
+ *   fdtd_yee_plan_*, fdtd_yee_step_f32  the same step, fused into one pass per
+ *                          step (the step function as one call, or a plan)
  *                          (no reference counterpart as one call; replaces
  *                          the >= 15 launches per step of the loop above)
  *   fdtd_symplectic_{h,e}_f32  4th_order-Symplectic/PyCUDA/100-base.py:10-44
@@ -244,6 +245,17 @@ int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
 int fdtd_yee_plan_info(const fdtd_yee_plan *plan, int32_t *info, int32_t n);
 int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 
+/* nsteps fused steps in one call: fdtd_yee_plan_create (default launch
+ * shape), fdtd_yee_plan_run, fdtd_yee_plan_destroy.  The plan's host set-up
+ * (tensor-map encoding, occupancy query) is paid on every call; keep a plan
+ * for repeated short runs.  cur: buffer holding the state now; *cur_out
+ * (may be NULL) receives the buffer holding it after the steps.  Replaces
+ * the time loop of fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:718-742
+ * (update_e, CPML-E, source, update_h, CPML-H per step) as one call. */
+int fdtd_yee_step_f32(const fdtd_grid *g, const fdtd_yee_state *st, const fdtd_cpml *c,
+                      const fdtd_sources *src, int32_t *status_dev, int32_t cur,
+                      int64_t t0, int64_t nsteps, int32_t *cur_out, void *stream);
+
 /* ---- batched fused step: many independent grids, one launch per step --- */
 /* Every grid keeps its own state, CPML and sources (arrays as for
  * fdtd_yee_plan_create); all grids advance together (same buffer index,
@@ -265,6 +277,15 @@ int fdtd_batch_plan_set_current(fdtd_batch_plan *plan, int32_t cur);
 /* info[0..5] = tile_y, stages, work items, CTAs launched, threads/CTA, shared bytes/CTA */
 int fdtd_batch_plan_info(const fdtd_batch_plan *plan, int32_t *info, int32_t n);
 int fdtd_batch_plan_destroy(fdtd_batch_plan *plan);
+
+/* The batched form in one call: fdtd_batch_plan_create (default launch
+ * shape), fdtd_batch_plan_run, fdtd_batch_plan_destroy; workspace as for
+ * fdtd_batch_plan_create.  *cur_out (may be NULL) receives the buffer
+ * holding every grid's state after the steps. */
+int fdtd_batched_run_f32(int32_t nsims, const fdtd_grid *grids, const fdtd_yee_state *states,
+                         const fdtd_cpml *cpmls, const fdtd_sources *srcs, int32_t *status_dev,
+                         void *workspace, size_t workspace_bytes, int32_t cur,
+                         int64_t t0, int64_t nsteps, int32_t *cur_out, void *stream);
 
 /* ---- adjoint (reverse-time) step -------------------------------------- */
 /* Point lists: comp 0..5 = ex, ey, ez, hx, hy, hz at (i, j, k); device arrays. */

@@ -170,3 +170,16 @@ def test_symplectic_stage_validation_before_cuda(lib):
     assert call(C.byref(g), C.byref(cp), 0, 0.5, 0.03, f6, None, C.byref(psi), None) == N.FDTD_ERR_SHAPE
     bad = N.Grid(20, 20, 20, 399, 20)
     assert call(C.byref(bad), None, 0, 0.5, 0.03, f6, None, None, None) == N.FDTD_ERR_SHAPE
+
+
+def test_one_call_entry_points_validation_before_cuda(lib):
+    """The one-call fused and batched entries reject a negative step count
+    and missing descriptions on the host."""
+    from fdtd_accelerate_gb300 import _native as N
+    g = N.Grid(20, 20, 20, 400, 20)
+    st = N.YeeState()
+    assert lib.fdtd_yee_step_f32(C.byref(g), C.byref(st), None, None, None, 0, 1, -1, None, None) == N.FDTD_ERR_ARG
+    assert lib.fdtd_yee_step_f32(None, C.byref(st), None, None, None, 0, 1, 2, None, None) == N.FDTD_ERR_ARG
+    assert lib.fdtd_yee_step_f32(C.byref(g), C.byref(st), None, None, None, 0, 1, 2, None, None) == N.FDTD_ERR_ARG
+    assert lib.fdtd_batched_run_f32(1, C.byref(g), C.byref(st), None, None, None, None, 0, 0, 1, -1, None,
+                                    None) == N.FDTD_ERR_ARG

@@ -150,3 +150,43 @@ def test_batch_argument_errors(F):
                                     C.c_void_p(ws.data_ptr()), ws.numel(), 0) == N.FDTD_ERR_ARG
     with pytest.raises(ValueError):
         F.BatchSolver([])
+
+
+def test_one_call_entry_points(F):
+    """fdtd_yee_step_f32 and fdtd_batched_run_f32 (plan create, run and
+    destroy in one call) give what the plans give, bit for bit, and report
+    the buffer that holds the state afterwards."""
+    import ctypes as C
+    from fdtd_accelerate_gb300 import _native as N
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # single grid: 5 steps through the plan (a) and through one call (b)
+    shape, npml, faces = GRIDS[2]
+    a, b = make_pair(F, 7, shape, npml, faces)
+    a.step(5)
+    out = C.c_int32(-1)
+    N.call("fdtd_yee_step_f32", C.byref(b.grid()), C.byref(b._state_struct()), C.byref(b.cpml.struct()),
+           C.byref(b.sources.struct()), C.c_void_p(b.status.data_ptr()), b.cur, int(b.tstep), 5,
+           C.byref(out), stream)
+    torch.cuda.synchronize()
+    assert out.value == a.cur
+    b.cur, b.tstep = out.value, b.tstep + 5
+    assert_same(a, b, "one-call step")
+    # a batch: 4 steps through BatchSolver and through one call
+    singles, batch = build(F)
+    for s in singles:
+        s.step(4)
+    sv = batch.solvers
+    n = len(sv)
+    grids = (N.Grid * n)(*[s.grid() for s in sv])
+    states = (N.YeeState * n)(*[s._state_struct() for s in sv])
+    cpmls = (N.Cpml * n)(*[s.cpml.struct() for s in sv])
+    srcs = (N.Sources * n)(*[s.sources.struct() for s in sv])
+    out = C.c_int32(-1)
+    N.call("fdtd_batched_run_f32", n, grids, states, cpmls, srcs, C.c_void_p(batch.status.data_ptr()),
+           C.c_void_p(batch.workspace.data_ptr()), batch.workspace.numel(), sv[0].cur, int(sv[0].tstep), 4,
+           C.byref(out), stream)
+    torch.cuda.synchronize()
+    for k, (s_single, s_batch) in enumerate(zip(singles, sv)):
+        s_batch.cur, s_batch.tstep = out.value, s_batch.tstep + 4
+        assert s_single.cur == out.value
+        assert_same(s_single, s_batch, "one-call batch grid %d" % k)

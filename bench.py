@@ -397,10 +397,10 @@ def run_symp512(args):
     # per step: 5 H stages and 4 E stages, one launch each (the CPML slabs in the same
     # launch), and the source kernel after each E stage
     per_step = 5 + 4 * 2
-    line = _base_line("Mcell-updates/s (4th-order symplectic 512^3, 10-cell CPML, FP32)", cells / (avg / 1e3) / 1e6,
+    line = _base_line("Mcell-updates/s (4th-order symplectic %dx%dx%d, 10-cell CPML, FP32)" % shape, cells / (avg / 1e3) / 1e6,
                       UNIT, args, avg, "f32", "4th-order symplectic %dx%dx%d, 10-cell CPML, 60 spheres eps_r " % shape +
                       "U[1,4], Ez dipole; 4 E + 5 H stages per step, one launch per stage with its CPML "
-                      "slabs (state 3.2 GB >> L2)",
+                      "slabs (6 fields + 3 coefficient arrays: %.1f GB >> L2)" % (9 * cells * 4 / 1e9),
                       {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                     "frac": achieved / peak, "traffic": None, "peak_source": psrc,
                                     "alg_bytes_per_launch": alg,

@@ -164,6 +164,18 @@ def cpu_oracle_sample(seconds=12.0, sample_shape=(256, 1024, 512)):
                       "scaled copy of the workload, %d steps, %.1f s" % (os.cpu_count(), *sample_shape, steps, el)}
 
 
+def max_over_ranks(x, device):
+    """The largest x over the ranks of the default process group (x itself
+    without one): whole-job times are the slowest rank's."""
+    import torch
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -222,10 +234,7 @@ def run_ours(args, rank, world):
     solver.check_status()
     total_ms = t_all0.elapsed_time(t_all1)
     per_launch_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     cells = int(np.prod(shape))
     value = cells * args.steps * world / (total_ms / 1e3) / 1e6
 
@@ -239,6 +248,8 @@ def run_ours(args, rank, world):
         for q in range(3):
             host_ce[q].copy_(solver.ce[q])
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -248,7 +259,7 @@ def run_ours(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         solver.check_status()
-        e_ms = e0.elapsed_time(e1)
+        e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
         h2d = 9 * cells * 4
         d2h = 6 * cells * 4
         e2e = {"value": cells * args.steps * world / (e_ms / 1e3) / 1e6, "unit": UNIT,

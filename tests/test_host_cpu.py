@@ -17,6 +17,22 @@ def test_cpml_tables_match_oracle_restatement(npml):
         np.testing.assert_allclose(a[k], b[k], rtol=1e-14, atol=1e-300, err_msg=k)
 
 
+@pytest.mark.parametrize("npml", [1, 4, 10, 16])
+def test_symplectic_stage_tables_match_oracle(npml):
+    """The 4th-order stage CPML tables (sub-step coef*S per stage) agree with
+    the oracle's restatement to FP64 rounding and are equal once rounded to
+    the FP32 the kernels read, for every stage coefficient."""
+    from fdtd_accelerate_gb300 import symplectic as S
+    for coef in sorted(set(S.CL) | set(S.DL[:4])):
+        a = S.stage_tables(npml, coef)
+        b = oracle.symp_stage_tables(npml, coef)
+        assert sorted(a) == sorted(b)
+        for k in a:
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-14, atol=1e-15, err_msg="%s %r" % (k, coef))
+            np.testing.assert_array_equal(np.asarray(a[k], np.float32), np.asarray(b[k], np.float32),
+                                          err_msg="%s %r" % (k, coef))
+
+
 def test_cpml_tables_reduce_to_non_kappa():
     """kappa_max = 1 gives km1 = 0 and a = sigma/(sigma+alpha)(b-1), the
     non-kappa coefficients of kuFDTD/v0.2.0/dim3/cpu/cpml.py:121-124."""

@@ -247,8 +247,10 @@ int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 
 /* nsteps fused steps in one call: fdtd_yee_plan_create (default launch
  * shape), fdtd_yee_plan_run, fdtd_yee_plan_destroy.  The plan's host set-up
- * (tensor-map encoding, occupancy query) is paid on every call; keep a plan
- * for repeated short runs.  cur: buffer holding the state now; *cur_out
+ * (tensor-map encoding, occupancy query, a synchronous read of the source
+ * positions: the call waits for the device once before it launches) is paid
+ * on every call; keep a plan for repeated short runs.  cur: buffer holding
+ * the state now; *cur_out
  * (may be NULL) receives the buffer holding it after the steps.  Replaces
  * the time loop of fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:718-742
  * (update_e, CPML-E, source, update_h, CPML-H per step) as one call. */
@@ -280,8 +282,9 @@ int fdtd_batch_plan_destroy(fdtd_batch_plan *plan);
 
 /* The batched form in one call: fdtd_batch_plan_create (default launch
  * shape), fdtd_batch_plan_run, fdtd_batch_plan_destroy; workspace as for
- * fdtd_batch_plan_create.  *cur_out (may be NULL) receives the buffer
- * holding every grid's state after the steps. */
+ * fdtd_batch_plan_create (whose synchronous copies into the workspace make
+ * the call wait for the device once before it launches).  *cur_out (may be
+ * NULL) receives the buffer holding every grid's state after the steps. */
 int fdtd_batched_run_f32(int32_t nsims, const fdtd_grid *grids, const fdtd_yee_state *states,
                          const fdtd_cpml *cpmls, const fdtd_sources *srcs, int32_t *status_dev,
                          void *workspace, size_t workspace_bytes, int32_t cur,

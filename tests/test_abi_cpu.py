@@ -183,3 +183,25 @@ def test_one_call_entry_points_validation_before_cuda(lib):
     assert lib.fdtd_yee_step_f32(C.byref(g), C.byref(st), None, None, None, 0, 1, 2, None, None) == N.FDTD_ERR_ARG
     assert lib.fdtd_batched_run_f32(1, C.byref(g), C.byref(st), None, None, None, None, 0, 0, 1, -1, None,
                                     None) == N.FDTD_ERR_ARG
+
+
+def _prototypes():
+    """name -> parameter count of every function prototype in include/*.h"""
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(fdtd_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+def test_ctypes_signatures_match_header():
+    """Every ctypes declaration in _native takes as many arguments as the C
+    prototype it binds (a changed prototype cannot drift from its binding)."""
+    from fdtd_accelerate_gb300 import _native as N
+    protos = _prototypes()
+    assert len(protos) >= 40
+    for name, (_, args) in N._SIGS.items():
+        assert name in protos, name
+        assert len(args) == protos[name], (name, len(args), protos[name])

@@ -21,6 +21,8 @@
 // family through its update mask, and only cells inside a mask are written.
 // No atomics: each output element is produced by one thread, so the result
 // does not depend on scheduling.
+#include <cuda.h>
+
 #include "common.cuh"
 
 #include <mutex>
@@ -477,9 +479,11 @@ int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_a
 //  * Maximum: kNoAllocScratchFloats floats (4 Mi floats = 16 MiB) for the
 //    12 w arrays, i.e. 4 * (2Px*ny*nz + nx*2Py*nz + nx*ny*2Pz) floats plus
 //    alignment; larger CPML layers are refused with FDTD_ERR_CAPACITY.
-//  * Set-up: the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current) and caches it; make
-//    that first call before any stream capture.
+//  * Set-up: the first call in a CUDA context looks up the array's device
+//    address (cudaGetSymbolAddress, with that context's device current) and
+//    caches it under the context's unique id; make that first call before
+//    any stream capture.  A context created anew (after cudaDeviceReset, for
+//    instance) loads the module again and gets a fresh lookup.
 //  * Nothing in the scratch has to start at zero: every element the kernels
 //    read is written earlier in the same call (disabled faces are neither
 //    written nor read).
@@ -490,26 +494,63 @@ namespace fdtd {
 namespace adj {
 
 constexpr size_t kNoAllocScratchFloats = size_t(4) << 20;
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
 
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Unique id of the calling thread's current context (0 when none is current).
+static int current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qb != cudaDriverEntryPointSuccess)
+            return FDTD_ERR_CUDA;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+        get_id = reinterpret_cast<CtxGetIdFn>(b);
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return FDTD_ERR_CUDA;
+    return get_id(ctx, id) == CUDA_SUCCESS ? FDTD_OK : FDTD_ERR_CUDA;
+}
+
 static std::mutex g_noalloc_mu;
-static float *g_noalloc_ptr[kMaxDevices];
+static unsigned long long g_noalloc_ctx[kMaxContexts];
+static float *g_noalloc_ptr[kMaxContexts];
+static int g_noalloc_n = 0;
 
 static int noalloc_scratch(float **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
-    if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    cudaError_t e;
+    if (current_context_id(&id) != FDTD_OK) {
+        // no context current on this thread yet: the symbol lookup initialises
+        // the current device's primary context and makes it current
         void *ptr = nullptr;
         e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
-        g_noalloc_ptr[dev] = static_cast<float *>(ptr);
+        FDTD_TRY(current_context_id(&id));
     }
-    *out = g_noalloc_ptr[dev];
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    for (int q = 0; q < g_noalloc_n; q++)
+        if (g_noalloc_ctx[q] == id) {
+            *out = g_noalloc_ptr[q];
+            return FDTD_OK;
+        }
+    if (g_noalloc_n == kMaxContexts) return FDTD_ERR_UNSUPPORTED;
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) { set_cuda_error(e); return FDTD_ERR_CUDA; }
+    g_noalloc_ctx[g_noalloc_n] = id;
+    g_noalloc_ptr[g_noalloc_n] = static_cast<float *>(ptr);
+    g_noalloc_n++;
+    *out = static_cast<float *>(ptr);
     return FDTD_OK;
 }
 

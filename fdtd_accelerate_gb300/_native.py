@@ -61,6 +61,10 @@ class YeeState(C.Structure):
                 ("tfsf", P)]
 
 
+class SympState(C.Structure):
+    _fields_ = [("f", (P * 6) * 2), ("psi_e", P * 6), ("psi_h", (P * 6) * 2), ("ce", P * 3)]
+
+
 class Tile(C.Structure):
     _fields_ = [("tile_y", I32), ("x_chunk", I32), ("ctas_per_sm", I32), ("stages", I32), ("l2_promotion", I32)]
 
@@ -106,7 +110,7 @@ _SIGS = {
     "fdtd_symplectic_stage_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), I32, F32, F32, C.POINTER(P * 6),
                                             C.POINTER(P * 3), C.POINTER(Psi), P]),
     "fdtd_yee_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
-                                       C.POINTER(Sources), C.POINTER(Tile), P, I32]),
+                                       C.POINTER(Sources), C.POINTER(Tile), P, I32, P]),
     "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),
     "fdtd_yee_plan_current": (C.c_int, [P]),
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
@@ -121,10 +125,20 @@ _SIGS = {
     "fdtd_gather_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_step_unfused_f64": (C.c_int, [C.POINTER(Grid), P, P, C.POINTER(Cpml), P, P, C.POINTER(Sources), I64, P]),
     "fdtd_gather_points_f64": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
+    "fdtd_add_sources_f64": (C.c_int, [C.POINTER(Grid), C.POINTER(Sources), I64, P, P, P, P]),
+    "fdtd_symplectic_stage_f64": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), I32, C.c_double, C.c_double,
+                                            C.POINTER(P * 6), C.POINTER(P * 3), C.POINTER(P * 6), P]),
     "fdtd_add_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
+    "fdtd_symp_pair_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(SympState),
+                                             C.POINTER(Sources), I32, I32, P, P]),
+    "fdtd_symp_pair_run": (C.c_int, [P, C.POINTER(Cpml), C.POINTER(Cpml), C.POINTER(Cpml), F32, F32, I32, F32,
+                                     F32, I64, P]),
+    "fdtd_symp_pair_plan_current": (C.c_int, [P]),
+    "fdtd_symp_pair_plan_set_current": (C.c_int, [P, I32]),
+    "fdtd_symp_pair_plan_destroy": (C.c_int, [P]),
     "fdtd_batch_workspace_bytes": (C.c_size_t, [I32]),
     "fdtd_batch_plan_create": (C.c_int, [C.POINTER(P), I32, C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml),
-                                         C.POINTER(Sources), C.POINTER(Tile), P, P, C.c_size_t, I32]),
+                                         C.POINTER(Sources), C.POINTER(Tile), P, P, C.c_size_t, I32, P]),
     "fdtd_batch_plan_run": (C.c_int, [P, I64, I64, P]),
     "fdtd_batch_plan_current": (C.c_int, [P]),
     "fdtd_batch_plan_set_current": (C.c_int, [P, I32]),

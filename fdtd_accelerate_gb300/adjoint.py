@@ -123,7 +123,7 @@ class YeeAdjoint:
                     h = C.c_void_p()
                     st = self._plan_state(m)
                     N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
-                           C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), 0)
+                           C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), 0, self._stream())
                     plans.append(h)
             self._plans = plans
         return self._plans

@@ -86,12 +86,13 @@ class BatchSolver:
             srcs = (N.Sources * n)(*[s.sources.struct() for s in self.solvers])
             tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             h = C.c_void_p()
-            # the workspace is rewritten: no launch of an earlier plan may still read it
-            torch.cuda.synchronize(self.device)
+            # the workspace is rewritten on the current stream, after the launches
+            # queued on it that may still read it
             with torch.cuda.device(self.device):
+                stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
                 N.call("fdtd_batch_plan_create", C.byref(h), n, grids, states, cpmls, srcs, C.byref(tile),
                        C.c_void_p(self.status.data_ptr()), C.c_void_p(self.workspace.data_ptr()),
-                       self.workspace.numel(), self.cur)
+                       self.workspace.numel(), self.cur, stream)
             self._plan = h
         return self._plan
 

@@ -142,8 +142,9 @@ class YeeSolver:
             tile = N.Tile(*(tuple(self.tile or ()) + (0, 0, 0, 0, 0))[:5])
             h = C.c_void_p()
             with torch.cuda.device(self.device):
+                stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
                 N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
-                       C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), self.cur)
+                       C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), self.cur, stream)
             self._plan = h
         return self._plan
 
@@ -155,13 +156,13 @@ class YeeSolver:
                          "launches_per_step"), list(info)))
 
     def step(self, n=1):
+        """Advance n steps with the fused kernel (one launch per step)."""
         if self.tfsf is not None:
             # the plan holds the source table's address: a longer table needs a new plan
             old = self.tfsf.amp.data_ptr()
             self.tfsf.ensure_steps(self.tstep + n)
             if self.tfsf.amp.data_ptr() != old:
                 self.close()
-        """Advance n steps with the fused kernel (one launch per step)."""
         plan = self.plan()
         L = N.lib()
         L.fdtd_yee_plan_set_current(plan, self.cur)

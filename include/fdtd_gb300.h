@@ -5,10 +5,15 @@
  * are DEVICE pointers to float32 arrays of logical shape (nx, ny, nz),
  * z fastest, with element strides sx (x) and sy (y) and unit z stride --
  * the memory layout of the reference's C-order NumPy field arrays (and of
- * KEMP's z-padded arrays).  Every entry point is stream-ordered (no host
- * synchronisation), allocates no device memory, never exits the process,
- * and returns an fdtd_status.  `stream` is a cudaStream_t (NULL = legacy
- * default stream).
+ * KEMP's z-padded arrays).  Every entry point that launches work is
+ * stream-ordered on its `stream` and does not synchronise the host, except
+ * plan creation: fdtd_yee_plan_create (when the grid has sources) and
+ * fdtd_batch_plan_create read or write device memory on the given stream
+ * and wait for that stream once before they return, so they belong
+ * outside stream capture; the plans' run calls are stream-ordered and
+ * capturable.  No entry point allocates device memory, none exits the
+ * process, and each returns an fdtd_status.  `stream` is a cudaStream_t
+ * (NULL = legacy default stream).
  *
  * Reference interfaces replaced (paths inside wbkifun/fdtd_accelerate):
  *   fdtd_update_e_f32      2nd_order-Yee/Numpy/fdtd3d.py:10-13 update_e;
@@ -232,10 +237,13 @@ typedef struct {
 typedef struct fdtd_yee_plan fdtd_yee_plan;
 
 /* status_dev: device int32 the kernel sets non-zero when a bounded wait
- * expires (may be NULL). cur: index of the buffer holding the state now. */
+ * expires (may be NULL). cur: index of the buffer holding the state now.
+ * stream: the source positions (device array src->ijk) are read on this
+ * stream, after any work queued on it, and the call waits for that read
+ * (host-side capacity checks need them). */
 int fdtd_yee_plan_create(fdtd_yee_plan **plan, const fdtd_grid *g, const fdtd_yee_state *st,
                          const fdtd_cpml *c, const fdtd_sources *src, const fdtd_tile *tile,
-                         int32_t *status_dev, int32_t cur);
+                         int32_t *status_dev, int32_t cur, void *stream);
 int fdtd_yee_plan_run(fdtd_yee_plan *plan, int64_t t0, int64_t nsteps, void *stream);
 int fdtd_yee_plan_current(const fdtd_yee_plan *plan);
 int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
@@ -246,10 +254,10 @@ int fdtd_yee_plan_info(const fdtd_yee_plan *plan, int32_t *info, int32_t n);
 int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 
 /* nsteps fused steps in one call: fdtd_yee_plan_create (default launch
- * shape), fdtd_yee_plan_run, fdtd_yee_plan_destroy.  The plan's host set-up
- * (tensor-map encoding, occupancy query, a synchronous read of the source
- * positions: the call waits for the device once before it launches) is paid
- * on every call; keep a plan for repeated short runs.  cur: buffer holding
+ * shape), fdtd_yee_plan_run, fdtd_yee_plan_destroy, all on `stream`.  The
+ * plan's host set-up (tensor-map encoding, occupancy query, the read of the
+ * source positions on `stream`: the call waits for that stream once before
+ * it launches) is paid on every call; keep a plan for repeated short runs.  cur: buffer holding
  * the state now; *cur_out
  * (may be NULL) receives the buffer holding it after the steps.  Replaces
  * the time loop of fdtd3d_201_250x250x320cell_15npml_100000tstep.cu:718-742
@@ -257,6 +265,40 @@ int fdtd_yee_plan_destroy(fdtd_yee_plan *plan);
 int fdtd_yee_step_f32(const fdtd_grid *g, const fdtd_yee_state *st, const fdtd_cpml *c,
                       const fdtd_sources *src, int32_t *status_dev, int32_t cur,
                       int64_t t0, int64_t nsteps, int32_t *cur_out, void *stream);
+
+/* ---- fused 4th-order stage pair (one HBM pass per H+E stage pair) ------- */
+/* State in two buffers (ping-pong): f[b] = ex,ey,ez,hx,hy,hz of buffer b,
+ * psi_h[b] the H psi slabs of buffer b (layouts of fdtd_psi); the E psi
+ * slabs psi_e are updated in place.  Requirements: C-order arrays with
+ * 16-byte aligned bases and rows (nz a multiple of 4 floats), fewer than
+ * 2^31 elements each, nx, ny, nz >= 4, a uniform ch. */
+typedef struct {
+    float *f[2][6];
+    float *psi_e[6];
+    float *psi_h[2][6];
+    const float *ce[3];
+} fdtd_symp_state;
+
+typedef struct fdtd_symp_plan fdtd_symp_plan;
+
+/* x_chunk: x planes per work item (0: 128); cur: buffer holding the state;
+ * the source positions are read on `stream` (the call waits for it once). */
+int fdtd_symp_pair_plan_create(fdtd_symp_plan **plan, const fdtd_grid *g, const fdtd_symp_state *st,
+                               const fdtd_sources *src, int32_t x_chunk, int32_t cur,
+                               int32_t *status_dev, void *stream);
+/* One pass: the H stage cl_a (with two_h = 1, then the H stage cl_b), the E
+ * stage dl, then the sources at amplitude index src_t, reading buffer cur and
+ * writing the other.  Each stage's CPML tables come from its fdtd_cpml (the
+ * H tables of h_a / h_b, the E tables of e; NULL: no CPML); ch is uniform.
+ * Bit-identical to fdtd_symplectic_stage_f32 for each stage in turn and
+ * fdtd_add_sources_f32.  Replaces one (update_h, update_e) pair of the
+ * stage loop of 4th_order-Symplectic/PyCUDA/100-base.py:124-141. */
+int fdtd_symp_pair_run(fdtd_symp_plan *plan, const fdtd_cpml *h_a, const fdtd_cpml *h_b,
+                       const fdtd_cpml *e, float cl_a, float cl_b, int32_t two_h, float dl,
+                       float ch, int64_t src_t, void *stream);
+int fdtd_symp_pair_plan_current(const fdtd_symp_plan *plan);
+int fdtd_symp_pair_plan_set_current(fdtd_symp_plan *plan, int32_t cur);
+int fdtd_symp_pair_plan_destroy(fdtd_symp_plan *plan);
 
 /* ---- batched fused step: many independent grids, one launch per step --- */
 /* Every grid keeps its own state, CPML and sources (arrays as for
@@ -269,10 +311,13 @@ int fdtd_yee_step_f32(const fdtd_grid *g, const fdtd_yee_state *st, const fdtd_c
  * replaces one reference time loop per simulation. */
 typedef struct fdtd_batch_plan fdtd_batch_plan;
 size_t fdtd_batch_workspace_bytes(int32_t nsims);
+/* stream: the workspace is filled on this stream, after the work queued on
+ * it (earlier launches that may still read the workspace), and the call
+ * waits for the copies before it returns. */
 int fdtd_batch_plan_create(fdtd_batch_plan **plan, int32_t nsims, const fdtd_grid *grids,
                            const fdtd_yee_state *states, const fdtd_cpml *cpmls,
                            const fdtd_sources *srcs, const fdtd_tile *tile, int32_t *status_dev,
-                           void *workspace, size_t workspace_bytes, int32_t cur);
+                           void *workspace, size_t workspace_bytes, int32_t cur, void *stream);
 int fdtd_batch_plan_run(fdtd_batch_plan *plan, int64_t t0, int64_t nsteps, void *stream);
 int fdtd_batch_plan_current(const fdtd_batch_plan *plan);
 int fdtd_batch_plan_set_current(fdtd_batch_plan *plan, int32_t cur);
@@ -281,9 +326,9 @@ int fdtd_batch_plan_info(const fdtd_batch_plan *plan, int32_t *info, int32_t n);
 int fdtd_batch_plan_destroy(fdtd_batch_plan *plan);
 
 /* The batched form in one call: fdtd_batch_plan_create (default launch
- * shape), fdtd_batch_plan_run, fdtd_batch_plan_destroy; workspace as for
- * fdtd_batch_plan_create (whose synchronous copies into the workspace make
- * the call wait for the device once before it launches).  *cur_out (may be
+ * shape), fdtd_batch_plan_run, fdtd_batch_plan_destroy, all on `stream`;
+ * workspace as for fdtd_batch_plan_create (whose copies into the workspace
+ * make the call wait for that stream once before it launches).  *cur_out (may be
  * NULL) receives the buffer holding every grid's state after the steps. */
 int fdtd_batched_run_f32(int32_t nsims, const fdtd_grid *grids, const fdtd_yee_state *states,
                          const fdtd_cpml *cpmls, const fdtd_sources *srcs, int32_t *status_dev,
@@ -354,6 +399,18 @@ int fdtd_step_unfused_f64(const fdtd_grid *g, double *const f[6], const double *
 /* out[p] = f[comp[p]][i, j, k] in double (NaN for a point outside the grid) */
 int fdtd_gather_points_f64(const fdtd_grid *g, const fdtd_points *pts, const double *const f[6],
                            double *out, void *stream);
+/* The soft sources of fdtd_add_sources_f32 on double arrays (FP32 amplitudes
+ * widened), list order. */
+int fdtd_add_sources_f64(const fdtd_grid *g, const fdtd_sources *src, int64_t t,
+                         double *ex, double *ey, double *ez, void *stream);
+/* One 4th-order stage with its stage-wise CPML in FP64, in place: the
+ * arithmetic of fdtd_symplectic_stage_f32 in double (4th_order-Symplectic/
+ * PyCUDA/100-base.py:10-44 run in float64).  coef, ch_scalar and cf are the
+ * FP32 path's values widened; the CPML tables stay FP32 and are widened; psi:
+ * the stage's six psi arrays (E stage: E psi, H stage: H psi) in double. */
+int fdtd_symplectic_stage_f64(const fdtd_grid *g, const fdtd_cpml *c, int32_t e_or_h, double coef,
+                              double ch_scalar, double *const f[6], const double *const cf[3],
+                              double *const psi[6], void *stream);
 
 /* ---- 4th-order symplectic stages (in place) --------------------------- */
 int fdtd_symplectic_h_f32(const fdtd_grid *g, float cl,

@@ -59,7 +59,7 @@ def test_validation_before_cuda(lib):
     assert lib.fdtd_update_e_f32(C.byref(bad), *null, None) == N.FDTD_ERR_SHAPE
     assert lib.fdtd_update_pbc_e_f32(None, 1, None, None, None, None) == N.FDTD_ERR_ARG
     h = C.c_void_p()
-    assert lib.fdtd_yee_plan_create(C.byref(h), C.byref(g), None, None, None, None, None, 0) == N.FDTD_ERR_ARG
+    assert lib.fdtd_yee_plan_create(C.byref(h), C.byref(g), None, None, None, None, None, 0, None) == N.FDTD_ERR_ARG
 
 
 def test_plan_rejects_unaligned_strides(lib):
@@ -74,7 +74,7 @@ def test_plan_rejects_unaligned_strides(lib):
     h = C.c_void_p()
     status = C.c_int32(0)
     r = lib.fdtd_yee_plan_create(C.byref(h), C.byref(g), C.byref(st), None, None, None,
-                                 C.byref(status), 0)
+                                 C.byref(status), 0, None)
     assert r == N.FDTD_ERR_ALIGN
 
 

@@ -143,11 +143,11 @@ def test_batch_argument_errors(F):
     ws = batch.workspace
     status = C.c_void_p(batch.status.data_ptr())
     assert L.fdtd_batch_plan_create(C.byref(h), n, grids, states, cpmls, srcs, C.byref(tile), status,
-                                    C.c_void_p(ws.data_ptr()), ws.numel() - 1, 0) == N.FDTD_ERR_CAPACITY
+                                    C.c_void_p(ws.data_ptr()), ws.numel() - 1, 0, None) == N.FDTD_ERR_CAPACITY
     assert L.fdtd_batch_plan_create(C.byref(h), n, grids, states, cpmls, srcs, C.byref(tile), status,
-                                    C.c_void_p(ws.data_ptr() + 16), ws.numel(), 0) == N.FDTD_ERR_ALIGN
+                                    C.c_void_p(ws.data_ptr() + 16), ws.numel(), 0, None) == N.FDTD_ERR_ALIGN
     assert L.fdtd_batch_plan_create(C.byref(h), 0, grids, states, cpmls, srcs, C.byref(tile), status,
-                                    C.c_void_p(ws.data_ptr()), ws.numel(), 0) == N.FDTD_ERR_ARG
+                                    C.c_void_p(ws.data_ptr()), ws.numel(), 0, None) == N.FDTD_ERR_ARG
     with pytest.raises(ValueError):
         F.BatchSolver([])
 
@@ -190,3 +190,35 @@ def test_one_call_entry_points(F):
         s_batch.cur, s_batch.tstep = out.value, s_batch.tstep + 4
         assert s_single.cur == out.value
         assert_same(s_single, s_batch, "one-call batch grid %d" % k)
+
+
+def test_plan_creation_is_stream_ordered(F):
+    """A batch plan created on a non-blocking stream, right after work on that
+    stream rewrote a source position and with no device-wide synchronisation
+    in between, sees the new position.  The source sits on an E z-slab node,
+    which the batched band kernel takes from the host-side list that plan
+    creation reads, so a read that ran ahead of the stream would drop it."""
+    shape, npml, nsteps = (40, 36, 48), 6, 12
+    t = np.arange(nsteps + 2, dtype=np.float64)
+    good = (shape[0] // 2, shape[1] // 2, 1)                 # E z-slab node (front z face)
+    src = [("ey", good, np.sin(0.3 * t))]
+    rng = np.random.default_rng(9)
+    init = {k: rng.standard_normal(shape).astype(np.float32) * np.float32(0.1) for k in NAMES}
+    single = F.YeeSolver(shape, npml=npml, sources=src)
+    single.set_fields(**init)
+    other = F.YeeSolver(shape, npml=npml, sources=src)
+    other.set_fields(**init)
+    batch = F.BatchSolver([other])
+    right = other.sources.ijk.clone()
+    other.sources.ijk.copy_(torch.tensor([good[0], good[1], shape[2] // 2], dtype=torch.int32, device="cuda"))
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        torch.cuda._sleep(200_000_000)          # keep the stream busy well past the plan call
+        other.sources.ijk.copy_(right)          # the position the plan must see
+        batch.plan()
+        batch.step(nsteps)
+    single.step(nsteps)
+    torch.cuda.synchronize()
+    batch.check_status()
+    assert_same(single, other, "stream-ordered plan")

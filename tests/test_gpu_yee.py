@@ -223,7 +223,8 @@ def test_fused_step_bit_exact_vs_oracle_and_unfused(fdtd, shape, npml, tile):
 def test_fused_z_slab_faces_and_sources(fdtd, shape, npml, faces, tile):
     """The z-slab CPML (band kernels after the fused kernel) with one or both z
     faces, and soft sources of every component on E z-slab nodes of both sides
-    (two of them on one cell: list order), equals the oracle bit for bit."""
+    (two of them on one cell: list order; some on the rows next to a tile edge
+    in y), equals the oracle bit for bit."""
     rng = np.random.default_rng(23)
     ce = [(0.5 / rng.uniform(1.0, 6.0, shape)).astype(np.float32) for _ in range(3)]
     nsteps = 7
@@ -233,6 +234,8 @@ def test_fused_z_slab_faces_and_sources(fdtd, shape, npml, faces, tile):
     for n, (comp, k) in enumerate([("ex", 1), ("ey", npml), ("ez", 2), ("ex", nz - npml - 1), ("ey", nz - 2),
                                    ("ez", nz - 3), ("ex", 1)]):
         sources.append((comp, (shape[0] // 2 + n % 3, shape[1] // 2 - n % 2, k), fdtd.gaussian_sine(t, 2.0 + n, 2.0, 0.1)))
+    for n, (comp, j, k) in enumerate([("ex", 8, 1), ("ey", 7, nz - 2), ("ez", 4, npml), ("ey", 3, nz - npml - 1)]):
+        sources.append((comp, (shape[0] // 3, j, k), fdtd.gaussian_sine(t, 3.0 + n, 2.0, 0.1)))
     init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
     sim = _oracle_sim(shape, ce, (npml,) * 3, faces, sources, init)
     sim.step(nsteps)

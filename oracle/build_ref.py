@@ -18,6 +18,8 @@ Artefacts
                                 (Python extension, Py3 init shim).
   ref_drude_ade*.so             kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c
                                 (Python extension, Py3 init shim).
+  ref_cpml_core*.so             kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c
+                                (the kappa CPML, Python extension, Py3 init shim).
 """
 import os
 import platform
@@ -35,6 +37,8 @@ KUFDTD_CPML = "kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c"
 KUFDTD_INC = "kuFDTD/v0.2.0/dim3/cpu/core"
 SYMP_SRC = "4th_order-Symplectic/Python-C/dielectric.c"
 KUFDTD_DRUDE = "kuFDTD/v0.2.0/dim3/cpu/core/drude_ade.c"
+KUFDTD_KAPPA = "kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c"
+KUFDTD_KAPPA_INC = "kuFDTD/before_CUDA/v0.3.0/boundary/core"
 
 
 def available():
@@ -106,7 +110,8 @@ def build(verbose=False):
     for name, src, old_init, extra in (
             ("ref_cpml_non_kappa", KUFDTD_CPML, "initcpml_non_kappa", ["-I" + os.path.join(REF, KUFDTD_INC)]),
             ("ref_symp_dielectric", SYMP_SRC, "initdielectric", []),
-            ("ref_drude_ade", KUFDTD_DRUDE, "initdrude_ade", ["-I" + os.path.join(REF, KUFDTD_INC)])):
+            ("ref_drude_ade", KUFDTD_DRUDE, "initdrude_ade", ["-I" + os.path.join(REF, KUFDTD_INC)]),
+            ("ref_cpml_core", KUFDTD_KAPPA, "initcpml_core", ["-I" + os.path.join(REF, KUFDTD_KAPPA_INC)])):
         jobs.append(["gcc", "-O2", "-fPIC", "-shared", "-w", "-I" + pyinc, "-I" + npinc, *extra,
                      '-DREF_SRC="%s"' % os.path.join(REF, src),
                      '-DSHIM_NAME="%s"' % name, "-DSHIM_INIT=PyInit_" + name,

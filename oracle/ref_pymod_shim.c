@@ -11,6 +11,12 @@
 
 static PyMethodDef *shim_methods_;
 #define Py_InitModule3(name, methods, doc) (shim_methods_ = (methods), (PyObject *)NULL)
+/* Python 3 has one integer type */
+#define PyInt_AsLong PyLong_AsLong
+/* Python 2's PyList_Check expanded to a parenthesised expression, and some
+ * sources use it bare (`else if PyList_Check(x)`) */
+#undef PyList_Check
+#define PyList_Check(op) (PyType_FastSubclass(Py_TYPE(op), Py_TPFLAGS_LIST_SUBCLASS))
 
 #include REF_SRC
 

@@ -430,8 +430,165 @@ def output_kufdtd(rng):
     return out
 
 
+def cpml_kappa_kufdtd(rng):
+    """Run the reference's kappa CPML (update_cpml_3d of
+    kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c:22-330) and remap it to
+    this package's slab layout.  That code keeps E on 'in_field' arrays (one
+    cell smaller) and H on 'out_field' arrays (a ghost layer at index 0), the
+    'hfaced' grid of boundary/cpml.py:150-158, whose differences are this
+    package's (E: forward, H: backward).  Mapping, per face axis d:
+      E update (in_field, N[d] = n_d - 3, other N = n - 1): reference cell
+        idx <-> our E cell idx + 1 along d; its base H(idx + 1 off d, idx along d)
+        <-> our H(idx) shifted by -1 along d; psi and coefficient index equal.
+      H update (out_field, N = n - 1): reference cell idx <-> our H cell idx;
+        its base E(idx - 1 off d) <-> our E(idx); psi index equal.
+    Tables: b, a (FP32) and kappa = 1/(1 + km1) (FP32) from the FP64 tables
+    of this package's formula (kappa_max = 5, R = 1e-8, m = 4, alpha_max = 0.05),
+    ds = 1.  The H coefficient is the scalar 0.5 (1x1x1 arrays, EorH = -1);
+    E takes per-cell coefficient arrays (EorH = +1)."""
+    sys.path.insert(0, build_ref.OUT)
+    import ref_cpml_core as ref
+    import oracle
+    out = {}
+    n = 0
+    shape = (10, 9, 12)
+    P = 3
+    tab64 = oracle.cpml_tables(P)
+    for axis in range(3):
+        for which in ("e", "h"):
+            for side in ("front", "back"):
+                nshape = list(shape)
+                perm1, perm2 = (axis + 1) % 3, (axis + 2) % 3
+                kapa = (1.0 / (1.0 + tab64["km1_" + which])).astype(F32)
+                b = tab64["b_" + which].astype(F32)
+                a = tab64["a_" + which].astype(F32)
+                if which == "e":
+                    N = [v - 1 for v in shape]
+                    N[axis] = shape[axis] - 3
+                    ushape = [v + 1 for v in N]                 # in_field
+                    bshape = [v + 2 for v in N]                 # out_field
+                    up = [rng.standard_normal(ushape).astype(F32) for _ in range(3)]
+                    base = [rng.standard_normal(bshape).astype(F32) for _ in range(3)]
+                    cb = [(rng.random(ushape, dtype=F32) * F32(0.5) + F32(0.05)) for _ in range(3)]
+                    pshape = list(ushape)
+                    pshape[axis] = 2 * P
+                else:
+                    N = [v - 1 for v in shape]
+                    ushape = [v + 2 for v in N]                 # out_field
+                    bshape = [v + 1 for v in N]                 # in_field
+                    up = [rng.standard_normal(ushape).astype(F32) for _ in range(3)]
+                    base = [rng.standard_normal(bshape).astype(F32) for _ in range(3)]
+                    cb = [np.full((1, 1, 1), 0.5, F32) for _ in range(3)]
+                    pshape = list(ushape)
+                    pshape[axis] = 2 * P
+                psi = [None] * 6
+                psi[2 * axis] = rng.standard_normal(pshape).astype(F32) * F32(0.1)
+                psi[2 * axis + 1] = rng.standard_normal(pshape).astype(F32) * F32(0.1)
+                for q in range(6):  # the other axes' psi arrays are not read
+                    if psi[q] is None:
+                        psi[q] = np.zeros((1, 1, 1), F32)
+                up_in = [u.copy() for u in up]
+                psi_in = [psi[2 * axis].copy(), psi[2 * axis + 1].copy()]
+                ref.update_cpml_3d("in_field" if which == "e" else "out_field", tuple(N), up, base, cb, 1.0, P,
+                                   [kapa, b, a], psi, axis, side)
+                # ---- remap into this package's layout
+                sl_all = [slice(None)] * 3
+                ours_up_in, ours_up_out, ours_base, ours_c = [], [], [], []
+                for q in range(3):
+                    if which == "e":
+                        fi = rng.standard_normal(shape).astype(F32)
+                        fo = fi.copy()
+                        dst = list(sl_all)
+                        dst[axis] = slice(1, shape[axis] - 1)
+                        fi[tuple(dst)] = up_in[q]
+                        fo[tuple(dst)] = up[q]
+                        hb = rng.standard_normal(shape).astype(F32)
+                        src = [slice(1, shape[x] + 1) for x in range(3)]
+                        src[axis] = slice(0, shape[axis] - 1)
+                        dsth = list(sl_all)
+                        dsth[axis] = slice(1, None)
+                        hb[tuple(dsth)] = base[q][tuple(src)]
+                        c = (rng.random(shape, dtype=F32) * F32(0.5) + F32(0.05))
+                        c[tuple(dst)] = cb[q]
+                        ours_c.append(c)
+                    else:
+                        fi = up_in[q][:shape[0], :shape[1], :shape[2]].copy()
+                        fo = up[q][:shape[0], :shape[1], :shape[2]].copy()
+                        hb = rng.standard_normal(shape).astype(F32)
+                        dst = [slice(1, None)] * 3
+                        dst[axis] = slice(None)
+                        src = [slice(0, shape[x] - 1) for x in range(3)]
+                        src[axis] = slice(None)
+                        hb[tuple(dst)] = base[q][tuple(src)]
+                    ours_up_in.append(fi)
+                    ours_up_out.append(fo)
+                    ours_base.append(hb)
+                mshape = [shape[0], shape[1], shape[2]]
+                mshape[axis] = 2 * P
+                crop = tuple(slice(0, v) for v in mshape)
+                p_in = [psi_in[r][crop].copy() for r in range(2)]
+                p_out = [psi[2 * axis + r][crop].copy() for r in range(2)]
+                # comparison masks: the face's nodes, where both conventions update
+                nodes = range(1, P + 1) if side == "front" else (
+                    range(shape[axis] - P - 1, shape[axis] - 1) if which == "e" else range(shape[axis] - P, shape[axis]))
+                fmask = [np.zeros(shape, bool) for _ in range(3)]
+                pmask = [np.zeros(mshape, bool) for _ in range(2)]
+                for r, comp in enumerate((perm1, perm2)):
+                    m = np.zeros(shape, bool)
+                    idx = list(sl_all)
+                    idx[axis] = list(nodes)
+                    m[tuple(idx)] = True
+                    for x in range(3):          # the component's own update range
+                        if x == comp:
+                            continue
+                        cut = [slice(None)] * 3
+                        if which == "e":
+                            cut[x] = shape[x] - 1   # E: the last plane across is never updated
+                        else:
+                            cut[x] = 0              # H: index 0 is never updated
+                        m[tuple(cut)] = False
+                    if which == "h":              # the reference's out_field loops start at 1
+                        for x in range(3):
+                            if x != axis:
+                                cut = [slice(None)] * 3
+                                cut[x] = 0
+                                m[tuple(cut)] = False
+                    fmask[comp] = m
+                    pm = np.zeros(mshape, bool)
+                    s0 = 0 if side == "front" else P
+                    idx = list(sl_all)
+                    idx[axis] = slice(s0, s0 + P)
+                    mm = np.moveaxis(m, axis, 0)[list(nodes)]
+                    pm_view = np.moveaxis(pm, axis, 0)
+                    pm_view[s0:s0 + P] = mm
+                    pmask[r] = pm
+                tag = "c%d_" % n
+                out[tag + "meta"] = np.array([axis, 0 if which == "e" else 1, 0 if side == "front" else 1, P])
+                names_u = ("ex", "ey", "ez") if which == "e" else ("hx", "hy", "hz")
+                names_b = ("hx", "hy", "hz") if which == "e" else ("ex", "ey", "ez")
+                for q in range(3):
+                    out[tag + "in_" + names_u[q]] = ours_up_in[q]
+                    out[tag + "out_" + names_u[q]] = ours_up_out[q]
+                    out[tag + "in_" + names_b[q]] = ours_base[q]
+                    out[tag + "fmask_" + names_u[q]] = fmask[q]
+                    if which == "e":
+                        out[tag + "in_" + ("cex", "cey", "cez")[q]] = ours_c[q]
+                for r in range(2):
+                    out[tag + "psi_in%d" % r] = p_in[r]
+                    out[tag + "psi_out%d" % r] = p_out[r]
+                    out[tag + "pmask%d" % r] = pmask[r]
+                out[tag + "tb"] = b
+                out[tag + "ta"] = a
+                out[tag + "tkm1"] = tab64["km1_" + which].astype(F32)
+                n += 1
+    out["ncases"] = np.array(n)
+    out["shape"] = np.array(shape)
+    return out
+
+
 CASES = (("yee_numpy", yee_numpy), ("kemp_core", kemp_core), ("cpml_kufdtd", cpml_kufdtd), ("symp_c", symp_c),
-         ("drude_kufdtd", drude_kufdtd), ("tfsf_kufdtd", tfsf_kufdtd), ("output_kufdtd", output_kufdtd))
+         ("drude_kufdtd", drude_kufdtd), ("tfsf_kufdtd", tfsf_kufdtd), ("output_kufdtd", output_kufdtd),
+         ("cpml_kappa_kufdtd", cpml_kappa_kufdtd))
 
 
 def main():

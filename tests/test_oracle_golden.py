@@ -3,7 +3,8 @@
 The fixtures in tests/golden/ were produced by tests/golden/make_golden.py
 from the reference's NumPy step (2nd_order-Yee/Numpy/fdtd3d.py), the KEMP
 SSE/OpenMP core (KEMP/v0.7_pml/fdtd3d/cpu/src/core.c), the kuFDTD CPML C
-routines (kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c) and the 4th-order C
+routines (kuFDTD/v0.2.0/dim3/cpu/core/cpml_non_kappa.c), the kappa CPML
+(kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c) and the 4th-order C
 extension (4th_order-Symplectic/Python-C/dielectric.c).
 """
 import os
@@ -95,6 +96,69 @@ def test_oracle_cpml_matches_kufdtd_bit_exact(golden_dir):
         for arr, k in zip(upd, comps):
             np.testing.assert_array_equal(arr[fm], d[t + "out_" + k][fm], err_msg="case %d %s" % (n, k))
         for r in range(2):
+            np.testing.assert_array_equal(psi[2 * axis + r][pm], d[t + "psi_out%d" % r][pm],
+                                          err_msg="case %d psi%d" % (n, r))
+
+
+def test_oracle_kappa_cpml_matches_kufdtd(golden_dir):
+    """The kappa CPML (kappa_max = 5) against the reference's own update_cpml_3d
+    (kuFDTD/before_CUDA/v0.3.0/boundary/core/cpml_core.c:238-265) on every axis,
+    both faces, E and H.  psi = b psi + a d is single precision in both and
+    must agree bit for bit.  The field correction differs in rounding: the
+    reference evaluates cb ((1./kappa - 1) d + ds psi) in double (the literal
+    1. promotes the expression) and rounds once when it adds the result to
+    the float field, while the restatement (and every kernel) rounds each
+    single-precision operation with km1 = 1/kappa - 1 rounded once from FP64.
+    With the correction's terms of size c |km1 d| and c |psi| (their own
+    roundings and the two km1 values differ by a few ulp of those terms), the
+    bound per element is 4 ulp of the field plus 8 eps c_max (|km1|_max
+    2 |base|_max + |psi|_max): a wrong sign, pairing or grouping of the kappa
+    term would miss it by five orders of magnitude."""
+    d = _load(golden_dir, "cpml_kappa_kufdtd")
+    f32 = np.float32
+    for n in range(int(d["ncases"])):
+        t = "c%d_" % n
+        axis, which, back, P = (int(v) for v in d[t + "meta"])
+        npml = [0, 0, 0]
+        npml[axis] = P
+        faces = 1 << (2 * axis + back)
+        tables = {}
+        for w in ("e", "h"):
+            for name, key in (("b", "tb"), ("a", "ta"), ("km1", "tkm1")):
+                tables["%s_%s" % (name, w)] = [d[t + key] if a == axis else None for a in range(3)]
+        psi = [None] * 6
+        psi[2 * axis] = d[t + "psi_in0"].copy()
+        psi[2 * axis + 1] = d[t + "psi_in1"].copy()
+        E = [d[t + "in_" + k].copy() for k in NAMES[:3]]
+        H = [d[t + "in_" + k].copy() for k in NAMES[3:]]
+        if which == 0:
+            oracle.cpml_e(npml, faces, tables, *E, *H, *(d[t + "in_" + k] for k in ("cex", "cey", "cez")), psi)
+            upd, comps = E, NAMES[:3]
+        else:
+            oracle.cpml_h(npml, faces, tables, *E, *H, psi)
+            upd, comps = H, NAMES[3:]
+        base = E if which else H
+        base_max = max(float(np.abs(x).max()) for x in base)
+        psi_max = max(float(np.abs(psi[2 * axis + r]).max()) for r in range(2))
+        km1_max = float(np.abs(d[t + "tkm1"]).max())
+        c_max = 0.5 if which else max(float(np.abs(d[t + "in_" + k]).max()) for k in ("cex", "cey", "cez"))
+        slack = 8 * np.finfo(f32).eps * c_max * (km1_max * 2 * base_max + psi_max)
+        checked = 0
+        for arr, k in zip(upd, comps):
+            m = d[t + "fmask_" + k]
+            if not m.any():
+                continue
+            ref_out, ref_in = d[t + "out_" + k][m], d[t + "in_" + k][m]
+            corr = np.abs(ref_out.astype(np.float64) - ref_in)
+            bound = 4 * np.spacing(np.maximum(np.abs(ref_out), np.abs(ref_in))) + slack
+            err = np.abs(arr[m].astype(np.float64) - ref_out)
+            assert (err <= bound).all(), "case %d %s: %g > bound" % (n, k, (err - bound).max())
+            assert corr.max() > 1e3 * slack, "case %d %s: the kappa correction is not exercised" % (n, k)
+            checked += 1
+        assert checked == 2, n
+        for r in range(2):
+            pm = d[t + "pmask%d" % r]
+            assert pm.any()
             np.testing.assert_array_equal(psi[2 * axis + r][pm], d[t + "psi_out%d" % r][pm],
                                           err_msg="case %d psi%d" % (n, r))
 

@@ -25,7 +25,8 @@ Other workloads (each prints its own line; the default is the headline):
 reference's own C cannot be built on the benchmark host (SSE intrinsics,
 Python-2 extension API), so the C oracle -- a line-by-line restatement of
 the reference's CPU arithmetic, OpenMP over all host threads -- stands in
-(kind "port"), on a bounded sample of the same workload.
+(kind "port"), on the same 1024 x 1024 x 512 workload (W untimed and K timed
+steps; a 256-plane slice only when the host lacks memory for the full grid).
 
 N > 1: the path has no exchange step on one GPU per box (replicas only);
 each rank runs an independent replica and `value` sums over ranks.
@@ -52,8 +53,7 @@ NPML = 12
 FALLBACK_HBM_GBS = 6790.7
 # DRAM bytes per cell-step of one time step (the fused kernel and the two z-band
 # kernels: dram__bytes_read.sum + dram__bytes_write.sum over the three launches of a
-# step / cells), from an ncu launch list of this workload at full size;
-# see profiles/k_yee_fused_cpml1024.md.
+# step / cells), from an ncu capture of this workload at full size.
 NCU_DRAM_BYTES_PER_CELL = 75.2
 
 
@@ -136,32 +136,104 @@ class ClockSampler:
                 "samples": len(sms)}
 
 
-def cpu_oracle_sample(seconds=12.0, sample_shape=(256, 1024, 512)):
-    """Time the oracle (reference CPU arithmetic, OpenMP) on a bounded sample."""
+def _mem_available_bytes():
+    try:
+        with open("/proc/meminfo") as fh:
+            for line in fh:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def _cpu_sample_shape(shape):
+    """The workload's own grid when the host has room for the oracle's state
+    (9 field and coefficient arrays, psi slabs, a margin); else a 256-plane
+    slice of it."""
+    need = 10 * 4 * int(np.prod(shape)) * 1.3
+    avail = _mem_available_bytes()
+    if avail is None or avail >= need:
+        return tuple(shape), False
+    return (256,) + tuple(shape[1:]), True
+
+
+def workload_name(shape):
+    return ("Yee+CPML %dx%dx%d, 12-cell CPML (m=4, R=1e-8, kappa_max=5, alpha_max=0.05), "
+            "200 spheres eps_r U[1,12], 6 Gaussian dipoles" % tuple(shape))
+
+
+def cpu_oracle_run(shape=SHAPE, seconds=12.0, warmup=1, steps=None):
+    """Time the oracle (the reference's CPU arithmetic restated in C, OpenMP
+    over all host threads) on the workload: `warmup` untimed steps, then
+    `steps` timed steps, or as many as fit in `seconds` when steps is None."""
     import oracle
     from fdtd_accelerate_gb300 import configs
-    work = configs.scaled(configs.cpml1024(steps=4), sample_shape, steps=4)
+    sample_shape, sliced = _cpu_sample_shape(shape)
+    work = configs.cpml1024(steps=4)
+    if sample_shape != SHAPE:
+        work = configs.scaled(work, sample_shape, steps=4)
     ce = [c.numpy() for c in configs.ce_from_spheres(sample_shape, work.spheres)]
     tables = [oracle.cpml_tables(NPML) for _ in range(3)]
     tab = {k: [t[k] for t in tables] for k in tables[0]}
     f = {k: np.zeros(sample_shape, np.float32) for k in ("ex", "ey", "ez", "hx", "hy", "hz")}
     f.update(cex=ce[0], cey=ce[1], cez=ce[2])
-    srcs = [(c, ijk, a.astype(np.float32)) for c, ijk, a in work.source_list(1000)]
+    del ce
+    srcs = [(c, ijk, a.astype(np.float32)) for c, ijk, a in work.source_list(4000)]
     sim = oracle.OracleSim(f, (NPML,) * 3, 0x3F, tab, srcs)
     sim.tstep = 150
-    sim.step(1)  # warm-up (page faults, thread pool)
-    steps = 0
+    sim.step(max(1, warmup))  # warm-up (page faults, thread pool)
+    done = 0
     t0 = time.perf_counter()
     while True:
         sim.step(1)
-        steps += 1
+        done += 1
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 2000:
+        if (steps is not None and done >= steps) or (steps is None and (el >= seconds or done >= 2000)):
             break
     cells = int(np.prod(sample_shape))
-    return {"value": cells * steps / el / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": "oracle (C restatement of the reference CPU path, OpenMP %d threads) on a %dx%dx%d "
-                      "scaled copy of the workload, %d steps, %.1f s" % (os.cpu_count(), *sample_shape, steps, el)}
+    what = ("the workload itself (%dx%dx%d)" % sample_shape if not sliced else
+            "a %dx%dx%d slice of the workload (host memory short of the full grid)" % sample_shape)
+    return {"value": cells * done / el / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "ms_per_step": el / done * 1e3, "same_config": not sliced,
+            "sample": "oracle (C restatement of the reference CPU path, OpenMP %d threads) on %s, %d steps "
+                      "after %d warm-up, %.1f s" % (os.cpu_count(), what, done, max(1, warmup), el)}
+
+
+def accuracy_summary(errs, steps, what):
+    """FP32-vs-FP64 distance of a run (fp64.family_errors output) for a JSON line."""
+    return {"steps": steps, "vs": what,
+            "max_family_rel": max(e["max"] for e in errs.values()),
+            "rms_family_rel": max(e["rms"] for e in errs.values()),
+            "per_component": {k: {"max": round(e["max"], 9), "rms": round(e["rms"], 9)} for k, e in errs.items()},
+            "metric": "per component: max |fp32 - fp64| / max |fp64| over its field family (E or H), and the "
+                      "root-mean-square ratio; the line reports the largest over components"}
+
+
+def cpml1024_accuracy(shape, steps, dev):
+    """The workload run from zero for `steps` steps by the fused FP32 path and by
+    the FP64 step on the GPU (FP32 coefficients, tables, amplitudes widened)."""
+    import torch
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs
+    from fdtd_accelerate_gb300.fp64 import YeeRun64, family_errors
+    work = configs.cpml1024(steps=steps, npml=NPML)
+    if shape != SHAPE:
+        work = configs.scaled(work, shape, steps=steps)
+    ce = configs.ce_from_spheres(shape, work.spheres, device=dev)
+    src = work.source_list(steps + 2)
+    s32 = F.YeeSolver(shape, ce=ce, npml=NPML, sources=src, device=dev)
+    s32.step(steps)
+    s64 = YeeRun64(shape, ce=ce, npml=NPML, sources=src, device=dev)
+    del ce
+    s64.step(steps)
+    torch.cuda.synchronize()
+    s32.check_status()
+    errs = family_errors(s32.fields, s64.fields)
+    s32.close()
+    del s32, s64
+    torch.cuda.empty_cache()
+    return accuracy_summary(errs, steps, "FP64 step on the GPU (fdtd_step_unfused_f64), same inputs")
 
 
 def max_over_ranks(x, device):
@@ -177,16 +249,18 @@ def max_over_ranks(x, device):
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores, on the same workload and
+    grid as our arm: W untimed steps, then K timed steps."""
     if rank != 0:
         return
-    base = cpu_oracle_sample(seconds=max(3.0, min(20.0, 2.0 * args.steps)))
+    base = cpu_oracle_run(shape=args.shape, warmup=args.warmup, steps=args.steps)
     line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded spheres/dipoles)", "impl": "reference",
-            "config": {"workload": "Yee+CPML %dx%dx%d, 12-cell CPML, 200 spheres, 6 dipoles (bounded CPU sample)"
-                                   % SHAPE},
-            "cpu_baseline": base,
+            "data": "synthetic (seeded spheres and dipoles, normalised units)", "impl": "reference",
+            "config": {"workload": workload_name(args.shape), "cells": int(np.prod(args.shape)),
+                       "same_config": base["same_config"]},
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
@@ -209,6 +283,7 @@ def run_ours(args, rank, world):
     del ce
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
+    info = solver.plan_info()
 
     for _ in range(args.warmup):
         solver.step(1)
@@ -268,6 +343,13 @@ def run_ours(args, rank, world):
                        "memory, %d fused steps, D2H of the fields" % (args.steps, args.steps)}
         del host_f, host_ce
 
+    accuracy = None
+    if args.accuracy_steps and world == 1:
+        solver.close()
+        del solver
+        torch.cuda.empty_cache()
+        accuracy = cpml1024_accuracy(shape, args.accuracy_steps, dev)
+
     if rank != 0:
         return
     alg = algorithmic_bytes_per_step(shape, NPML)
@@ -279,14 +361,12 @@ def run_ours(args, rank, world):
         line_note = "scaled workload %dx%dx%d (not the headline size)" % tuple(shape)
     else:
         line_note = None
-    info = solver.plan_info()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded spheres and dipoles, normalised units)",
-        "config": {"workload": "Yee+CPML %dx%dx%d, 12-cell CPML (m=4, R=1e-8, kappa_max=5, alpha_max=0.05), "
-                               "200 spheres eps_r U[1,12], 6 Gaussian dipoles" % tuple(shape),
+        "config": {"workload": workload_name(shape),
                    "cells": cells, "l2": "state 33 GB >> L2 (no flush needed)",
                    "kernel": "k_yee_fused (TMA 3-D boxes, ping-pong state)" +
                              (" + k_zband_e + k_zband_h (z-slab CPML)" if info["z_band"] else ""),
@@ -304,8 +384,11 @@ def run_ours(args, rank, world):
     }
     if line_note:
         line["config"]["note"] = line_note
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_oracle_sample(seconds=args.cpu_seconds)
+        base = cpu_oracle_run(shape=shape, seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
 
 
@@ -384,14 +467,7 @@ def run_symp512(args):
     from fdtd_accelerate_gb300 import configs, symplectic
     dev = torch.device("cuda", 0)
     shape, npml = tuple(args.symp_shape), 10
-    rng = np.random.default_rng(20261206)
-    spheres = configs.random_spheres(rng, shape, 60, 5, 40, 1.0, 4.0)
-    ce = [(c * np.float32(symplectic.COURANT / 24 / 0.5)) for c in configs.ce_from_spheres(shape, spheres, device=dev)]
-    src = [("ez", tuple(n // 2 for n in shape),
-            lambda t: float(np.sin(2 * np.pi * 0.05 * t) * np.exp(-0.5 * ((t - 150.0) / 30.0) ** 2)))]
-    s = symplectic.SymplecticSolver(shape, ce=ce, npml=npml, sources=src, device=dev,
-                                    max_steps=args.warmup + args.steps + 2)
-    del ce
+    s = configs.symp512_solver(shape, device=dev, max_steps=args.warmup + args.steps + 2, npml=npml)
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
         s.step(1)
@@ -408,6 +484,20 @@ def run_symp512(args):
     # per step: 5 H stages and 4 E stages, one launch each (the CPML slabs in the same
     # launch), and the source kernel after each E stage
     per_step = 5 + 4 * 2
+    accuracy = None
+    if args.accuracy_steps:
+        from fdtd_accelerate_gb300.fp64 import SympRun64, family_errors
+        del s
+        torch.cuda.empty_cache()
+        s32 = configs.symp512_solver(shape, device=dev, max_steps=args.accuracy_steps + 2, npml=npml)
+        r64 = SympRun64(s32)
+        s32.step(args.accuracy_steps)
+        r64.step(args.accuracy_steps)
+        torch.cuda.synchronize()
+        accuracy = accuracy_summary(family_errors(s32.fields, r64.fields), args.accuracy_steps,
+                                    "FP64 twin of the stage kernels on the GPU (fdtd_symplectic_stage_f64), same inputs")
+        del s32, r64
+        torch.cuda.empty_cache()
     line = _base_line("Mcell-updates/s (4th-order symplectic %dx%dx%d, 10-cell CPML, FP32)" % shape, cells / (avg / 1e3) / 1e6,
                       UNIT, args, avg, "f32", "4th-order symplectic %dx%dx%d, 10-cell CPML, 60 spheres eps_r " % shape +
                       "U[1,4], Ez dipole; 4 E + 5 H stages per step, one launch per stage with its CPML "
@@ -418,6 +508,8 @@ def run_symp512(args):
                                     "scope": "one time step, stage by stage (372 B/cell + 144 B per slab cell)",
                                     "frac_of_fused_step_bytes": alg_fused / (avg / 1e3) / 1e9 / peak},
                        "clocks": clocks, "gpu_launches": args.steps * per_step})
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     print(json.dumps(line), flush=True)
 
 
@@ -685,9 +777,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the FP32-vs-FP64 accuracy run reported in the line (default: the workload's "
+                         "own count, 2000 for cpml1024, 1000 for symp512; 0 skips it)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.accuracy_steps is None:
+        args.accuracy_steps = {"cpml1024": 2000, "symp512": 1000}.get(args.workload, 0)
     if args.steps is None:
         args.steps = {"cpml1024": 200, "plain128": 1000, "symp512": 50, "batched64": 500,
                       "adjoint256": 3000, "drude512": 100, "tfsf512": 100}[args.workload]

@@ -30,7 +30,7 @@ import torch
 from .sources import gaussian_sine
 
 __all__ = ["Workload", "plain128", "cpml1024", "batched64", "adjoint256", "scaled", "paint_spheres", "ce_from_spheres",
-           "random_spheres", "random_dipoles", "STAGGER"]
+           "random_spheres", "random_dipoles", "symp512_solver", "STAGGER"]
 
 # offsets of (ex, ey, ez) sample points from (i, j, k)
 STAGGER = ((0.0, 0.5, 0.5), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0))
@@ -144,6 +144,21 @@ def adjoint256(steps=3000, shape=(256, 256, 128), region=(128, 128, 64), npml=12
     return AdjointWorkload("adjoint %dx%dx%d, %d-cell CPML, design %dx%dx%d eps U[1,12], Ez line source, "
                            "%d Ez probes, %d steps" % (*shape, npml, *region, nprobes, steps),
                            tuple(shape), steps, npml, eps, design, sources, [("ez", p) for p in probes], segment)
+
+
+def symp512_solver(shape=(512, 512, 512), device="cuda", max_steps=0, npml=10, seed=20261206):
+    """The 4th-order workload: 512^3, 10-cell CPML, 60 seeded spheres (radius
+    5..40, eps_r U[1,4]), ce = (S/24)/eps_r, ch = S/24, an Ez dipole at the
+    centre with the Gaussian-modulated sine (f dt = 0.05, width 30, t0 = 150)
+    evaluated at the stage times."""
+    from .symplectic import COURANT, SymplecticSolver
+    shape = tuple(shape)
+    rng = np.random.default_rng(seed)
+    spheres = random_spheres(rng, shape, 60, 5, 40, 1.0, 4.0)
+    ce = [(c * np.float32(COURANT / 24 / 0.5)) for c in ce_from_spheres(shape, spheres, device=device)]
+    src = [("ez", tuple(n // 2 for n in shape),
+            lambda t: float(np.sin(2 * np.pi * 0.05 * t) * np.exp(-0.5 * ((t - 150.0) / 30.0) ** 2)))]
+    return SymplecticSolver(shape, ce=ce, npml=npml, sources=src, device=device, max_steps=max_steps)
 
 
 def scaled(work, shape, steps=None):

@@ -228,6 +228,17 @@ int fdtd_step_unfused_f64(const fdtd_grid *gp, double *const f[6], const double 
     return check_launch();
 }
 
+int fdtd_add_sources_f64(const fdtd_grid *gp, const fdtd_sources *src, int64_t t, double *ex, double *ey,
+                         double *ez, void *stream) {
+    Grid g;
+    FDTD_TRY(validate_grid(gp, &g));
+    if (!src || src->nsrc < 0 || src->namp < 0) return FDTD_ERR_ARG;
+    if (src->nsrc == 0) return FDTD_OK;
+    if (!all_nonnull(src->ijk, src->comp, src->amp, ex, ey, ez)) return FDTD_ERR_ARG;
+    k_sources<<<1, 32, 0, as_stream(stream)>>>(g, *src, t, ex, ey, ez);
+    return check_launch();
+}
+
 int fdtd_gather_points_f64(const fdtd_grid *gp, const fdtd_points *pts, const double *const f[6], double *out,
                            void *stream) {
     Grid g;

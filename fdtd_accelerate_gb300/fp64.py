@@ -1,4 +1,5 @@
-"""FP64 run of the 2nd-order Yee step on the GPU (fdtd_step_unfused_f64).
+"""FP64 runs on the GPU: the 2nd-order Yee step (fdtd_step_unfused_f64) and
+the 4th-order symplectic stages (fdtd_symplectic_stage_f64).
 
 The same step as YeeSolver (update_e, cpml_e, sources, update_h, cpml_h, in
 the reference's operation order) evaluated in double precision.  The CPML
@@ -16,7 +17,7 @@ from . import _native as N
 from .cpml import CpmlLayer
 from .sources import PointSources
 
-__all__ = ["YeeRun64"]
+__all__ = ["YeeRun64", "SympRun64", "family_errors"]
 
 COMPONENTS6 = ("ex", "ey", "ez", "hx", "hy", "hz")
 
@@ -100,3 +101,87 @@ class YeeRun64:
         out = torch.zeros((nsteps, max(self.nmon, 1)), dtype=torch.float64, device=self.device)
         self.step(nsteps, out)
         return out[:, :self.nmon]
+
+
+class SympRun64:
+    """FP64 twin of a SymplecticSolver (fdtd_symplectic_stage_f64): the same
+    stages, CPML and sources in double precision on the GPU, with the FP32
+    solver's coefficients, CPML tables and source amplitudes widened, so the
+    two runs discretise the same problem.  Build it from the solver whose
+    accuracy it measures; its fields start at zero."""
+
+    def __init__(self, solver):
+        self.src32 = solver
+        self.shape = solver.shape
+        self.device = solver.device
+        dev = self.device
+        self.f = torch.zeros((6,) + self.shape, dtype=torch.float64, device=dev)
+        self.ce = torch.stack([c.double() for c in solver.ce])
+        if isinstance(solver.ch, float):
+            self.ch_arrays = None
+            self.ch = float(np.float32(solver.ch))
+        else:
+            self.ch_arrays = torch.stack([c.double() for c in solver.ch])
+            self.ch = 0.0
+        cp = solver.cpml
+        self.psi_e = [torch.zeros_like(t, dtype=torch.float64) if t is not None else None for t in cp.psi_e]
+        self.psi_h = [torch.zeros_like(t, dtype=torch.float64) if t is not None else None for t in cp.psi_h]
+        self.tstep = solver.tstep
+
+    @property
+    def fields(self):
+        return dict(zip(COMPONENTS6, self.f))
+
+    def step(self, n=1):
+        from .symplectic import CL, DL
+        s = self.src32
+        if s.src_spec and self.tstep + n > s._src_steps:
+            s._build_sources(self.tstep + n)
+        nx, ny, nz = self.shape
+        g = N.Grid(nx, ny, nz, ny * nz, nz)
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        f = (C.c_void_p * 6)(*[self.f[q].data_ptr() for q in range(6)])
+        ce = (C.c_void_p * 3)(*[self.ce[q].data_ptr() for q in range(3)])
+        ch = (C.c_void_p * 3)(*[self.ch_arrays[q].data_ptr() for q in range(3)]) if self.ch_arrays is not None else None
+        pe = (C.c_void_p * 6)(*map(ptr, self.psi_e))
+        ph = (C.c_void_p * 6)(*map(ptr, self.psi_h))
+        active = s.cpml.active
+        src = s._src.struct()
+        L = N.lib()
+        w32 = lambda v: float(np.float32(v))   # the FP32 path's coefficient, widened
+
+        def stage(e_or_h, coef, cf, psi, chv):
+            cp = C.byref(s.cpml._structs[coef]) if active else None
+            st = L.fdtd_symplectic_stage_f64(C.byref(g), cp, int(e_or_h), w32(coef), chv, f, cf,
+                                             psi if active else None, stream)
+            if st:
+                N.check(st, "fdtd_symplectic_stage_f64")
+
+        with torch.cuda.device(self.device):
+            stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            for _ in range(n):
+                tn = self.tstep
+                for sn in range(4):
+                    stage(0, CL[sn], ch, ph, self.ch)
+                    stage(1, DL[sn], ce, pe, 0.0)
+                    if s.src_spec:
+                        N.call("fdtd_add_sources_f64", C.byref(g), C.byref(src), 4 * tn + sn,
+                               *[C.c_void_p(self.f[q].data_ptr()) for q in range(3)], stream)
+                stage(0, CL[4], ch, ph, self.ch)
+                self.tstep += 1
+
+
+def family_errors(f32, f64):
+    """Distance of an FP32 run to its FP64 twin, per component: max |a - b| and
+    the root-mean-square |a - b|, each divided by the largest |b| (resp. the
+    root-mean-square |b|) of the component's field family (E or H).
+    Per-component normalisation is meaningless for a component that is zero
+    in exact arithmetic (its FP64 value is roundoff)."""
+    out = {}
+    for fam in (COMPONENTS6[:3], COMPONENTS6[3:]):
+        vmax = max(float(f64[k].abs().max()) for k in fam)
+        vrms = (sum(float((f64[k] ** 2).sum()) for k in fam) / sum(f64[k].numel() for k in fam)) ** 0.5
+        for k in fam:
+            d = f32[k].double() - f64[k]
+            out[k] = {"max": float(d.abs().max()) / vmax, "rms": float((d ** 2).mean()) ** 0.5 / vrms}
+    return out

@@ -55,7 +55,8 @@ def test_reference_arm_under_torchrun_two_ranks():
     build()  # the reference arm times the oracle, built with the library
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
-           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1"]
+           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1",
+           "--shape", "64,48,40"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -63,3 +64,4 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["config"]["same_config"] and d["config"]["cells"] == 64 * 48 * 40

@@ -84,16 +84,17 @@ def test_fp64_step_bit_exact_vs_fp64_oracle():
         np.testing.assert_array_equal(run.psi_h[q].cpu().numpy(), sim.psi_h[q], err_msg="psi_h%d" % q)
 
 
-def test_cpml_workload_fp32_vs_fp64():
-    """The C2 workload scaled to 512x512x256 (12-cell CPML, spheres, dipoles),
-    2000 steps: the fused FP32 path against the GPU FP64 step, same inputs.
-    Reported per field family as max |a - b| / max |b|."""
+def test_cpml1024_workload_fp32_vs_fp64_full_size():
+    """The Yee + CPML workload at its own size (1024 x 1024 x 512, 12-cell CPML,
+    200 spheres, 6 dipoles), 2000 steps: the fused FP32 path against the GPU
+    FP64 step, same inputs (FP32 coefficients, tables and amplitudes widened).
+    Per field family: max |a - b| / max |b| and the root-mean-square ratio."""
     import fdtd_accelerate_gb300 as F
     from fdtd_accelerate_gb300 import configs
-    from fdtd_accelerate_gb300.fp64 import YeeRun64
+    from fdtd_accelerate_gb300.fp64 import YeeRun64, family_errors
     F.build()
-    shape, nsteps = (512, 512, 256), 2000
-    work = configs.scaled(configs.cpml1024(steps=nsteps), shape)
+    work = configs.cpml1024(steps=2000)
+    shape, nsteps = work.shape, work.steps
     ce = configs.ce_from_spheres(shape, work.spheres, device="cuda")
     src = work.source_list(nsteps + 2)
     s32 = F.YeeSolver(shape, ce=ce, npml=12, sources=src)
@@ -103,13 +104,96 @@ def test_cpml_workload_fp32_vs_fp64():
     s64.step(nsteps)
     torch.cuda.synchronize()
     s32.check_status()
-    errs = {}
-    for fam in (NAMES[:3], NAMES[3:]):
-        scale = max(float(s64.fields[k].abs().max()) for k in fam)
-        for k in fam:
-            errs[k] = float((s32.fields[k].double() - s64.fields[k]).abs().max()) / scale
-    print("cpml workload 512x512x256, %d steps, FP32 vs FP64 (family-normalised):" % nsteps,
-          ", ".join("%s %.2e" % (k, errs[k]) for k in NAMES))
+    errs = family_errors(s32.fields, s64.fields)
+    print("cpml workload 1024x1024x512, %d steps, FP32 vs FP64 (family-normalised max / rms):" % nsteps,
+          ", ".join("%s %.2e / %.2e" % (k, errs[k]["max"], errs[k]["rms"]) for k in NAMES))
     # The FP32 path equals the reference's FP32 arithmetic bit for bit; this is
-    # that arithmetic's distance to FP64 (measured 6e-5..1.1e-4 for E, 1e-5 for H).
-    assert max(errs.values()) < 3e-4, errs
+    # that arithmetic's distance to FP64 at the workload's size and step count.
+    assert max(e["max"] for e in errs.values()) < 3e-4, errs
+    assert max(e["rms"] for e in errs.values()) < 1e-4, errs
+
+
+def _symp_oracle64(S, shape, ce32, npml, faces, src, init, nsteps):
+    """The FP64 oracle stepping the 4th-order scheme with the FP32 path's
+    constants widened: coefficients, uniform ch, CPML tables, amplitudes."""
+    w = lambda v: np.float64(np.float32(v))
+    f = {k: init[k].astype(np.float64) for k in NAMES}
+    ce = [c.astype(np.float64) for c in ce32]
+    ch = w(S.COURANT / 24.0)
+    tables = {}
+    for coef in set(S.CL) | set(S.DL[:4]):
+        t = [oracle.symp_stage_tables(p, coef, S.COURANT) if p else None for p in npml]
+        tables[coef] = {k: [x[k].astype(np.float32).astype(np.float64) if x is not None else None for x in t]
+                        for k in ("b_e", "a_e", "km1_e", "b_h", "a_h", "km1_h")}
+    nx, ny, nz = shape
+    ps = [(2 * npml[0], ny, nz), (nx, 2 * npml[1], nz), (nx, ny, 2 * npml[2])]
+    psi_e = [np.zeros(ps[a]) if npml[a] else None for a in range(3) for _ in range(2)]
+    psi_h = [np.zeros(ps[a]) if npml[a] else None for a in range(3) for _ in range(2)]
+    pml = any(npml)
+
+    def h_stage(cl):
+        oracle.symp_h_scalar(w(cl), ch, *(f[k] for k in NAMES))
+        if pml:
+            oracle.symp_cpml_h(npml, faces, w(cl), ch, tables[cl], *(f[k] for k in NAMES), psi_h)
+
+    for tn in range(1, nsteps + 1):
+        for sn in range(4):
+            h_stage(S.CL[sn])
+            oracle.symp_e(w(S.DL[sn]), *(f[k] for k in NAMES), *ce)
+            if pml:
+                oracle.symp_cpml_e(npml, faces, w(S.DL[sn]), tables[S.DL[sn]], *(f[k] for k in NAMES), *ce, psi_e)
+            for comp, (i, j, k), amp in src:
+                f[comp][i, j, k] = f[comp][i, j, k] + w(amp(tn + sn / 5.0))
+        h_stage(S.CL[4])
+    return f, psi_e, psi_h
+
+
+def test_symplectic_fp64_stage_bit_exact_vs_fp64_oracle():
+    """The GPU FP64 4th-order stages (fdtd_symplectic_stage_f64, SympRun64)
+    equal the FP64 C oracle bit for bit: CPML on all faces, a source, spheres,
+    random initial state."""
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs, symplectic as S
+    from fdtd_accelerate_gb300.fp64 import SympRun64
+    F.build()
+    shape, npml, nsteps = (26, 22, 30), 4, 4
+    rng = np.random.default_rng(31)
+    spheres = configs.random_spheres(rng, shape, 4, 2, 5, 1.0, 4.0)
+    ce32 = [(c.numpy() * np.float32(S.COURANT / 24 / 0.5)).astype(np.float32)
+            for c in configs.ce_from_spheres(shape, spheres)]
+    amp = lambda t: np.sin(0.3 * t) * np.exp(-0.5 * ((t - 3.0) / 2.0) ** 2)
+    src = [("ez", (13, 11, 15), amp)]
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    s32 = S.SymplecticSolver(shape, ce=ce32, npml=npml, sources=src, max_steps=nsteps + 2)
+    r64 = SympRun64(s32)
+    for q, k in enumerate(NAMES):
+        r64.f[q].copy_(torch.from_numpy(init[k].astype(np.float64)))
+    r64.step(nsteps)
+    torch.cuda.synchronize()
+    f, psi_e, psi_h = _symp_oracle64(S, shape, ce32, (npml,) * 3, 0x3F, src, init, nsteps)
+    for q, k in enumerate(NAMES):
+        np.testing.assert_array_equal(r64.f[q].cpu().numpy(), f[k], err_msg=k)
+    for q in range(6):
+        np.testing.assert_array_equal(r64.psi_e[q].cpu().numpy(), psi_e[q], err_msg="psi_e%d" % q)
+        np.testing.assert_array_equal(r64.psi_h[q].cpu().numpy(), psi_h[q], err_msg="psi_h%d" % q)
+
+
+def test_symp512_workload_fp32_vs_fp64_full_size():
+    """The 4th-order workload at its own size (512^3, 10-cell CPML, 60 spheres
+    eps_r U[1,4], centred Ez dipole), 1000 steps: the FP32 stage kernels against
+    their FP64 twin on the GPU.  Per field family: max |a - b| / max |b| and
+    the root-mean-square ratio."""
+    import fdtd_accelerate_gb300 as F
+    from fdtd_accelerate_gb300 import configs
+    from fdtd_accelerate_gb300.fp64 import SympRun64, family_errors
+    F.build()
+    s32 = configs.symp512_solver(device="cuda", max_steps=1002)
+    r64 = SympRun64(s32)
+    s32.step(1000)
+    r64.step(1000)
+    torch.cuda.synchronize()
+    errs = family_errors(s32.fields, r64.fields)
+    print("symp512 workload, 1000 steps, FP32 vs FP64 (family-normalised max / rms):",
+          ", ".join("%s %.2e / %.2e" % (k, errs[k]["max"], errs[k]["rms"]) for k in NAMES))
+    assert max(e["max"] for e in errs.values()) < 3e-4, errs
+    assert max(e["rms"] for e in errs.values()) < 1e-4, errs

@@ -67,6 +67,18 @@ def algorithmic_bytes_per_step(shape, npml):
     return cells * 60 + slab_cells * 32
 
 
+def symplectic_pair_bytes_per_step(shape, npml):
+    """FP32 traffic of one 4th-order step taken as four fused stage-pair passes
+    (each H stage with the E stage after it: fields read and written, E
+    coefficients read = 60 B/cell; the closing H stage of a step merged into the
+    next pass), plus per pass two E psi and two H psi values read and written
+    on every slab cell (32 B x 4)."""
+    nx, ny, nz = shape
+    cells = nx * ny * nz
+    slab_cells = 2 * npml * (ny * nz + nx * nz + nx * ny) if npml else 0
+    return cells * 4 * 60 + slab_cells * 4 * 32
+
+
 def symplectic_bytes_per_step(shape, npml):
     """Algorithmic FP32 traffic of one 4th-order symplectic step taken stage by
     stage (5 H stages: E read, H read+written = 36 B/cell; 4 E stages: H read,
@@ -467,23 +479,34 @@ def run_symp512(args):
     from fdtd_accelerate_gb300 import configs, symplectic
     dev = torch.device("cuda", 0)
     shape, npml = tuple(args.symp_shape), 10
-    s = configs.symp512_solver(shape, device=dev, max_steps=args.warmup + args.steps + 2, npml=npml)
+    s = configs.symp512_solver(shape, device=dev, max_steps=args.warmup + args.steps + 2, npml=npml,
+                               fused=args.symp_fused)
     stream = torch.cuda.current_stream(dev)
-    for _ in range(args.warmup):
-        s.step(1)
+    s.step(args.warmup)
+    torch.cuda.synchronize()
     sampler = ClockSampler(0)
     sampler.start()
-    ms = _timed_steps(torch, stream, lambda: s.step(1), args.steps)
+    # one run of K steps, as a simulation advances (consecutive steps share a
+    # pass: the closing H stage of a step merges with the opening one of the next)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    s.step(args.steps)
+    b.record(stream)
+    torch.cuda.synchronize()
     clocks = sampler.stop()
-    avg = statistics.mean(ms)
+    s.check_status()
+    avg = a.elapsed_time(b) / args.steps
     cells = int(np.prod(shape))
     alg = symplectic_bytes_per_step(shape, npml)
+    alg_pair = symplectic_pair_bytes_per_step(shape, npml)
     alg_fused = algorithmic_bytes_per_step(shape, npml)
     peak, psrc = measured_peak()
     achieved = alg / (avg / 1e3) / 1e9
-    # per step: 5 H stages and 4 E stages, one launch each (the CPML slabs in the same
-    # launch), and the source kernel after each E stage
-    per_step = 5 + 4 * 2
+    pair = s.pair_path()
+    # launches: four stage-pair passes per step and the run's last H stage, or
+    # per step 5 H and 4 E stage launches and a source launch after each E stage
+    launches = 4 * args.steps + 1 if pair else args.steps * (5 + 4 * 2)
     accuracy = None
     if args.accuracy_steps:
         from fdtd_accelerate_gb300.fp64 import SympRun64, family_errors
@@ -500,14 +523,19 @@ def run_symp512(args):
         torch.cuda.empty_cache()
     line = _base_line("Mcell-updates/s (4th-order symplectic %dx%dx%d, 10-cell CPML, FP32)" % shape, cells / (avg / 1e3) / 1e6,
                       UNIT, args, avg, "f32", "4th-order symplectic %dx%dx%d, 10-cell CPML, 60 spheres eps_r " % shape +
-                      "U[1,4], Ez dipole; 4 E + 5 H stages per step, one launch per stage with its CPML "
-                      "slabs (6 fields + 3 coefficient arrays: %.1f GB >> L2)" % (9 * cells * 4 / 1e9),
+                      "U[1,4], Ez dipole; 4 E + 5 H stages per step, " +
+                      ("four fused stage-pair passes per step (k_symp_pair) in one %d-step run" % args.steps
+                       if pair else "one launch per stage with its CPML slabs") +
+                      " (6 fields + 3 coefficient arrays: %.1f GB >> L2)" % (9 * cells * 4 / 1e9),
                       {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                     "frac": achieved / peak, "traffic": None, "peak_source": psrc,
                                     "alg_bytes_per_launch": alg,
-                                    "scope": "one time step, stage by stage (372 B/cell + 144 B per slab cell)",
+                                    "scope": "one time step on the stage-by-stage byte count of the workload "
+                                             "(372 B/cell + 144 B per slab cell)",
+                                    "frac_of_pair_pass_bytes": alg_pair / (avg / 1e3) / 1e9 / peak,
+                                    "pair_pass_bytes_per_step": alg_pair,
                                     "frac_of_fused_step_bytes": alg_fused / (avg / 1e3) / 1e9 / peak},
-                       "clocks": clocks, "gpu_launches": args.steps * per_step})
+                       "clocks": clocks, "gpu_launches": launches})
     if accuracy is not None:
         line["accuracy"] = accuracy
     print(json.dumps(line), flush=True)
@@ -771,6 +799,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--symp-shape", type=lambda s: tuple(int(v) for v in s.split(",")), default=(512, 512, 512),
                     help="grid of --workload symp512 (a smaller one for profiling)")
+    ap.add_argument("--symp-fused", action="store_true",
+                    help="--workload symp512 on the fused stage-pair kernel instead of the per-stage kernels")
     ap.add_argument("--shape", type=lambda s: tuple(int(v) for v in s.split(",")), default=SHAPE,
                     help="grid (default 1024,1024,512); other sizes scale the same workload")
     ap.add_argument("--tile", type=lambda s: tuple(int(v) for v in s.split(",")), default=None)

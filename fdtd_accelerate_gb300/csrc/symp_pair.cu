@@ -9,22 +9,27 @@
 //   fdtd_symplectic_stage_f32(E, dl), sources,
 // with the same round-to-nearest operations, so the result is bit-identical.
 //
-// Design
+// Design (2.5-D blocking)
 //  * Ping-pong state: the pass reads buffer `cur` (E, H) and writes `1-cur`;
 //    the H psi slabs ping-pong too (halo H cells are recomputed from the
 //    input psi), the E psi slabs are updated in place (only their owner
 //    touches them).
-//  * A CTA owns TZ = 32 (z, one cell per lane) x TY = 16 (y) cells for a chunk
-//    of x planes and marches along x.  E_new(i) needs H_new on planes
-//    i-1 .. i+2 and rows/columns -1 .. +2 around the tile; H_new(m) needs the
-//    input E on planes m-2 .. m+1 and rows/columns -2 .. +1 around those.
-//    So plane p of the input arrives (3-D TMA boxes: E with a 3-row, 4-column
-//    halo, H with a 1-row halo, CE on the tile) and the CTA computes H_new(p-1)
-//    on (TY+3) x (TZ+3) cells into a 4-plane ring in shared memory, then
-//    E_new(p-3) on the tile.  Own H_new and E_new are stored as computed.
+//  * A CTA owns TZ = 32 (z) x TY = 16 (y) cells for a chunk of x planes and
+//    marches along x.  E_new(i) needs H_new on planes i-1 .. i+2 and on the
+//    rows/columns -1 .. +2 around the tile, so H_new is computed on
+//    (TY+3) x (TZ+3) cells: one thread per cell column (j, k), the 512 tile
+//    columns first, then the 153 halo columns.  Each thread keeps the x
+//    neighbours it needs in registers: the input E of planes m-2 .. m+1 for
+//    H_new(m), and its own H_new of planes i-1 .. i+2 for E_new(i).  Shared
+//    memory holds one plane with its y/z halo: input E boxes (4-slot ring),
+//    input H and CE boxes (3-slot rings, 3-D TMA, issued two planes ahead)
+//    and H_new (3-slot ring).
+//  * Iteration q: input plane p arrives; every thread computes H_new(p-1) at
+//    its column; tile threads then compute E_new(p-3).  One CTA barrier per
+//    iteration: H_new(p-1) is read by neighbours two iterations later.
 //  * Lane 0 of the last warp is the producer: it waits on the mbarriers and
-//    issues every copy two iterations ahead.  Every wait is bounded (1 s);
-//    on expiry the CTA records FDTD_ERR_TIMEOUT, drains its copies and stops.
+//    issues the copies.  Every wait is bounded (1 s); on expiry the CTA
+//    records FDTD_ERR_TIMEOUT, drains its copies and stops.
 #include <cuda.h>
 
 #include <algorithm>
@@ -42,8 +47,10 @@ constexpr int HOR = TY + 3;         // H box rows: j0-1 .. j0+TY+1
 constexpr int HNR = TY + 3;         // H_new rows: j0-1 .. j0+TY+1
 constexpr int HNC = TZ + 3;         // H_new columns: k0-1 .. k0+TZ+1
 constexpr int HNP = 36;             // H_new row pitch
-constexpr int NE = 6, NH = 3, NC = 3, NHN = 4;  // ring depths (E, H, CE inputs; H_new)
-constexpr int NCW = (HNR * HNC + 31) / 32;      // compute warps: one H_new cell per thread
+constexpr int NE = 4, NH = 3, NC = 3, NHN = 3;  // ring depths (E, H, CE inputs; H_new)
+constexpr int NOWN = TY * TZ;                   // tile columns (threads 0 .. NOWN-1)
+constexpr int NHALO = HNR * HNC - NOWN;         // halo H columns
+constexpr int NCW = (NOWN + NHALO + 31) / 32;   // compute warps
 constexpr int THREADS = (NCW + 1) * 32;         // + the producer warp
 constexpr int MAX_SRC = 64;                     // sources per work item
 constexpr uint64_t WAIT_NS = 1000000000ull;
@@ -100,14 +107,16 @@ __device__ __forceinline__ void mbar_expect(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+// try_wait with a suspend-time hint: the waiting thread sleeps (up to the hint)
+// until the phase completes instead of spinning on issue slots
 __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
         : "memory");
     return ok != 0;
 }
@@ -155,6 +164,14 @@ __device__ __forceinline__ float sterm(const Axis &A, int s, float &psi, float d
     psi = fadd(fmul(A.b[s], psi), fmul(A.a[s], d));
     return fmul(fmul(coef, cv), fadd(fmul(A.km1[s], d), psi));
 }
+// 4th-order difference of an H node: 27 (F0 - Fm1) - (Fp1 - Fm2)
+__device__ __forceinline__ float d4h(float fm2, float fm1, float f0, float fp1) {
+    return fsub(fmul(27.0f, fsub(f0, fm1)), fsub(fp1, fm2));
+}
+// 4th-order difference of an E node: 27 (Fp1 - F0) - (Fp2 - Fm1)
+__device__ __forceinline__ float d4e(float fm1, float f0, float fp1, float fp2) {
+    return fsub(fmul(27.0f, fsub(fp1, f0)), fsub(fp2, fm1));
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
 k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
@@ -177,14 +194,33 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         s_abort = 0;
     }
-    // H_new cell of this thread (flat index over HNR x HNC) and E cell (warps 0..TY-1)
-    const int hf = tid, hr = hf / HNC, hc = hf - hr * HNC;
-    const bool h_thread = hf < HNR * HNC;
-    const bool e_thread = warp < TY;
+    // the H_new column (hr, hc) of this thread: tile columns first (warp = row,
+    // lane = column), then the halo: rows j0-1, j0+TY, j0+TY+1, then the
+    // columns k0-1, k0+TZ, k0+TZ+1 of the tile rows
+    int hr = 0, hc = 0;
+    const bool e_thread = tid < NOWN, h_thread = tid < NOWN + NHALO;
+    if (e_thread) {
+        hr = warp + 1;
+        hc = lane + 1;
+    } else if (h_thread) {
+        const int h = tid - NOWN;
+        if (h < 3 * HNC) {
+            const int band = h / HNC;
+            hr = band == 0 ? 0 : TY + band;
+            hc = h - band * HNC;
+        } else {
+            const int g = (h - 3 * HNC) / TY;
+            hr = 1 + (h - 3 * HNC) - g * TY;
+            hc = g == 0 ? 0 : TZ + g;
+        }
+    }
+    const int eo = (hr + 2) * BW + hc + 3;   // E box element of the column (row j0-3.., column k0-4..)
+    const int ho = hr * BW + hc + 3;         // H box element (row j0-1..)
+    const int no = hr * HNP + hc;            // H_new element (row j0-1.., column k0-1..)
+    const int co = warp * TZ + lane;         // CE element (tile threads)
 
-    uint32_t gE = 0, gH = 0, gC = 0;  // planes issued on each ring before the current item
+    uint32_t gE = 0, gH = 0, gC = 0;  // ring uses before the current item
     bool aborted = false;
-    int64_t q_abort = 0, Q_abort = 0;
     const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
     for (int64_t item = blockIdx.x; item < nitems && !aborted; item += gridDim.x) {
         const int tzi = (int)(item % p.ntz), tyi = (int)((item / p.ntz) % p.nty);
@@ -195,15 +231,14 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         // q >= 3, E_new(p-3) for q >= 6
         const int Q = x1 - x0 + 6;
         // ring uses: E at every iteration, H from iteration 3, CE from iteration 6;
-        // u-th use of a ring lands in slot u % depth and completes phase (u / depth) & 1
+        // the u-th use of a ring lands in slot u % depth and completes phase (u / depth) & 1
         auto eslot = [&](int q) { return (int)((gE + (uint32_t)q) % NE); };
         auto hslot = [&](int q) { return (int)((gH + (uint32_t)(q - 3)) % NH); };
         auto cslot = [&](int q) { return (int)((gC + (uint32_t)(q - 6)) % NC); };
         auto ephase = [&](int q) { return ((gE + (uint32_t)q) / NE) & 1; };
         auto hphase = [&](int q) { return ((gH + (uint32_t)(q - 3)) / NH) & 1; };
         auto cphase = [&](int q) { return ((gC + (uint32_t)(q - 6)) / NC) & 1; };
-        // copies needed at iteration q (issued two iterations ahead)
-        auto issue = [&](int q) {
+        auto issue = [&](int q) {  // copies needed at iteration q (issued two iterations ahead)
             const int pl = x0 - 3 + q;
             {   // E(p)
                 const int sl = eslot(q);
@@ -248,243 +283,242 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         __syncthreads();  // previous item finished everywhere; source list ready
         if (producer) {
             issue(0);
-            if (Q > 1) issue(1);
+            issue(1);
         }
         const int nls = s_nls;
+        const int j = j0 - 1 + hr, k = k0 - 1 + hc;
+        const bool col_in = h_thread && j >= 0 && j < p.ny && k >= 0 && k < p.nz;
+        const bool jin_h = j > 1 && j < p.ny - 1, kin_h = k > 1 && k < p.nz - 1;
+        const bool jin_e = j > 0 && j < p.ny - 2, kin_e = k > 0 && k < p.nz - 2;
+        const bool own_col = e_thread;
+        // y/z slab indices of the column (H nodes for the H stages, E nodes for the E stage)
+        int syh = -1, szh = -1, sye = -1, sze = -1;
+        if (p.cpml && col_in) {
+            syh = slab(p.ha[1], j, p.ny, false);
+            szh = slab(p.ha[2], k, p.nz, false);
+            sye = slab(p.ea[1], j, p.ny, true);
+            sze = slab(p.ea[2], k, p.nz, true);
+        }
+        // register queues of the column: input E of planes p-3 .. p-1 (ex, ey, ez),
+        // own H_new of planes p-4 .. p-2 (hy, hz)
+        float e0x = 0.f, e0y = 0.f, e0z = 0.f, e1x = 0.f, e1y = 0.f, e1z = 0.f, e2x = 0.f, e2y = 0.f, e2z = 0.f;
+        float n0y = 0.f, n0z = 0.f, n1y = 0.f, n1z = 0.f, n2y = 0.f, n2z = 0.f;
+        int q_abort = 0;
         for (int q = 0; q < Q; q++) {
             const int pl = x0 - 3 + q;
-            const int eS = eslot(q), hS = q >= 3 ? hslot(q) : 0, cS = q >= 6 ? cslot(q) : 0;
+            const int eS = eslot(q);
             if (producer) {
                 bool ok = mbar_wait(&bars[eS], ephase(q), p.status);
-                if (ok && q >= 3) ok = mbar_wait(&bars[NE + hS], hphase(q), p.status);
-                if (ok && q >= 6) ok = mbar_wait(&bars[NE + NH + cS], cphase(q), p.status);
+                if (ok && q >= 3) ok = mbar_wait(&bars[NE + hslot(q)], hphase(q), p.status);
+                if (ok && q >= 6) ok = mbar_wait(&bars[NE + NH + cslot(q)], cphase(q), p.status);
                 if (!ok) s_abort = 1;
             }
-            __syncthreads();  // (A) copies of iteration q visible; iteration q-1 done everywhere
+            __syncthreads();  // copies of iteration q visible; iteration q-1 done everywhere
             if (s_abort) {
                 aborted = true;
                 q_abort = q;
-                Q_abort = Q;
                 break;
             }
             if (producer && q + 2 < Q) issue(q + 2);
 
-            // ---- H_new(m), m = p - 1: (TY+3) x (TZ+3) cells around the tile ----
+            // input E of plane p at this column
+            float e3x = 0.f, e3y = 0.f, e3z = 0.f;
+            if (h_thread) {
+                e3x = sE(eS, 0)[eo];
+                e3y = sE(eS, 1)[eo];
+                e3z = sE(eS, 2)[eo];
+            }
+            // ---- H_new(m), m = p - 1, at this column ----
             const int m = pl - 1;
-            if (q >= 3 && h_thread && m >= 0 && m < p.nx) {
-                const int j = j0 - 1 + hr, k = k0 - 1 + hc;
-                if (j >= 0 && j < p.ny && k >= 0 && k < p.nz) {
-                    // E slots of planes m-2 .. m+1 (iterations q-3 .. q)
-                    const float *E0[3], *Em1[3], *Em2[3], *Ep1[3];
-                    for (int c = 0; c < 3; c++) {
-                        E0[c] = sE(eslot(q - 1), c);
-                        Em1[c] = sE(eslot(q - 2), c);
-                        Em2[c] = sE(eslot(q - 3), c);
-                        Ep1[c] = sE(eS, c);
+            float hny = 0.f, hnz = 0.f;
+            if (q >= 3 && col_in && m >= 0 && m < p.nx) {
+                const int eSm = eslot(q - 1), hS = hslot(q);
+                const float *ex = sE(eSm, 0), *ey = sE(eSm, 1), *ez = sE(eSm, 2);
+                const float hx0 = sH(hS, 0)[ho], hy0 = sH(hS, 1)[ho], hz0 = sH(hS, 2)[ho];
+                const bool iin = m > 1 && m < p.nx - 1;
+                const bool own = own_col && m >= x0 && m < x1;
+                const int sxh = p.cpml ? slab(p.ha[0], m, p.nx, false) : -1;
+                const int nst = p.hh ? 2 : 1;
+                float vx = hx0, vy = hy0, vz = hz0;
+                const int e = eo;
+                if (jin_h && kin_h) {  // hx: ez along y, ey along z (plane m)
+                    const float ezm2 = ez[e - 2 * BW], ezm1 = ez[e - BW], ezp1 = ez[e + BW];
+                    const float eym2 = ey[e - 2], eym1 = ey[e - 1], eyp1 = ey[e + 1];
+                    const float n = curl4(e2z, ezm1, e2y, eym1);
+                    const float f = curl4(ezp1, ezm2, eyp1, eym2);
+                    const float d27 = fsub(fmul(27.0f, n), f);
+                    float py = 0.f, pz = 0.f;
+                    uint32_t qy = 0, qz = 0;
+                    if (syh >= 0) { qy = psi_index(p, 1, syh, m, j, k, p.ha[1].P); py = p.psi_h_in[3][qy]; }
+                    if (szh >= 0) { qz = psi_index(p, 2, szh, m, j, k, p.ha[2].P); pz = p.psi_h_in[4][qz]; }
+                    const float dy = syh >= 0 ? d4h(ezm2, ezm1, e2z, ezp1) : 0.f;
+                    const float dz = szh >= 0 ? d4h(eym2, eym1, e2y, eyp1) : 0.f;
+                    for (int st = 0; st < nst; st++) {
+                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
+                        const Axis *A = st ? p.hb : p.ha;
+                        vx = fsub(vx, fmul(clch, d27));
+                        if (syh >= 0) vx = fsub(vx, sterm(A[1], syh, py, dy, cl, p.ch));
+                        if (szh >= 0) vx = fadd(vx, sterm(A[2], szh, pz, dz, cl, p.ch));
                     }
-                    const int e = (hr + 2) * BW + hc + 3;  // E box: row j0-3+r, column k0-4+c
-                    const int hb = hr * BW + hc + 3;       // H box: row j0-1+r
-                    const float *ex = E0[0], *ey = E0[1], *ez = E0[2];
-                    const float hx0 = sH(hS, 0)[hb], hy0 = sH(hS, 1)[hb], hz0 = sH(hS, 2)[hb];
-                    const bool jin = j > 1 && j < p.ny - 1, kin = k > 1 && k < p.nz - 1, iin = m > 1 && m < p.nx - 1;
-                    const bool own = hr >= 1 && hr <= TY && hc >= 1 && hc <= TZ && m >= x0 && m < x1;
-                    int sx = -1, sy = -1, sz = -1;
-                    if (p.cpml) {
-                        sx = slab(p.ha[0], m, p.nx, false);
-                        sy = slab(p.ha[1], j, p.ny, false);
-                        sz = slab(p.ha[2], k, p.nz, false);
+                    if (own && syh >= 0) p.psi_h_out[3][qy] = py;
+                    if (own && szh >= 0) p.psi_h_out[4][qz] = pz;
+                }
+                if (iin && kin_h) {  // hy: ex along z (plane m), ez along x (queue)
+                    const float exm2 = ex[e - 2], exm1 = ex[e - 1], exp1 = ex[e + 1];
+                    const float n = curl4(e2x, exm1, e2z, e1z);
+                    const float f = curl4(exp1, exm2, e3z, e0z);
+                    const float d27 = fsub(fmul(27.0f, n), f);
+                    float px = 0.f, pz = 0.f;
+                    uint32_t qx = 0, qz = 0;
+                    if (sxh >= 0) { qx = psi_index(p, 0, sxh, m, j, k, p.ha[0].P); px = p.psi_h_in[0][qx]; }
+                    if (szh >= 0) { qz = psi_index(p, 2, szh, m, j, k, p.ha[2].P); pz = p.psi_h_in[5][qz]; }
+                    const float dx = sxh >= 0 ? d4h(e0z, e1z, e2z, e3z) : 0.f;
+                    const float dz = szh >= 0 ? d4h(exm2, exm1, e2x, exp1) : 0.f;
+                    for (int st = 0; st < nst; st++) {
+                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
+                        const Axis *A = st ? p.hb : p.ha;
+                        vy = fsub(vy, fmul(clch, d27));
+                        if (sxh >= 0) vy = fadd(vy, sterm(A[0], sxh, px, dx, cl, p.ch));
+                        if (szh >= 0) vy = fsub(vy, sterm(A[2], szh, pz, dz, cl, p.ch));
                     }
-                    const int nst = p.hh ? 2 : 1;
-                    float vx = hx0, vy = hy0, vz = hz0;
-                    // the stage's differences do not change between the two H stages
-                    if (jin && kin) {
-                        const float n = curl4(ez[e], ez[e - BW], ey[e], ey[e - 1]);
-                        const float f = curl4(ez[e + BW], ez[e - 2 * BW], ey[e + 1], ey[e - 2]);
-                        const float d27 = fsub(fmul(27.0f, n), f);
-                        const float dy = sy >= 0 ? fsub(fmul(27.0f, fsub(ez[e], ez[e - BW])), fsub(ez[e + BW], ez[e - 2 * BW])) : 0.f;
-                        const float dz = sz >= 0 ? fsub(fmul(27.0f, fsub(ey[e], ey[e - 1])), fsub(ey[e + 1], ey[e - 2])) : 0.f;
-                        float py = 0.f, pz = 0.f;
-                        const uint32_t qy = sy >= 0 ? psi_index(p, 1, sy, m, j, k, p.ha[1].P) : 0u;
-                        const uint32_t qz = sz >= 0 ? psi_index(p, 2, sz, m, j, k, p.ha[2].P) : 0u;
-                        if (sy >= 0) py = p.psi_h_in[3][qy];
-                        if (sz >= 0) pz = p.psi_h_in[4][qz];
-                        for (int st = 0; st < nst; st++) {
-                            const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                            const Axis *A = st ? p.hb : p.ha;
-                            vx = fsub(vx, fmul(clch, d27));
-                            if (sy >= 0) vx = fsub(vx, sterm(A[1], sy, py, dy, cl, p.ch));
-                            if (sz >= 0) vx = fadd(vx, sterm(A[2], sz, pz, dz, cl, p.ch));
-                        }
-                        if (own && sy >= 0) p.psi_h_out[3][qy] = py;
-                        if (own && sz >= 0) p.psi_h_out[4][qz] = pz;
+                    if (own && sxh >= 0) p.psi_h_out[0][qx] = px;
+                    if (own && szh >= 0) p.psi_h_out[5][qz] = pz;
+                }
+                if (iin && jin_h) {  // hz: ey along x (queue), ex along y (plane m)
+                    const float exm2 = ex[e - 2 * BW], exm1 = ex[e - BW], exp1 = ex[e + BW];
+                    const float n = curl4(e2y, e1y, e2x, exm1);
+                    const float f = curl4(e3y, e0y, exp1, exm2);
+                    const float d27 = fsub(fmul(27.0f, n), f);
+                    float px = 0.f, py = 0.f;
+                    uint32_t qx = 0, qy = 0;
+                    if (sxh >= 0) { qx = psi_index(p, 0, sxh, m, j, k, p.ha[0].P); px = p.psi_h_in[1][qx]; }
+                    if (syh >= 0) { qy = psi_index(p, 1, syh, m, j, k, p.ha[1].P); py = p.psi_h_in[2][qy]; }
+                    const float dx = sxh >= 0 ? d4h(e0y, e1y, e2y, e3y) : 0.f;
+                    const float dy = syh >= 0 ? d4h(exm2, exm1, e2x, exp1) : 0.f;
+                    for (int st = 0; st < nst; st++) {
+                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
+                        const Axis *A = st ? p.hb : p.ha;
+                        vz = fsub(vz, fmul(clch, d27));
+                        if (sxh >= 0) vz = fsub(vz, sterm(A[0], sxh, px, dx, cl, p.ch));
+                        if (syh >= 0) vz = fadd(vz, sterm(A[1], syh, py, dy, cl, p.ch));
                     }
-                    if (iin && kin) {
-                        const float n = curl4(ex[e], ex[e - 1], ez[e], Em1[2][e]);
-                        const float f = curl4(ex[e + 1], ex[e - 2], Ep1[2][e], Em2[2][e]);
-                        const float d27 = fsub(fmul(27.0f, n), f);
-                        const float dx = sx >= 0 ? fsub(fmul(27.0f, fsub(ez[e], Em1[2][e])), fsub(Ep1[2][e], Em2[2][e])) : 0.f;
-                        const float dz = sz >= 0 ? fsub(fmul(27.0f, fsub(ex[e], ex[e - 1])), fsub(ex[e + 1], ex[e - 2])) : 0.f;
-                        float px = 0.f, pz = 0.f;
-                        const uint32_t qx = sx >= 0 ? psi_index(p, 0, sx, m, j, k, p.ha[0].P) : 0u;
-                        const uint32_t qz = sz >= 0 ? psi_index(p, 2, sz, m, j, k, p.ha[2].P) : 0u;
-                        if (sx >= 0) px = p.psi_h_in[0][qx];
-                        if (sz >= 0) pz = p.psi_h_in[5][qz];
-                        for (int st = 0; st < nst; st++) {
-                            const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                            const Axis *A = st ? p.hb : p.ha;
-                            vy = fsub(vy, fmul(clch, d27));
-                            if (sx >= 0) vy = fadd(vy, sterm(A[0], sx, px, dx, cl, p.ch));
-                            if (sz >= 0) vy = fsub(vy, sterm(A[2], sz, pz, dz, cl, p.ch));
-                        }
-                        if (own && sx >= 0) p.psi_h_out[0][qx] = px;
-                        if (own && sz >= 0) p.psi_h_out[5][qz] = pz;
-                    }
-                    if (iin && jin) {
-                        const float n = curl4(ey[e], Em1[1][e], ex[e], ex[e - BW]);
-                        const float f = curl4(Ep1[1][e], Em2[1][e], ex[e + BW], ex[e - 2 * BW]);
-                        const float d27 = fsub(fmul(27.0f, n), f);
-                        const float dx = sx >= 0 ? fsub(fmul(27.0f, fsub(ey[e], Em1[1][e])), fsub(Ep1[1][e], Em2[1][e])) : 0.f;
-                        const float dy = sy >= 0 ? fsub(fmul(27.0f, fsub(ex[e], ex[e - BW])), fsub(ex[e + BW], ex[e - 2 * BW])) : 0.f;
-                        float px = 0.f, py = 0.f;
-                        const uint32_t qx = sx >= 0 ? psi_index(p, 0, sx, m, j, k, p.ha[0].P) : 0u;
-                        const uint32_t qy = sy >= 0 ? psi_index(p, 1, sy, m, j, k, p.ha[1].P) : 0u;
-                        if (sx >= 0) px = p.psi_h_in[1][qx];
-                        if (sy >= 0) py = p.psi_h_in[2][qy];
-                        for (int st = 0; st < nst; st++) {
-                            const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                            const Axis *A = st ? p.hb : p.ha;
-                            vz = fsub(vz, fmul(clch, d27));
-                            if (sx >= 0) vz = fsub(vz, sterm(A[0], sx, px, dx, cl, p.ch));
-                            if (sy >= 0) vz = fadd(vz, sterm(A[1], sy, py, dy, cl, p.ch));
-                        }
-                        if (own && sx >= 0) p.psi_h_out[1][qx] = px;
-                        if (own && sy >= 0) p.psi_h_out[2][qy] = py;
-                    }
-                    const int nsl = (int)((uint32_t)(m - (x0 - 4)) % NHN);  // ring slot of plane m
-                    const int no = hr * HNP + hc;
-                    sN(nsl, 0)[no] = vx;
-                    sN(nsl, 1)[no] = vy;
-                    sN(nsl, 2)[no] = vz;
-                    if (own) {
-                        const uint32_t g = (uint32_t)m * p.sx + (uint32_t)j * p.sy + k;
-                        p.out[3][g] = vx;
-                        p.out[4][g] = vy;
-                        p.out[5][g] = vz;
-                    }
+                    if (own && sxh >= 0) p.psi_h_out[1][qx] = px;
+                    if (own && syh >= 0) p.psi_h_out[2][qy] = py;
+                }
+                const int nsl = (m - (x0 - 1)) % NHN;
+                sN(nsl, 0)[no] = vx;
+                sN(nsl, 1)[no] = vy;
+                sN(nsl, 2)[no] = vz;
+                hny = vy;
+                hnz = vz;
+                if (own) {
+                    const uint32_t g = (uint32_t)m * p.sx + (uint32_t)j * p.sy + k;
+                    p.out[3][g] = vx;
+                    p.out[4][g] = vy;
+                    p.out[5][g] = vz;
                 }
             }
-            __syncthreads();  // (B) H_new(p-1) visible
 
-            // ---- E_new(i), i = p - 3, on the tile ----
+            // ---- E_new(i), i = p - 3, at tile columns ----
             const int i = pl - 3;
-            if (q >= 6 && e_thread) {
-                const int r = warp, j = j0 + r, k = k0 + lane;
-                if (j < p.ny && k < p.nz) {
-                    const float *N0[3], *Nm1[3], *Np1[3], *Np2[3];
-                    for (int c = 0; c < 3; c++) {
-                        N0[c] = sN((int)((uint32_t)(i - (x0 - 4)) % NHN), c);
-                        Nm1[c] = sN((int)((uint32_t)(i - 1 - (x0 - 4)) % NHN), c);
-                        Np1[c] = sN((int)((uint32_t)(i + 1 - (x0 - 4)) % NHN), c);
-                        Np2[c] = sN((int)((uint32_t)(i + 2 - (x0 - 4)) % NHN), c);
+            if (q >= 6 && own_col && col_in) {
+                // H_new at planes i-1 .. i+2 of this column: n0 (i-1), n1 (i), n2 (i+1), new (i+2);
+                // H_new(i) neighbours from the ring (written two iterations ago)
+                const int nsl = (i - (x0 - 1)) % NHN;
+                const float *hx = sN(nsl, 0), *hy = sN(nsl, 1), *hz = sN(nsl, 2);
+                const int cS = cslot(q);
+                const int h = no;
+                float vx = e0x, vy = e0y, vz = e0z;  // input E of plane i
+                const bool iin = i > 0 && i < p.nx - 2;
+                const int sxe = p.cpml ? slab(p.ea[0], i, p.nx, true) : -1;
+                if (jin_e && kin_e) {  // ex: hz along y, hy along z (plane i)
+                    const float hzm1 = hz[h - HNP], hzp1 = hz[h + HNP], hzp2 = hz[h + 2 * HNP];
+                    const float hym1 = hy[h - 1], hyp1 = hy[h + 1], hyp2 = hy[h + 2];
+                    const float n = curl4(hzp1, n1z, hyp1, n1y);
+                    const float f = curl4(hzp2, hzm1, hyp2, hym1);
+                    const float cv = sC(cS, 0)[co];
+                    vx = fadd(vx, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                    if (sye >= 0) {
+                        const uint32_t qi = psi_index(p, 1, sye, i, j, k, p.ea[1].P);
+                        float ps = p.psi_e[3][qi];
+                        vx = fadd(vx, sterm(p.ea[1], sye, ps, d4e(hzm1, n1z, hzp1, hzp2), p.dl, cv));
+                        p.psi_e[3][qi] = ps;
                     }
-                    const int h = (r + 1) * HNP + lane + 1;   // H_new: row j0-1+r', column k0-1+c'
-                    const int e = (r + 3) * BW + lane + 4;    // E box of plane i
-                    const int ce = r * TZ + lane;
-                    const int eS3 = eslot(q - 3);
-                    const float *hx = N0[0], *hy = N0[1], *hz = N0[2];
-                    float vx = sE(eS3, 0)[e], vy = sE(eS3, 1)[e], vz = sE(eS3, 2)[e];
-                    const bool jin = j > 0 && j < p.ny - 2, kin = k > 0 && k < p.nz - 2, iin = i > 0 && i < p.nx - 2;
-                    int sx = -1, sy = -1, sz = -1;
-                    if (p.cpml) {
-                        sx = slab(p.ea[0], i, p.nx, true);
-                        sy = slab(p.ea[1], j, p.ny, true);
-                        sz = slab(p.ea[2], k, p.nz, true);
+                    if (sze >= 0) {
+                        const uint32_t qi = psi_index(p, 2, sze, i, j, k, p.ea[2].P);
+                        float ps = p.psi_e[4][qi];
+                        vx = fsub(vx, sterm(p.ea[2], sze, ps, d4e(hym1, n1y, hyp1, hyp2), p.dl, cv));
+                        p.psi_e[4][qi] = ps;
                     }
-                    if (jin && kin) {
-                        const float n = curl4(hz[h + HNP], hz[h], hy[h + 1], hy[h]);
-                        const float f = curl4(hz[h + 2 * HNP], hz[h - HNP], hy[h + 2], hy[h - 1]);
-                        const float cv = sC(cS, 0)[ce];
-                        vx = fadd(vx, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                        if (sy >= 0) {
-                            const uint32_t qi = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
-                            float ps = p.psi_e[3][qi];
-                            const float d = fsub(fmul(27.0f, fsub(hz[h + HNP], hz[h])), fsub(hz[h + 2 * HNP], hz[h - HNP]));
-                            vx = fadd(vx, sterm(p.ea[1], sy, ps, d, p.dl, cv));
-                            p.psi_e[3][qi] = ps;
-                        }
-                        if (sz >= 0) {
-                            const uint32_t qi = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
-                            float ps = p.psi_e[4][qi];
-                            const float d = fsub(fmul(27.0f, fsub(hy[h + 1], hy[h])), fsub(hy[h + 2], hy[h - 1]));
-                            vx = fsub(vx, sterm(p.ea[2], sz, ps, d, p.dl, cv));
-                            p.psi_e[4][qi] = ps;
-                        }
-                    }
-                    if (iin && kin) {
-                        const float n = curl4(hx[h + 1], hx[h], Np1[2][h], hz[h]);
-                        const float f = curl4(hx[h + 2], hx[h - 1], Np2[2][h], Nm1[2][h]);
-                        const float cv = sC(cS, 1)[ce];
-                        vy = fadd(vy, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                        if (sx >= 0) {
-                            const uint32_t qi = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
-                            float ps = p.psi_e[0][qi];
-                            const float d = fsub(fmul(27.0f, fsub(Np1[2][h], hz[h])), fsub(Np2[2][h], Nm1[2][h]));
-                            vy = fsub(vy, sterm(p.ea[0], sx, ps, d, p.dl, cv));
-                            p.psi_e[0][qi] = ps;
-                        }
-                        if (sz >= 0) {
-                            const uint32_t qi = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
-                            float ps = p.psi_e[5][qi];
-                            const float d = fsub(fmul(27.0f, fsub(hx[h + 1], hx[h])), fsub(hx[h + 2], hx[h - 1]));
-                            vy = fadd(vy, sterm(p.ea[2], sz, ps, d, p.dl, cv));
-                            p.psi_e[5][qi] = ps;
-                        }
-                    }
-                    if (iin && jin) {
-                        const float n = curl4(Np1[1][h], hy[h], hx[h + HNP], hx[h]);
-                        const float f = curl4(Np2[1][h], Nm1[1][h], hx[h + 2 * HNP], hx[h - HNP]);
-                        const float cv = sC(cS, 2)[ce];
-                        vz = fadd(vz, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                        if (sx >= 0) {
-                            const uint32_t qi = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
-                            float ps = p.psi_e[1][qi];
-                            const float d = fsub(fmul(27.0f, fsub(Np1[1][h], hy[h])), fsub(Np2[1][h], Nm1[1][h]));
-                            vz = fadd(vz, sterm(p.ea[0], sx, ps, d, p.dl, cv));
-                            p.psi_e[1][qi] = ps;
-                        }
-                        if (sy >= 0) {
-                            const uint32_t qi = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
-                            float ps = p.psi_e[2][qi];
-                            const float d = fsub(fmul(27.0f, fsub(hx[h + HNP], hx[h])), fsub(hx[h + 2 * HNP], hx[h - HNP]));
-                            vz = fsub(vz, sterm(p.ea[1], sy, ps, d, p.dl, cv));
-                            p.psi_e[2][qi] = ps;
-                        }
-                    }
-                    for (int s = 0; s < nls; s++) {  // soft sources, list order
-                        if (s_ls_i[s] != i || s_ls_j[s] != j || (s_ls_kc[s] >> 2) != k) continue;
-                        const float v = p.src_amp[(int64_t)s_ls_s[s] * p.namp + p.t];
-                        const int comp = s_ls_kc[s] & 3;
-                        if (comp == 0) vx = fadd(vx, v);
-                        else if (comp == 1) vy = fadd(vy, v);
-                        else vz = fadd(vz, v);
-                    }
-                    const uint32_t g = (uint32_t)i * p.sx + (uint32_t)j * p.sy + k;
-                    p.out[0][g] = vx;
-                    p.out[1][g] = vy;
-                    p.out[2][g] = vz;
                 }
+                if (iin && kin_e) {  // ey: hx along z (plane i), hz along x (queue)
+                    const float hx0 = hx[h], hxm1 = hx[h - 1], hxp1 = hx[h + 1], hxp2 = hx[h + 2];
+                    const float n = curl4(hxp1, hx0, n2z, n1z);
+                    const float f = curl4(hxp2, hxm1, hnz, n0z);
+                    const float cv = sC(cS, 1)[co];
+                    vy = fadd(vy, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                    if (sxe >= 0) {
+                        const uint32_t qi = psi_index(p, 0, sxe, i, j, k, p.ea[0].P);
+                        float ps = p.psi_e[0][qi];
+                        vy = fsub(vy, sterm(p.ea[0], sxe, ps, d4e(n0z, n1z, n2z, hnz), p.dl, cv));
+                        p.psi_e[0][qi] = ps;
+                    }
+                    if (sze >= 0) {
+                        const uint32_t qi = psi_index(p, 2, sze, i, j, k, p.ea[2].P);
+                        float ps = p.psi_e[5][qi];
+                        vy = fadd(vy, sterm(p.ea[2], sze, ps, d4e(hxm1, hx0, hxp1, hxp2), p.dl, cv));
+                        p.psi_e[5][qi] = ps;
+                    }
+                }
+                if (iin && jin_e) {  // ez: hy along x (queue), hx along y (plane i)
+                    const float hx0 = hx[h], hxm1 = hx[h - HNP], hxp1 = hx[h + HNP], hxp2 = hx[h + 2 * HNP];
+                    const float n = curl4(n2y, n1y, hxp1, hx0);
+                    const float f = curl4(hny, n0y, hxp2, hxm1);
+                    const float cv = sC(cS, 2)[co];
+                    vz = fadd(vz, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                    if (sxe >= 0) {
+                        const uint32_t qi = psi_index(p, 0, sxe, i, j, k, p.ea[0].P);
+                        float ps = p.psi_e[1][qi];
+                        vz = fadd(vz, sterm(p.ea[0], sxe, ps, d4e(n0y, n1y, n2y, hny), p.dl, cv));
+                        p.psi_e[1][qi] = ps;
+                    }
+                    if (sye >= 0) {
+                        const uint32_t qi = psi_index(p, 1, sye, i, j, k, p.ea[1].P);
+                        float ps = p.psi_e[2][qi];
+                        vz = fsub(vz, sterm(p.ea[1], sye, ps, d4e(hxm1, hx0, hxp1, hxp2), p.dl, cv));
+                        p.psi_e[2][qi] = ps;
+                    }
+                }
+                for (int s = 0; s < nls; s++) {  // soft sources, list order
+                    if (s_ls_i[s] != i || s_ls_j[s] != j || (s_ls_kc[s] >> 2) != k) continue;
+                    const float v = p.src_amp[(int64_t)s_ls_s[s] * p.namp + p.t];
+                    const int comp = s_ls_kc[s] & 3;
+                    if (comp == 0) vx = fadd(vx, v);
+                    else if (comp == 1) vy = fadd(vy, v);
+                    else vz = fadd(vz, v);
+                }
+                const uint32_t g = (uint32_t)i * p.sx + (uint32_t)j * p.sy + k;
+                p.out[0][g] = vx;
+                p.out[1][g] = vy;
+                p.out[2][g] = vz;
             }
+            // advance the queues
+            e0x = e1x; e0y = e1y; e0z = e1z;
+            e1x = e2x; e1y = e2y; e1z = e2z;
+            e2x = e3x; e2y = e3y; e2z = e3z;
+            n0y = n1y; n0z = n1z;
+            n1y = n2y; n1z = n2z;
+            n2y = hny; n2z = hnz;
         }
         if (aborted) {
             if (producer) {
                 atomicExch(p.status, FDTD_ERR_TIMEOUT);
                 // let the copies in flight (iterations q and q+1) land before the
                 // shared memory is released; each wait bounded
-                for (int64_t q = q_abort; q < Q_abort && q < q_abort + 2; q++) {
-                    const int qq = (int)q;
-                    mbar_wait(&bars[eslot(qq)], ephase(qq), nullptr);
-                    if (qq >= 3) mbar_wait(&bars[NE + hslot(qq)], hphase(qq), nullptr);
-                    if (qq >= 6) mbar_wait(&bars[NE + NH + cslot(qq)], cphase(qq), nullptr);
+                for (int q = q_abort; q < Q && q < q_abort + 2; q++) {
+                    mbar_wait(&bars[eslot(q)], ephase(q), nullptr);
+                    if (q >= 3) mbar_wait(&bars[NE + hslot(q)], hphase(q), nullptr);
+                    if (q >= 6) mbar_wait(&bars[NE + NH + cslot(q)], cphase(q), nullptr);
                 }
             }
             break;

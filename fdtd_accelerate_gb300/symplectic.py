@@ -117,13 +117,35 @@ class SymplecticCpml:
             self.tables[coef] = [{k: f32(v) for k, v in ta.items()} if ta else None for ta in t]
         pshapes = [(2 * npml[0], ny, nz), (nx, 2 * npml[1], nz), (nx, ny, 2 * npml[2])]
         z = lambda a: torch.zeros(pshapes[a], dtype=torch.float32, device=self.device) if npml[a] else None
+        self._pshapes = pshapes
         self.psi_e = [z(a) for a in range(3) for _ in range(2)]
-        self.psi_h = [z(a) for a in range(3) for _ in range(2)]
+        # H psi of the current state buffer; the fused stage-pair path keeps a
+        # second set (hbuf[1 - hcur]) that it writes while it reads this one
+        self.hbuf = [[z(a) for a in range(3) for _ in range(2)], None]
+        self.hcur = 0
         self._structs = {c: self._make_struct(c) for c in self.tables}
         self._psi = N.Psi()
+        self._fill_psi()
+
+    @property
+    def psi_h(self):
+        return self.hbuf[self.hcur]
+
+    def _fill_psi(self):
         for q in range(6):
             self._psi.e[q] = self.psi_e[q].data_ptr() if self.psi_e[q] is not None else None
             self._psi.h[q] = self.psi_h[q].data_ptr() if self.psi_h[q] is not None else None
+
+    def second_h_buffer(self):
+        """Allocate the second H psi set (stage-pair path) and return both."""
+        if self.hbuf[1] is None:
+            self.hbuf[1] = [torch.zeros_like(t) if t is not None else None for t in self.hbuf[0]]
+        return self.hbuf
+
+    def set_hcur(self, b):
+        if b != self.hcur:
+            self.hcur = b
+            self._fill_psi()
 
     @property
     def active(self):
@@ -162,15 +184,27 @@ class SymplecticSolver:
     (uniform, default S/24) or three arrays; sources: (component, (i, j, k),
     amplitude) with amplitude a callable of continuous time t (FP64), added
     after every E stage at t = tn + sn/5 (PyCUDA/100-base.py:136).
+    fused: take the stage-pair kernel (one pass per H + E stage pair) where
+    pair_path() allows; it is bit-identical to the per-stage kernels but
+    currently slower than them on the 512^3 workload, so the default is the
+    one-launch-per-stage path; x_chunk: x planes per work item of the pair
+    kernel (0: 128).
     """
 
     def __init__(self, shape, ce=None, ch=None, npml=0, faces=0x3F, sources=(), device="cuda",
-                 S=COURANT, cpml_params=None, max_steps=0):
+                 S=COURANT, cpml_params=None, max_steps=0, fused=False, x_chunk=0):
         self.shape = tuple(int(v) for v in shape)
         self.device = torch.device(device)
         dev = self.device
         self.S = S
-        self.f = [torch.zeros(self.shape, dtype=torch.float32, device=dev) for _ in range(6)]
+        # state buffers: buf[cur] holds the fields; the stage-pair path writes
+        # buf[1 - cur] from buf[cur] (the second buffer is allocated on first use)
+        self._buf = [torch.zeros((6,) + self.shape, dtype=torch.float32, device=dev), None]
+        self._cur = 0
+        self.fused = fused
+        self.x_chunk = int(x_chunk)
+        self._pair = None
+        self._pair_src = None
         if ce is None:
             ce = [np.full(self.shape, S / 24.0)] * 3
         self.ce = [torch.as_tensor(c, dtype=torch.float32, device=dev).contiguous() for c in ce]
@@ -197,14 +231,108 @@ class SymplecticSolver:
         self._src_steps = nsteps
 
     @property
+    def f(self):
+        """ex, ey, ez, hx, hy, hz of the current state buffer."""
+        return list(self._buf[self._cur])
+
+    @property
     def fields(self):
         return dict(zip(("ex", "ey", "ez", "hx", "hy", "hz"), self.f))
+
+    def pair_path(self):
+        """True when step() runs the fused stage pairs: uniform ch, rows of a
+        multiple of 4 floats (16-byte TMA rows), fewer than 2^31 cells, every
+        extent at least 4."""
+        nx, ny, nz = self.shape
+        return (self.fused and isinstance(self.ch, float) and nz % 4 == 0 and min(self.shape) >= 4
+                and nx * ny * nz < 2 ** 31)
+
+    def _pair_plan(self):
+        if self._pair is not None and self._pair_src is self._src:
+            return self._pair
+        self.close()
+        if self._buf[1] is None:
+            self._buf[1] = torch.zeros_like(self._buf[0])
+        hb = self.cpml.second_h_buffer()
+        st = N.SympState()
+        for b in range(2):
+            for q in range(6):
+                st.f[b][q] = self._buf[b][q].data_ptr()
+                st.psi_h[b][q] = hb[b][q].data_ptr() if hb[b][q] is not None else None
+        for q in range(6):
+            e = self.cpml.psi_e[q]
+            st.psi_e[q] = e.data_ptr() if e is not None else None
+        for q in range(3):
+            st.ce[q] = self.ce[q].data_ptr()
+        if not hasattr(self, "_status"):
+            self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        h = C.c_void_p()
+        src = self._src.struct()
+        with torch.cuda.device(self.device):
+            N.call("fdtd_symp_pair_plan_create", C.byref(h), C.byref(grid_of(self._buf[0][0])), C.byref(st),
+                   C.byref(src), int(self.x_chunk), int(self._cur), C.c_void_p(self._status.data_ptr()),
+                   stream_of(self._buf[0][0]))
+        self._pair, self._pair_src = h, self._src
+        return h
+
+    def close(self):
+        if self._pair is not None:
+            N.lib().fdtd_symp_pair_plan_destroy(self._pair)
+            self._pair = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check_status(self):
+        """Raise if a bounded device wait of the stage-pair kernel expired."""
+        if hasattr(self, "_status"):
+            v = int(self._status.item())
+            if v:
+                self._status.zero_()
+                N.check(v, "fdtd_symp_pair_run (device status)")
 
     def set_fields(self, **arrays):
         for k, v in arrays.items():
             self.fields[k].copy_(torch.as_tensor(v, dtype=torch.float32, device=self.device))
 
     def step(self, n=1):
+        """Advance n steps.  On the stage-pair path (pair_path()): each H stage
+        and the E stage after it run as one fused pass with the sources
+        (fdtd_symp_pair_run), the closing H stage of a step merges with the
+        opening H stage of the next into one pass, and the run's last H stage
+        runs alone in place: 4 n passes and one H stage for n steps.  Otherwise
+        step_stages()."""
+        if n <= 0:
+            return
+        if not self.pair_path():
+            return self.step_stages(n)
+        if self.src_spec and self.tstep + n > self._src_steps:
+            self._build_sources(self.tstep + n)
+        plan = self._pair_plan()
+        L = N.lib()
+        L.fdtd_symp_pair_plan_set_current(plan, self._cur)
+        cp = self.cpml
+        tabs = (lambda c: C.byref(cp._structs[c])) if cp.active else (lambda c: None)
+        ch = float(self.ch)
+        with torch.cuda.device(self.device):
+            stream = stream_of(self._buf[0][0])
+            for m in range(n):
+                tn = self.tstep + m
+                for sn in range(4):
+                    two = 1 if (sn == 0 and m > 0) else 0   # closing H(c1) of step tn-1, then H(c1)
+                    cl_a = CL[4] if two else CL[sn]
+                    N.call("fdtd_symp_pair_run", plan, tabs(cl_a), tabs(CL[sn]), tabs(DL[sn]), float(cl_a),
+                           float(CL[sn]), two, float(DL[sn]), ch, 4 * tn + sn if self.src_spec else -1, stream)
+                    self._cur = 1 - self._cur
+                    cp.set_hcur(self._cur)
+            self._stage_args = None
+            self._fused_stage(0, CL[4], None, ch, stream)
+        self.tstep += n
+
+    def step_stages(self, n=1):
         """Advance n steps: one launch per stage (the stage update and its CPML
         slabs together, fdtd_symplectic_stage_f32) and the sources after each E
         stage.  Fields of 2^31 or more elements (the stage kernel's offsets are
@@ -214,8 +342,7 @@ class SymplecticSolver:
             return self.step_unfused(n)
         if self.src_spec and self.tstep + n > self._src_steps:
             self._build_sources(self.tstep + n)
-        if self._stage_args is None:
-            self._stage_args = self._make_stage_args()
+        self._stage_args = self._make_stage_args()
         g, fptr, ceptr, chptr, chv = self._stage_args
         with torch.cuda.device(self.device):
             stream = stream_of(f[0])
@@ -240,6 +367,8 @@ class SymplecticSolver:
         return g, fptr, ceptr, chptr, chv
 
     def _fused_stage(self, e_or_h, coef, cptr, chv, stream):
+        if self._stage_args is None:
+            self._stage_args = self._make_stage_args()
         g, fptr = self._stage_args[0], self._stage_args[1]
         cp = C.byref(self.cpml._structs[coef]) if self.cpml.active else None
         psi = C.byref(self.cpml._psi) if self.cpml.active else None

@@ -187,3 +187,67 @@ def test_symplectic_cpml_absorbs(S):
         energies[npml] = sum(float((t.double() ** 2).sum()) for t in s.f)
         assert np.isfinite(energies[npml])
     assert energies[8] < 0.05 * energies[0], energies
+
+
+@pytest.mark.parametrize("shape,npml,faces,x_chunk,steps", [
+    ((40, 36, 68), 5, 0x3F, 0, 3),        # one x chunk, ragged y and z tiles
+    ((44, 34, 72), 6, 0x3F, 8, 4),        # several x chunks: halo planes recomputed at chunk starts
+    ((30, 40, 64), 4, 0x15, 5, 2),        # front faces only, odd chunk length
+    ((28, 20, 36), 3, 0x2A, 7, 3),        # back faces only
+    ((36, 18, 40), 0, 0x3F, 9, 3),        # no CPML
+    ((24, 50, 100), 6, 0x3F, 0, 1),       # one step: no merged H stages
+])
+def test_stage_pairs_equal_stage_kernels(S, shape, npml, faces, x_chunk, steps):
+    """The fused stage pairs (one pass per H+E stage pair, the closing and
+    opening H stages of consecutive steps merged) equal the one-launch-per-stage
+    path bit for bit: fields, E psi and H psi, with sources on tile edges in y
+    and z and on a chunk edge in x, spheres, random initial state."""
+    from fdtd_accelerate_gb300 import configs
+    rng = np.random.default_rng(12)
+    spheres = configs.random_spheres(rng, shape, 5, 2, 5, 1.0, 4.0)
+    ce = [(c.numpy() * np.float32(S.COURANT / 24 / 0.5)).astype(np.float32)
+          for c in configs.ce_from_spheres(shape, spheres)]
+    amp = lambda t: np.sin(0.3 * t) * np.exp(-0.5 * ((t - 4.0) / 2.0) ** 2)
+    nx, ny, nz = shape
+    src = [("ez", (nx // 2, ny // 2, nz // 2), amp), ("ex", (max(x_chunk, 3), 15, 31), amp),
+           ("ey", (nx // 3, 16, 32), lambda t: 0.5 * amp(t + 1.0)), ("ez", (nx - 4, ny - 3, nz - 2), amp)]
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    runs = []
+    for fused in (True, False):
+        s = S.SymplecticSolver(shape, ce=ce, npml=npml, faces=faces, sources=src, max_steps=steps + 2,
+                               fused=fused, x_chunk=x_chunk)
+        assert s.pair_path() == fused
+        s.set_fields(**init)
+        s.step(steps)
+        runs.append(s)
+    torch.cuda.synchronize()
+    a, b = runs
+    a.check_status()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)
+    if a.cpml.active:
+        for q in range(6):
+            if a.cpml.psi_e[q] is not None:
+                np.testing.assert_array_equal(_host(a.cpml.psi_e[q]), _host(b.cpml.psi_e[q]), err_msg="psi_e%d" % q)
+                np.testing.assert_array_equal(_host(a.cpml.psi_h[q]), _host(b.cpml.psi_h[q]), err_msg="psi_h%d" % q)
+
+
+def test_stage_pairs_then_stage_kernels_interleave(S):
+    """Runs alternating between the stage-pair path and the stage kernels keep
+    the state (the current buffer, H psi set, step number) consistent."""
+    shape, npml = (32, 34, 44), 4
+    rng = np.random.default_rng(3)
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    src = [("ez", (16, 17, 22), lambda t: np.sin(0.2 * t))]
+    a = S.SymplecticSolver(shape, npml=npml, sources=src, max_steps=10, fused=True)
+    b = S.SymplecticSolver(shape, npml=npml, sources=src, max_steps=10, fused=False)
+    for s in (a, b):
+        s.set_fields(**init)
+    assert a.pair_path() and not b.pair_path()
+    a.step(2)
+    a.step_stages(1)
+    a.step(3)
+    b.step(6)
+    torch.cuda.synchronize()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)

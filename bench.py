@@ -51,10 +51,18 @@ NPML = 12
 # Measured STREAM-style copy bandwidth of this machine's GB300 (GB/s); read
 # from MEASURED_PEAKS.json when present.
 FALLBACK_HBM_GBS = 6790.7
-# DRAM bytes per cell-step of one time step (the fused kernel and the two z-band
-# kernels: dram__bytes_read.sum + dram__bytes_write.sum over the three launches of a
-# step / cells), from an ncu capture of this workload at full size.
-NCU_DRAM_BYTES_PER_CELL = 75.2
+# DRAM traffic of one time step (dram__bytes_read.sum + dram__bytes_write.sum),
+# from an ncu capture of the same workload scaled to 512x512x256 (three steps,
+# the per-launch values agree to 0.2 %), scaled to another size by the units
+# each kernel processes: the fused kernel's bytes per grid cell, and the two
+# z-band kernels' bytes per band cell (nx * ny * 2P z-slab E nodes).
+NCU_FUSED_DRAM_BYTES_PER_CELL = 63.48
+NCU_BAND_DRAM_BYTES_PER_BAND_CELL = 193.0
+
+
+def step_traffic_bytes(shape, npml):
+    nx, ny, nz = shape
+    return NCU_FUSED_DRAM_BYTES_PER_CELL * nx * ny * nz + NCU_BAND_DRAM_BYTES_PER_BAND_CELL * nx * ny * 2 * npml
 
 
 def algorithmic_bytes_per_step(shape, npml):
@@ -368,7 +376,7 @@ def run_ours(args, rank, world):
     avg_launch_s = statistics.mean(per_launch_ms) / 1e3
     peak, peak_src = measured_peak()
     achieved = alg / avg_launch_s / 1e9
-    traffic = None if NCU_DRAM_BYTES_PER_CELL is None else NCU_DRAM_BYTES_PER_CELL * cells
+    traffic = step_traffic_bytes(shape, NPML)
     if shape != SHAPE:
         line_note = "scaled workload %dx%dx%d (not the headline size)" % tuple(shape)
     else:
@@ -386,6 +394,8 @@ def run_ours(args, rank, world):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "ncu dram bytes at 512x512x256, scaled per grid cell (fused kernel) "
+                                       "and per z-band cell (band kernels)",
                      "alg_bytes_per_launch": alg, "peak_source": peak_src,
                      "avg_launch_ms": avg_launch_s * 1e3,
                      "scope": "one time step (%d launch%s, timed together with CUDA events)"
@@ -687,6 +697,13 @@ def run_batched64(args):
     ms_seq = a.elapsed_time(b) / n
     cells = batch.cells
     info = batch.plan_info()
+    # one step = the batched fused launch plus the two batched z-band launches
+    # when any grid has a z face with CPML; bytes summed over the grids
+    band = any(sv.cpml.active and sv.cpml.npml[2] > 0 for sv in batch.solvers)
+    per_step = 3 if band else 1
+    alg = sum(algorithmic_bytes_per_step(sv.shape, sv.cpml.npml[0]) for sv in batch.solvers)
+    peak, peak_src = measured_peak()
+    achieved = alg / (ms_batch / 1e3) / 1e9
     line = _base_line("Mcell-updates/s (64 ragged Yee+CPML grids, one launch per step, FP32)",
                       cells / (ms_batch / 1e3) / 1e6, UNIT, args, ms_batch, "f32",
                       "64 grids, axes from {32..192 step 16}, 8-cell CPML, 10 spheres eps_r U[1,8] each, Ez "
@@ -694,7 +711,12 @@ def run_batched64(args):
                       {"sequential": {"value": cells / (ms_seq / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms_seq,
                                       "how": "the same 64 grids stepped one after another (single-grid plans)"},
                        "speedup_vs_sequential": ms_seq / ms_batch,
-                       "clocks": clocks, "gpu_launches": n})
+                       "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": None, "alg_bytes_per_launch": alg,
+                                    "peak_source": peak_src, "avg_launch_ms": ms_batch,
+                                    "scope": "one batched step (%d launch%s in the graph, timed together)"
+                                             % (per_step, "es" if per_step > 1 else "")},
+                       "clocks": clocks, "gpu_launches": n * per_step})
     line["config"]["tile"] = info
     line["config"]["autotune"] = tune
     print(json.dumps(line), flush=True)

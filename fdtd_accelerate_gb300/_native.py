@@ -114,6 +114,7 @@ _SIGS = {
     "fdtd_yee_plan_run": (C.c_int, [P, I64, I64, P]),
     "fdtd_yee_plan_current": (C.c_int, [P]),
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
+    "fdtd_yee_plan_test_timeout": (C.c_int, [P, I64, I32]),
     "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
     "fdtd_yee_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml), C.POINTER(Sources), P,

@@ -72,7 +72,7 @@ def build(force=False, verbose=False, extra_flags=()):
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        run([nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", tmp])
+        run([nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-ldl", "-o", tmp])
         os.replace(tmp, LIB)
     return LIB
 

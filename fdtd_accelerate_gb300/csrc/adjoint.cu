@@ -404,6 +404,7 @@ extern "C" {
 int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
                           const float *const h_prev[3], const float *const psi_e_cur[6], const float *const ce[3],
                           const fdtd_points *mon, const float *mon_grad, void *stream) {
+    NvtxRange nvtx_range("fdtd_adjoint_step");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
     if (!s || !h_prev || !ce) return FDTD_ERR_ARG;

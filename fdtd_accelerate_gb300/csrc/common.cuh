@@ -1,11 +1,22 @@
 // Shared helpers for the sm_103a kernels and the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "fdtd_gb300.h"
 
 namespace fdtd {
+
+// NVTX range around one step (or stage) of an entry point, for Nsight
+// Systems timelines and `ncu --nvtx` filters.  Header-only NVTX v3: without
+// an attached tool a push/pop pair is a call through a no-op pointer.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Thread-local record of the last CUDA error seen by an entry point.
 void set_cuda_error(cudaError_t e);

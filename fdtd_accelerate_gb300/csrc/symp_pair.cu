@@ -176,8 +176,10 @@ __device__ __forceinline__ float d4e(float fm1, float f0, float fp1, float fp2) 
 __global__ void __launch_bounds__(THREADS, 1)
 k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
     extern __shared__ unsigned char smem_raw[];
+    // 128-byte aligned base, computed from the shared-window offset so the
+    // pointer stays in the shared address space (shared loads, not generic ones)
     unsigned char *smem =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+        smem_raw + ((128u - (static_cast<uint32_t>(__cvta_generic_to_shared(smem_raw)) & 127u)) & 127u);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + OFF_BAR);  // E[NE], H[NH], CE[NC]
     auto sE = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_E + (sl * 3 + c) * EBOXB); };
     auto sH = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_H + (sl * 3 + c) * HBOXB); };
@@ -655,6 +657,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
 int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdtd_cpml *ch_tabs_b,
                        const fdtd_cpml *ce_tabs, float cl_a, float cl_b, int32_t two_h, float dl, float ch,
                        int64_t src_t, void *stream) {
+    NvtxRange nvtx_range("fdtd_symp_pair");
     if (!pl || (two_h != 0 && two_h != 1)) return FDTD_ERR_ARG;
     const int in = pl->cur, ob = 1 - pl->cur;
     Params p = pl->base;

@@ -421,6 +421,7 @@ int fdtd_symplectic_cpml_h_f32(const fdtd_grid *gp, const fdtd_cpml *c, float cl
 int fdtd_symplectic_stage_f32(const fdtd_grid *gp, const fdtd_cpml *cp, int32_t e_or_h, float coef,
                               float ch_scalar, float *const f[6], const float *const cf[3], const fdtd_psi *psi,
                               void *stream) {
+    NvtxRange nvtx_range("fdtd_symplectic_stage");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
     if (!f || (e_or_h != 0 && e_or_h != 1)) return FDTD_ERR_ARG;

@@ -144,6 +144,7 @@ extern "C" {
 int fdtd_symplectic_stage_f64(const fdtd_grid *gp, const fdtd_cpml *cp, int32_t e_or_h, double coef,
                               double ch_scalar, double *const f[6], const double *const cf[3],
                               double *const psi[6], void *stream) {
+    NvtxRange nvtx_range("fdtd_symplectic_stage_f64");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
     if (!f || (e_or_h != 0 && e_or_h != 1)) return FDTD_ERR_ARG;

@@ -174,6 +174,7 @@ extern "C" {
 int fdtd_step_unfused_f64(const fdtd_grid *gp, double *const f[6], const double *const ce[3], const fdtd_cpml *c,
                           double *const psi_e[6], double *const psi_h[6], const fdtd_sources *src, int64_t t,
                           void *stream) {
+    NvtxRange nvtx_range("fdtd_step_unfused_f64");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
     if (!f || !ce) return FDTD_ERR_ARG;

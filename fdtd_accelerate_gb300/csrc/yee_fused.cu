@@ -188,6 +188,8 @@ int fdtd_yee_plan_create(fdtd_yee_plan **out, const fdtd_grid *gp, const fdtd_ye
     p.x_chunk = pl->x_chunk;
     pl->nitems = (int64_t)p.ntz * p.nty * p.nxc;
     p.status = status_dev;
+    p.wait_ns = 0;         // the 1 s limit
+    p.test_withhold = -1;  // every copy issued
 
     const bool pml = c && (c->npml[0] > 0 || c->npml[1] > 0 || c->npml[2] > 0);
     if (pml) {
@@ -396,6 +398,7 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
         FDTD_TRY(tfsf_launch_1d(&pl->tfsf, 0, t0, st));
     }
     for (int64_t n = 0; n < nsteps; n++) {
+        NvtxRange nvtx_range("fdtd_yee_step");
         const int in = pl->cur, outb = 1 - pl->cur;
         Params p = pl->base;
         for (int q = 0; q < 6; q++) {
@@ -424,6 +427,13 @@ int fdtd_yee_plan_run(fdtd_yee_plan *pl, int64_t t0, int64_t nsteps, void *strea
 }
 
 int fdtd_yee_plan_current(const fdtd_yee_plan *pl) { return pl ? pl->cur : -1; }
+
+int fdtd_yee_plan_test_timeout(fdtd_yee_plan *pl, int64_t wait_ns, int32_t withhold_plane) {
+    if (!pl || wait_ns < 0 || withhold_plane < -1) return FDTD_ERR_ARG;
+    pl->base.wait_ns = (uint64_t)wait_ns;
+    pl->base.test_withhold = withhold_plane;
+    return FDTD_OK;
+}
 
 int fdtd_yee_plan_set_current(fdtd_yee_plan *pl, int32_t cur) {
     if (!pl || (cur != 0 && cur != 1)) return FDTD_ERR_ARG;
@@ -622,6 +632,7 @@ int fdtd_batch_plan_run(fdtd_batch_plan *bp, int64_t t0, int64_t nsteps, void *s
     memset(&dummy_maps, 0, sizeof(dummy_maps));
     Params dummy{};
     for (int64_t n = 0; n < nsteps; n++) {
+        NvtxRange nvtx_range("fdtd_batch_step");
         BatchDesc bd{};
         bd.nsims = bp->nsims;
         bd.cur = bp->cur;

@@ -128,6 +128,12 @@ struct Params {
     float tcoef[2][6][2];
     int32_t tix[2][6][2];
     const float *te1d, *th1d;
+    // test hook of single-grid plans (plan creation sets 0 and -1): wait_ns > 0
+    // replaces the 1 s wait limit; test_withhold >= 0 makes CTA 0 skip the
+    // copies of that plane of its first work item, so its wait runs out with
+    // no copy in flight.
+    uint64_t wait_ns;
+    int32_t test_withhold;
 };
 
 // Many independent grids advanced by one launch: work items of all grids are
@@ -176,16 +182,17 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
-// Bounded wait: true on completion; false after WAIT_NS, or early when
+// Bounded wait: true on completion; false after limit_ns, or early when
 // another CTA has already recorded a timeout in the status word (status may
 // be null: then only the deadline applies).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, const int32_t *status) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, const int32_t *status,
+                                                  uint64_t limit_ns = WAIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t n = 1;; n++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((n & 255) == 0) {
-            if (globaltimer_ns() - t0 > WAIT_NS) return false;
+            if (globaltimer_ns() - t0 > limit_ns) return false;
             if (status && *(volatile const int32_t *)status == FDTD_ERR_TIMEOUT) return false;
         }
     }
@@ -371,8 +378,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     static_assert(NS >= 3, "the fused pipeline needs at least 3 stages");
     static_assert((2 * NS + 2) * 8 <= 128, "the mbarriers live in 128 bytes");
     extern __shared__ unsigned char smem_raw[];
+    // 128-byte aligned base, computed from the shared-window offset so the
+    // pointer stays in the shared address space (shared loads, not generic ones)
     unsigned char *smem =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+        smem_raw + ((128u - (static_cast<uint32_t>(__cvta_generic_to_shared(smem_raw)) & 127u)) & 127u);
     // stage size: read from the kernel parameters at each use (a constant-bank
     // operand) rather than held in a register
 #define FDTD_SB (BATCH ? bd.stage_bytes : pk.stage_bytes)
@@ -468,6 +477,8 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
     int64_t psi_hi = -1;      // highest plane whose psi boxes were issued (tid 0)
     int64_t q_abort = 0, i_start_abort = 0;
     bool aborted = false;
+    const uint64_t wlim = (!BATCH && pk.wait_ns) ? pk.wait_ns : WAIT_NS;
+    bool first_item = true;
     const int64_t nitems = BATCH ? bd.item_off[bd.nsims] : (int64_t)pk.ntz * pk.nty * pk.nxc;
     int cur_sim = -1;
 
@@ -556,6 +567,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             const int64_t plane = i_start + q;
             const int st = (int)((g0 + q) % NS);
             uint64_t *bar = &bars[st], *bare = &bars[NS + st];
+            if (!BATCH && first_item && blockIdx.x == 0 && q == pk.test_withhold) return;  // test hook
             issued_hi = q;
             if (plane >= p.nx) {
                 // Past the last plane: H(p.nx) only feeds E components that are
@@ -675,9 +687,10 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             // every thread's reads).  Plane q+1 is needed for its H only:
             // its E and CE have one more iteration to arrive.
             if (producer &&
-                (!mbar_wait_bounded(&bars[st], par, p.status) || !mbar_wait_bounded(&bars[st1], par1, p.status) ||
-                 !mbar_wait_bounded(&bars[NS + st], par, p.status) ||
-                 !mbar_wait_bounded(&bars[2 * NS + psl], (Gp >> 1) & 1, p.status)))
+                (!mbar_wait_bounded(&bars[st], par, p.status, wlim) ||
+                 !mbar_wait_bounded(&bars[st1], par1, p.status, wlim) ||
+                 !mbar_wait_bounded(&bars[NS + st], par, p.status, wlim) ||
+                 !mbar_wait_bounded(&bars[2 * NS + psl], (Gp >> 1) & 1, p.status, wlim)))
                 s_abort = 1;
             __syncthreads();  // (A) H of planes q, q+1, E and CE of q visible; iteration q-1 finished everywhere
             if (s_abort) {
@@ -908,6 +921,7 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             }
         }
         if (aborted) break;
+        first_item = false;
         g0 += (uint32_t)nplanes;
         gp0 += (uint32_t)(nplanes - 1);  // one psi phase per iteration
         issued_hi = -1;
@@ -939,12 +953,12 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
             for (int64_t q = q_abort; q <= issued_hi; q++) {
                 if (i_start_abort + q >= p.nx) continue;
                 const uint32_t G = g0 + (uint32_t)q;
-                mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr);
-                mbar_wait_bounded(&bars[NS + G % NS], (G / NS) & 1, nullptr);
+                mbar_wait_bounded(&bars[G % NS], (G / NS) & 1, nullptr, wlim);
+                mbar_wait_bounded(&bars[NS + G % NS], (G / NS) & 1, nullptr, wlim);
             }
             for (int64_t q = q_abort; q <= psi_hi; q++) {
                 const uint32_t Gp = gp0 + (uint32_t)q;
-                mbar_wait_bounded(&bars[2 * NS + (Gp & 1)], (Gp >> 1) & 1, nullptr);
+                mbar_wait_bounded(&bars[2 * NS + (Gp & 1)], (Gp >> 1) & 1, nullptr, wlim);
             }
         }
         __syncthreads();

@@ -442,6 +442,7 @@ int fdtd_drude_update_e_f32(const fdtd_grid *gp, const fdtd_drude *d, float *ex,
 int fdtd_step_unfused_f32(const fdtd_grid *gp, float *const f[6], const float *const ce[3],
                           const float *const ch[3], const fdtd_cpml *c, const fdtd_psi *psi,
                           const fdtd_sources *src, int64_t t, void *stream) {
+    NvtxRange nvtx_range("fdtd_step_unfused");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
     if (!f || !ce) return FDTD_ERR_ARG;

@@ -210,6 +210,13 @@ class YeeSolver:
                         N.call("fdtd_tfsf_update_h_f32", C.byref(g), C.byref(t), *H, stream)
                 self.tstep += 1
 
+    def test_timeout(self, wait_ns=0, withhold_plane=-1):
+        """Set the plan's bounded-wait test hook (fdtd_yee_plan_test_timeout):
+        wait_ns > 0 shortens every wait of the fused kernel, withhold_plane >= 0
+        makes CTA 0 skip that plane's copies so its wait runs out.  The defaults
+        restore normal operation."""
+        N.call("fdtd_yee_plan_test_timeout", self.plan(), int(wait_ns), int(withhold_plane))
+
     def check_status(self):
         """Raise if a bounded device wait expired in an earlier step."""
         v = int(self.status.item())

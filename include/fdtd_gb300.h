@@ -247,6 +247,14 @@ int fdtd_yee_plan_create(fdtd_yee_plan **plan, const fdtd_grid *g, const fdtd_ye
 int fdtd_yee_plan_run(fdtd_yee_plan *plan, int64_t t0, int64_t nsteps, void *stream);
 int fdtd_yee_plan_current(const fdtd_yee_plan *plan);
 int fdtd_yee_plan_set_current(fdtd_yee_plan *plan, int32_t cur);
+/* Test hook for the bounded device waits (no reference counterpart: the
+ * reference's kernels never wait on a copy).  wait_ns > 0 replaces the 1 s
+ * limit of every mbarrier wait of the plan's fused kernel (0 restores it);
+ * withhold_plane >= 0 makes CTA 0 skip the copies of that plane of its first
+ * work item, so that its wait runs out with no copy in flight, the kernel
+ * writes FDTD_ERR_TIMEOUT to status_dev and every CTA returns; -1 issues
+ * every copy.  The aborted step leaves the output buffer partly written. */
+int fdtd_yee_plan_test_timeout(fdtd_yee_plan *plan, int64_t wait_ns, int32_t withhold_plane);
 /* info[0..5] = tile_y, stages, x_chunk, CTAs launched, threads/CTA, shared bytes/CTA;
  * with n >= 8 also info[6] = 1 when the z slab runs on the band kernels and
  * info[7] = kernel launches per step */

@@ -1,8 +1,8 @@
 """Recipe: compile pieces of the reference's own CPU code into oracle/_ref/.
 
 Test infrastructure only.  Runs where the reference checkout is present
-(FDTD_REFERENCE_ROOT, default /root/reference) and the host is x86_64 (the
-reference's C uses SSE intrinsics).  Nothing is copied into the repository:
+(FDTD_REFERENCE_ROOT, else the checkout location this recipe names in REF)
+and the host is x86_64 (the reference's C uses SSE intrinsics).  Nothing is copied into the repository:
 sources are read in place and every artefact lands in oracle/_ref/
 (git-ignored).
 
@@ -30,6 +30,7 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+# the reference checkout: FDTD_REFERENCE_ROOT, else where this build recipe reads it
 REF = os.environ.get("FDTD_REFERENCE_ROOT", "/root/reference")
 
 KEMP_SRC = "KEMP/v0.7_pml/fdtd3d/cpu/src/core.c"

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run here, where the reference checkout exists (FDTD_REFERENCE_ROOT, default
-/root/reference), after ``python oracle/build_ref.py``:
+Run where the reference checkout exists (FDTD_REFERENCE_ROOT, else the
+location oracle/build_ref.py reads), after ``python oracle/build_ref.py``:
 
     python tests/golden/make_golden.py
 
@@ -32,9 +32,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("FDTD_REFERENCE_ROOT", "/root/reference")
-
 from oracle import build_ref  # noqa: E402
+
+REF = build_ref.REF
 
 F32 = np.float32
 

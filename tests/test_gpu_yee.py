@@ -298,6 +298,45 @@ def test_fused_then_unfused_interleave(fdtd):
         np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)
 
 
+def test_bounded_wait_expires_and_solver_recovers(fdtd):
+    """A pipeline wait that runs out: CTA 0 withholds the copies of one plane
+    (nothing is in flight for it), its wait gives up after the shortened limit,
+    the kernel records FDTD_ERR_TIMEOUT and returns; the context and the plan
+    stay usable, and with the hook cleared the same plan steps bit-exactly."""
+    import time
+    shape, npml = (37, 29, 45), 5
+    rng = np.random.default_rng(23)
+    init = {k: (0.1 * rng.standard_normal(shape)).astype(np.float32) for k in NAMES}
+    t = np.arange(8, dtype=np.float64)
+    sources = [("ez", (18, 14, 22), fdtd.gaussian_sine(t, 3.0, 2.0, 0.1))]
+    a = fdtd.YeeSolver(shape, npml=npml, sources=sources)
+    a.set_fields(**init)
+    a.test_timeout(wait_ns=20_000_000, withhold_plane=1)   # 20 ms limit
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a.step(1)
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 5.0
+    with pytest.raises(TimeoutError):
+        a.check_status()
+    assert int(a.status.item()) == 0   # check_status cleared the word
+
+    # same plan, hook cleared, state reset: bit-exact against a fresh solver
+    a.test_timeout()
+    a.cpml.reset()
+    a.cur, a.tstep = 0, 1
+    a.set_fields(**init)
+    b = fdtd.YeeSolver(shape, npml=npml, sources=sources)
+    b.set_fields(**init)
+    a.step(4)
+    b.step(4)
+    torch.cuda.synchronize()
+    a.check_status()
+    b.check_status()
+    for k in NAMES:
+        np.testing.assert_array_equal(_host(a.fields[k]), _host(b.fields[k]), err_msg=k)
+
+
 def test_api_errors(fdtd):
     a = torch.zeros((4, 5, 6), device="cuda")
     with pytest.raises(TypeError):

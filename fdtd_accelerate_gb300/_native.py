@@ -131,7 +131,7 @@ _SIGS = {
                                             C.POINTER(P * 6), C.POINTER(P * 3), C.POINTER(P * 6), P]),
     "fdtd_add_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_symp_pair_plan_create": (C.c_int, [C.POINTER(P), C.POINTER(Grid), C.POINTER(SympState),
-                                             C.POINTER(Sources), I32, I32, P, P]),
+                                             C.POINTER(Sources), I32, I32, P, P, P]),
     "fdtd_symp_pair_run": (C.c_int, [P, C.POINTER(Cpml), C.POINTER(Cpml), C.POINTER(Cpml), F32, F32, I32, F32,
                                      F32, I64, P]),
     "fdtd_symp_pair_plan_current": (C.c_int, [P]),

@@ -9,25 +9,37 @@
 //   fdtd_symplectic_stage_f32(E, dl), sources,
 // with the same round-to-nearest operations, so the result is bit-identical.
 //
-// Design (2.5-D blocking)
+// Design (2.5-D blocking, 4 z cells per thread)
 //  * Ping-pong state: the pass reads buffer `cur` (E, H) and writes `1-cur`;
 //    the H psi slabs ping-pong too (halo H cells are recomputed from the
 //    input psi), the E psi slabs are updated in place (only their owner
 //    touches them).
 //  * A CTA owns TZ = 32 (z) x TY = 16 (y) cells for a chunk of x planes and
 //    marches along x.  E_new(i) needs H_new on planes i-1 .. i+2 and on the
-//    rows/columns -1 .. +2 around the tile, so H_new is computed on
-//    (TY+3) x (TZ+3) cells: one thread per cell column (j, k), the 512 tile
-//    columns first, then the 153 halo columns.  Each thread keeps the x
-//    neighbours it needs in registers: the input E of planes m-2 .. m+1 for
-//    H_new(m), and its own H_new of planes i-1 .. i+2 for E_new(i).  Shared
-//    memory holds one plane with its y/z halo: input E boxes (4-slot ring),
-//    input H and CE boxes (3-slot rings, 3-D TMA, issued two planes ahead)
-//    and H_new (3-slot ring).
-//  * Iteration q: input plane p arrives; every thread computes H_new(p-1) at
-//    its column; tile threads then compute E_new(p-3).  One CTA barrier per
+//    rows/columns -1 .. +2 around the tile, so H_new is computed on the rows
+//    j0-1 .. j0+TY+1 and the columns k0-4 .. k0+TZ+3, in groups of 4 z cells:
+//    one thread per group, the 128 tile groups first (those threads also
+//    compute E_new of their group), then the 62 halo groups.  Every group is
+//    16-byte aligned, so its z window (the group and the neighbouring
+//    groups) is three 16-byte shared loads.
+//  * Each thread keeps the x neighbours it needs in registers: the input E of
+//    planes m-3 .. m-1 for H_new(m-1), and its own H_new (hy, hz) of planes
+//    i-1 .. i+1 for E_new(i).  Shared memory holds one plane with its y/z
+//    halo: input E boxes (4-slot ring) and H boxes (3-slot ring), both issued
+//    two planes ahead, CE boxes (2-slot ring, one plane ahead) and H_new
+//    (3-slot ring).  About 108 KB, two CTAs per SM.
+//  * Iteration q: input plane p arrives; every thread computes H_new(p-1) for
+//    its group; tile threads then compute E_new(p-3).  One CTA barrier per
 //    iteration: H_new(p-1) is read by neighbours two iterations later.
-//  * Lane 0 of the last warp is the producer: it waits on the mbarriers and
+//  * Warps whose groups lie in no CPML slab on a plane outside the x slabs
+//    take a path without psi code; the others run the CPML terms cell by
+//    cell in the operation order of the stage kernels, each component's psi
+//    values of the 4 cells loaded together.
+//  * CTAs draw work items from a device queue (two ints the caller provides,
+//    cleared by the last CTA of each launch).  With y or z slabs the edge
+//    tiles, which carry them, are handed out first, so a launch ends on
+//    interior tiles.
+//  * Lane 31 of the last warp is the producer: it waits on the mbarriers and
 //    issues the copies.  Every wait is bounded (1 s); on expiry the CTA
 //    records FDTD_ERR_TIMEOUT, drains its copies and stops.
 #include <cuda.h>
@@ -41,28 +53,26 @@ namespace fdtd {
 namespace sp {
 
 constexpr int TZ = 32, TY = 16;
-constexpr int BW = TZ + 8;          // box width: k0-4 .. k0+TZ+3
+constexpr int NG = TZ / 4 + 2;      // groups per H row: columns k0-4 .. k0+TZ+3
+constexpr int BW = TZ + 8;          // row width of the E, H and H_new boxes (column k0-4 first)
 constexpr int ER = TY + 6;          // E box rows: j0-3 .. j0+TY+2
-constexpr int HOR = TY + 3;         // H box rows: j0-1 .. j0+TY+1
-constexpr int HNR = TY + 3;         // H_new rows: j0-1 .. j0+TY+1
-constexpr int HNC = TZ + 3;         // H_new columns: k0-1 .. k0+TZ+1
-constexpr int HNP = 36;             // H_new row pitch
-constexpr int NE = 4, NH = 3, NC = 3, NHN = 3;  // ring depths (E, H, CE inputs; H_new)
-constexpr int NOWN = TY * TZ;                   // tile columns (threads 0 .. NOWN-1)
-constexpr int NHALO = HNR * HNC - NOWN;         // halo H columns
-constexpr int NCW = (NOWN + NHALO + 31) / 32;   // compute warps
-constexpr int THREADS = (NCW + 1) * 32;         // + the producer warp
+constexpr int HOR = TY + 3;         // H and H_new rows: j0-1 .. j0+TY+1
+constexpr int NE = 4, NH = 3, NC = 2, NHN = 3;  // ring depths (E, H, CE inputs; H_new)
+constexpr int NTILE = TY * (TZ / 4);            // tile groups (threads 0 .. NTILE-1)
+constexpr int NHALO = HOR * NG - NTILE;         // halo groups
+constexpr int THREADS = (NTILE + NHALO + 1 + 31) / 32 * 32;
+constexpr int PRODUCER = THREADS - 1;
 constexpr int MAX_SRC = 64;                     // sources per work item
 constexpr uint64_t WAIT_NS = 1000000000ull;
+static_assert(NTILE + NHALO < PRODUCER, "the producer lane computes no group");
 
 constexpr int al128(int b) { return (b + 127) / 128 * 128; }
 constexpr int EBOXB = al128(ER * BW * 4), HBOXB = al128(HOR * BW * 4), CBOXB = al128(TY * TZ * 4);
-constexpr int HNB = al128(HNR * HNP * 4);
 constexpr int OFF_E = 0;
 constexpr int OFF_H = OFF_E + NE * 3 * EBOXB;
 constexpr int OFF_C = OFF_H + NH * 3 * HBOXB;
 constexpr int OFF_HN = OFF_C + NC * 3 * CBOXB;
-constexpr int OFF_BAR = OFF_HN + NHN * 3 * HNB;
+constexpr int OFF_BAR = OFF_HN + NHN * 3 * HBOXB;
 constexpr int SMEM = OFF_BAR + 128 + 128 /*align slack*/;
 static_assert((NE + NH + NC) * 8 <= 128, "the mbarriers live in 128 bytes");
 
@@ -90,11 +100,15 @@ struct Params {
     float clch_a, clch_b;     // cl * ch as one single-precision product
     int32_t hh;               // 1: two H stages (a then b) before the E stage
     int32_t cpml;             // any slab
+    int32_t edge_first;       // y or z slabs: edge tiles first in the work order
     int32_t nsrc;
     const int32_t *src_ijk, *src_comp;
     const float *src_amp;
     int64_t namp, t;          // amplitude table length and the index used
     int32_t *status;
+    // work queue: [0] next item, [1] CTAs finished; zero between launches (the
+    // last CTA to finish clears both)
+    int32_t *queue;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -159,10 +173,19 @@ __device__ __forceinline__ uint32_t psi_index(const Params &p, int ax, int s, in
     return ax == 0 ? ((uint32_t)s * p.ny + j) * p.nz + k
                    : (ax == 1 ? ((uint32_t)i * twoP + s) * p.nz + k : ((uint32_t)i * p.ny + j) * twoP + s);
 }
+// CPML tables of one stage along one axis
+struct Tab {
+    const float *b, *a, *km1;
+};
+__device__ __forceinline__ Tab tab(const Axis &A) { return Tab{A.b, A.a, A.km1}; }
+// the tables of H stage b (st = 1) or a, selected by value
+__device__ __forceinline__ Tab tab_h(const Params &p, int st, int ax) {
+    return Tab{st ? p.hb[ax].b : p.ha[ax].b, st ? p.hb[ax].a : p.ha[ax].a, st ? p.hb[ax].km1 : p.ha[ax].km1};
+}
 // psi <- b psi + a d; returns (coef * cv) * (km1 d + psi)
-__device__ __forceinline__ float sterm(const Axis &A, int s, float &psi, float d, float coef, float cv) {
-    psi = fadd(fmul(A.b[s], psi), fmul(A.a[s], d));
-    return fmul(fmul(coef, cv), fadd(fmul(A.km1[s], d), psi));
+__device__ __forceinline__ float sterm(const Tab &T, int s, float &psi, float d, float coef, float cv) {
+    psi = fadd(fmul(__ldg(T.b + s), psi), fmul(__ldg(T.a + s), d));
+    return fmul(fmul(coef, cv), fadd(fmul(__ldg(T.km1 + s), d), psi));
 }
 // 4th-order difference of an H node: 27 (F0 - Fm1) - (Fp1 - Fm2)
 __device__ __forceinline__ float d4h(float fm2, float fm1, float f0, float fp1) {
@@ -173,7 +196,77 @@ __device__ __forceinline__ float d4e(float fm1, float f0, float fp1, float fp2) 
     return fsub(fmul(27.0f, fsub(fp1, f0)), fsub(fp2, fm1));
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
+// four consecutive floats of shared memory (16-byte aligned)
+struct V4 {
+    float v[4];
+};
+__device__ __forceinline__ V4 lds4(const float *s) {
+    const float4 t = *reinterpret_cast<const float4 *>(s);
+    return V4{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ void sts4(float *s, const V4 &a) {
+    *reinterpret_cast<float4 *>(s) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+}
+// z window of a group: w(d) = the value at z offset d (-4 .. 7) from the
+// group's first cell, from the loads of the groups left (L), own (C), right (R)
+struct ZW {
+    V4 L, C, R;
+    __device__ __forceinline__ float at(int d) const {
+        return d < 0 ? L.v[d + 4] : (d < 4 ? C.v[d] : R.v[d - 4]);
+    }
+};
+
+// global store of a group's 4 values (cells k .. k+3 of a row); cells at
+// z >= nz are not stored
+__device__ __forceinline__ void stg4(float *row, int k, int nz, const V4 &a) {
+    if (k + 3 < nz) {
+        *reinterpret_cast<float4 *>(row + k) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+    } else {
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            if (k + c < nz) row[k + c] = a.v[c];
+    }
+}
+
+// Work item u -> tile (tzi, tyi) and x chunk xci.  The y/z edge tiles (first
+// or last tile row or column) of every x chunk come first, then the interior
+// tiles; inside each part the z tile runs fastest, then the y tile, then the
+// x chunk.
+__device__ __forceinline__ void item_tile(const Params &p, int u, int &tzi, int &tyi, int &xci) {
+    const int nz = p.ntz, ny = p.nty;
+    const int ni = (nz > 2 && ny > 2) ? (nz - 2) * (ny - 2) : 0;  // interior tiles per chunk
+    const int ne = nz * ny - ni;                                   // edge tiles per chunk
+    if (!p.edge_first) {  // z tile fastest, then y tile, then x chunk
+        tzi = u % nz;
+        tyi = (u / nz) % ny;
+        xci = u / (nz * ny);
+        return;
+    }
+    if (u < ne * p.nxc) {
+        xci = u / ne;
+        const int e = u - xci * ne;
+        if (e < 2 * nz || ni == 0) {  // the first and last tile rows (all tiles when ni == 0)
+            const int r = ni == 0 ? e / nz : (e < nz ? 0 : ny - 1);
+            tyi = r;
+            tzi = ni == 0 ? e - r * nz : (e < nz ? e : e - nz);
+        } else {                      // the first and last tile of each inner row
+            const int f = e - 2 * nz;
+            tyi = 1 + (f >> 1);
+            tzi = (f & 1) ? nz - 1 : 0;
+        }
+    } else {
+        const int v = u - ne * p.nxc;
+        xci = v / ni;
+        const int r = v - xci * ni;
+        tyi = 1 + r / (nz - 2);
+        tzi = 1 + r % (nz - 2);
+    }
+}
+
+// HH: two H stages before the E stage (the pass that merges the closing H
+// stage of a step with the opening one of the next)
+template <bool HH>
+__global__ void __launch_bounds__(THREADS, 2)
 k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
     extern __shared__ unsigned char smem_raw[];
     // 128-byte aligned base, computed from the shared-window offset so the
@@ -184,49 +277,57 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
     auto sE = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_E + (sl * 3 + c) * EBOXB); };
     auto sH = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_H + (sl * 3 + c) * HBOXB); };
     auto sC = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_C + (sl * 3 + c) * CBOXB); };
-    auto sN = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_HN + (sl * 3 + c) * HNB); };
-    __shared__ int s_abort, s_nls;
+    auto sN = [&](int sl, int c) { return reinterpret_cast<float *>(smem + OFF_HN + (sl * 3 + c) * HBOXB); };
+    __shared__ int s_abort, s_nls, s_item;
     __shared__ int s_ls_i[MAX_SRC], s_ls_j[MAX_SRC], s_ls_kc[MAX_SRC], s_ls_s[MAX_SRC];
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool producer = tid == NCW * 32;
+    const int tid = threadIdx.x;
+    const bool producer = tid == PRODUCER;
     if (tid == 0) {
         for (int s = 0; s < NE + NH + NC; s++) mbar_init(&bars[s]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         s_abort = 0;
     }
-    // the H_new column (hr, hc) of this thread: tile columns first (warp = row,
-    // lane = column), then the halo: rows j0-1, j0+TY, j0+TY+1, then the
-    // columns k0-1, k0+TZ, k0+TZ+1 of the tile rows
-    int hr = 0, hc = 0;
-    const bool e_thread = tid < NOWN, h_thread = tid < NOWN + NHALO;
+    // the group of this thread: H row hr (j0-1+hr), group g (columns
+    // k0-4+4g .. k0-1+4g).  Tile groups first (row hr = 1 + tid/8, groups
+    // 1 .. 8), then the halo: rows 0, TY+1, TY+2 (all groups), then groups 0
+    // and NG-1 of the tile rows.
+    int hr = 0, g = 0;
+    const bool e_thread = tid < NTILE, h_thread = tid < NTILE + NHALO;
     if (e_thread) {
-        hr = warp + 1;
-        hc = lane + 1;
+        hr = 1 + tid / (TZ / 4);
+        g = 1 + tid % (TZ / 4);
     } else if (h_thread) {
-        const int h = tid - NOWN;
-        if (h < 3 * HNC) {
-            const int band = h / HNC;
+        const int h = tid - NTILE;
+        if (h < 3 * NG) {
+            const int band = h / NG;
             hr = band == 0 ? 0 : TY + band;
-            hc = h - band * HNC;
+            g = h - band * NG;
         } else {
-            const int g = (h - 3 * HNC) / TY;
-            hr = 1 + (h - 3 * HNC) - g * TY;
-            hc = g == 0 ? 0 : TZ + g;
+            const int u = h - 3 * NG;
+            hr = 1 + (u >> 1);
+            g = (u & 1) ? NG - 1 : 0;
         }
     }
-    const int eo = (hr + 2) * BW + hc + 3;   // E box element of the column (row j0-3.., column k0-4..)
-    const int ho = hr * BW + hc + 3;         // H box element (row j0-1..)
-    const int no = hr * HNP + hc;            // H_new element (row j0-1.., column k0-1..)
-    const int co = warp * TZ + lane;         // CE element (tile threads)
+    const int col = 4 * g;                                   // first box column of the group
+    const int colL = g == 0 ? col : col - 4;                 // left and right neighbour groups (clamped:
+    const int colR = g == NG - 1 ? col : col + 4;            // the cells that would use them are not needed)
+    const int eo = (hr + 2) * BW + col;                      // E box element of the group (row j0-3..)
+    const int ho = hr * BW + col;                            // H and H_new box element (row j0-1..)
+    const int co = (hr - 1) * TZ + col - 4;                  // CE box element (tile threads)
 
     uint32_t gE = 0, gH = 0, gC = 0;  // ring uses before the current item
     bool aborted = false;
     const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
-    for (int64_t item = blockIdx.x; item < nitems && !aborted; item += gridDim.x) {
-        const int tzi = (int)(item % p.ntz), tyi = (int)((item / p.ntz) % p.nty);
-        const int xci = (int)(item / ((int64_t)p.ntz * p.nty));
+    // items from the work queue (item_tile gives the order: the y/z edge tiles,
+    // which carry the y and z CPML slabs, first): CTAs that drew cheaper tiles
+    // take more of them, and the last items of a launch are interior tiles
+    if (tid == 0) s_item = atomicAdd(&p.queue[0], 1);
+    __syncthreads();
+    for (int64_t item = s_item; item < nitems && !aborted;) {
+        int tzi, tyi, xci;
+        item_tile(p, (int)item, tzi, tyi, xci);
         const int k0 = tzi * TZ, j0 = tyi * TY, x0 = xci * p.x_chunk;
         const int x1 = min(x0 + p.x_chunk, p.nx);
         // iteration q: input plane p = x0 - 3 + q arrives; H_new(p-1) for
@@ -240,7 +341,7 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         auto ephase = [&](int q) { return ((gE + (uint32_t)q) / NE) & 1; };
         auto hphase = [&](int q) { return ((gH + (uint32_t)(q - 3)) / NH) & 1; };
         auto cphase = [&](int q) { return ((gC + (uint32_t)(q - 6)) / NC) & 1; };
-        auto issue = [&](int q) {  // copies needed at iteration q (issued two iterations ahead)
+        auto issue_eh = [&](int q) {  // E and H copies of iteration q (issued two iterations ahead)
             const int pl = x0 - 3 + q;
             {   // E(p)
                 const int sl = eslot(q);
@@ -254,12 +355,12 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 mbar_expect(bar, 3u * HOR * BW * 4);
                 for (int c = 0; c < 3; c++) tma3(sH(sl, c), &mk.h[c], bar, k0 - 4, j0 - 1, pl - 1);
             }
-            if (q >= 6) {  // CE(p-3)
-                const int sl = cslot(q);
-                uint64_t *bar = &bars[NE + NH + sl];
-                mbar_expect(bar, 3u * TY * TZ * 4);
-                for (int c = 0; c < 3; c++) tma3(sC(sl, c), &mk.ce[c], bar, k0, j0, pl - 3);
-            }
+        };
+        auto issue_c = [&](int q) {  // CE(p-3) of iteration q >= 6 (issued one iteration ahead)
+            const int sl = cslot(q);
+            uint64_t *bar = &bars[NE + NH + sl];
+            mbar_expect(bar, 3u * TY * TZ * 4);
+            for (int c = 0; c < 3; c++) tma3(sC(sl, c), &mk.ce[c], bar, k0, j0, x0 + q - 6);
         };
         if (tid == 0) {  // sources of this item's tile, list order
             int n = 0;
@@ -284,27 +385,44 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         }
         __syncthreads();  // previous item finished everywhere; source list ready
         if (producer) {
-            issue(0);
-            issue(1);
+            issue_eh(0);
+            if (Q > 1) issue_eh(1);
         }
         const int nls = s_nls;
-        const int j = j0 - 1 + hr, k = k0 - 1 + hc;
-        const bool col_in = h_thread && j >= 0 && j < p.ny && k >= 0 && k < p.nz;
-        const bool jin_h = j > 1 && j < p.ny - 1, kin_h = k > 1 && k < p.nz - 1;
-        const bool jin_e = j > 0 && j < p.ny - 2, kin_e = k > 0 && k < p.nz - 2;
-        const bool own_col = e_thread;
-        // y/z slab indices of the column (H nodes for the H stages, E nodes for the E stage)
-        int syh = -1, szh = -1, sye = -1, sze = -1;
-        if (p.cpml && col_in) {
-            syh = slab(p.ha[1], j, p.ny, false);
-            szh = slab(p.ha[2], k, p.nz, false);
-            sye = slab(p.ea[1], j, p.ny, true);
-            sze = slab(p.ea[2], k, p.nz, true);
+        const int j = j0 - 1 + hr, kg = k0 - 4 + col;   // row and first z cell of the group
+        const bool row_in = h_thread && j >= 0 && j < p.ny;
+        const bool jin_h = j > 1 && j < p.ny - 1, jin_e = j > 0 && j < p.ny - 2;
+        // per-cell z masks of the group (bit c: cell kg+c)
+        uint32_t kin_h = 0, kin_e = 0, k_in = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int k = kg + c;
+            kin_h |= (uint32_t)(k > 1 && k < p.nz - 1) << c;
+            kin_e |= (uint32_t)(k > 0 && k < p.nz - 2) << c;
+            k_in |= (uint32_t)(k >= 0 && k < p.nz) << c;
         }
-        // register queues of the column: input E of planes p-3 .. p-1 (ex, ey, ez),
+        // CPML: y slab of the row (H and E nodes); any z-slab cell in the group
+        int syh = -1, sye = -1;
+        bool zh_any = false, ze_any = false;
+        if (p.cpml && row_in) {
+            syh = slab(p.ha[1], j, p.ny, false);
+            sye = slab(p.ea[1], j, p.ny, true);
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                zh_any |= slab(p.ha[2], kg + c, p.nz, false) >= 0;
+                ze_any |= slab(p.ea[2], kg + c, p.nz, true) >= 0;
+            }
+        }
+        // the path choice is made per warp: a warp with any slab cell runs the
+        // CPML path for all its lanes (it handles plain cells as well), so it
+        // never runs both paths one after the other
+        const bool yz_h = __any_sync(0xffffffffu, syh >= 0 || zh_any);
+        const bool yz_e = __any_sync(0xffffffffu, sye >= 0 || ze_any);
+
+        // register queues of the group: input E of planes p-3 .. p-1 (ex, ey, ez),
         // own H_new of planes p-4 .. p-2 (hy, hz)
-        float e0x = 0.f, e0y = 0.f, e0z = 0.f, e1x = 0.f, e1y = 0.f, e1z = 0.f, e2x = 0.f, e2y = 0.f, e2z = 0.f;
-        float n0y = 0.f, n0z = 0.f, n1y = 0.f, n1z = 0.f, n2y = 0.f, n2z = 0.f;
+        V4 e0x{}, e0y{}, e0z{}, e1x{}, e1y{}, e1z{}, e2x{}, e2y{}, e2z{};
+        V4 n0y{}, n0z{}, n1y{}, n1z{}, n2y{}, n2z{};
         int q_abort = 0;
         for (int q = 0; q < Q; q++) {
             const int pl = x0 - 3 + q;
@@ -321,188 +439,321 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 q_abort = q;
                 break;
             }
-            if (producer && q + 2 < Q) issue(q + 2);
-
-            // input E of plane p at this column
-            float e3x = 0.f, e3y = 0.f, e3z = 0.f;
-            if (h_thread) {
-                e3x = sE(eS, 0)[eo];
-                e3y = sE(eS, 1)[eo];
-                e3z = sE(eS, 2)[eo];
+            if (producer) {
+                if (q + 2 < Q) issue_eh(q + 2);
+                if (q + 1 < Q && q + 1 >= 6) issue_c(q + 1);
             }
-            // ---- H_new(m), m = p - 1, at this column ----
+
+            // input E of plane p at this group
+            V4 e3x{}, e3y{}, e3z{};
+            if (h_thread) {
+                e3x = lds4(sE(eS, 0) + eo);
+                e3y = lds4(sE(eS, 1) + eo);
+                e3z = lds4(sE(eS, 2) + eo);
+            }
+            // ---- H_new(m), m = p - 1, at this group ----
             const int m = pl - 1;
-            float hny = 0.f, hnz = 0.f;
-            if (q >= 3 && col_in && m >= 0 && m < p.nx) {
+            V4 hny{}, hnz{};
+            if (q >= 3 && row_in && m >= 0 && m < p.nx) {
                 const int eSm = eslot(q - 1), hS = hslot(q);
                 const float *ex = sE(eSm, 0), *ey = sE(eSm, 1), *ez = sE(eSm, 2);
-                const float hx0 = sH(hS, 0)[ho], hy0 = sH(hS, 1)[ho], hz0 = sH(hS, 2)[ho];
+                const V4 hx0 = lds4(sH(hS, 0) + ho), hy0 = lds4(sH(hS, 1) + ho), hz0 = lds4(sH(hS, 2) + ho);
+                // rows j-2, j-1, j+1 of ez (hx) and ex (hz); z windows of ey (hx) and ex (hy)
+                const V4 ezm2 = lds4(ez + eo - 2 * BW), ezm1 = lds4(ez + eo - BW), ezp1 = lds4(ez + eo + BW);
+                const V4 exm2 = lds4(ex + eo - 2 * BW), exm1 = lds4(ex + eo - BW), exp1 = lds4(ex + eo + BW);
+                const ZW wy{lds4(ey + eo - col + colL), e2y, lds4(ey + eo - col + colR)};
+                const ZW wx{lds4(ex + eo - col + colL), e2x, lds4(ex + eo - col + colR)};
                 const bool iin = m > 1 && m < p.nx - 1;
-                const bool own = own_col && m >= x0 && m < x1;
+                const bool own = e_thread && m >= x0 && m < x1;
                 const int sxh = p.cpml ? slab(p.ha[0], m, p.nx, false) : -1;
-                const int nst = p.hh ? 2 : 1;
-                float vx = hx0, vy = hy0, vz = hz0;
-                const int e = eo;
-                if (jin_h && kin_h) {  // hx: ez along y, ey along z (plane m)
-                    const float ezm2 = ez[e - 2 * BW], ezm1 = ez[e - BW], ezp1 = ez[e + BW];
-                    const float eym2 = ey[e - 2], eym1 = ey[e - 1], eyp1 = ey[e + 1];
-                    const float n = curl4(e2z, ezm1, e2y, eym1);
-                    const float f = curl4(ezp1, ezm2, eyp1, eym2);
-                    const float d27 = fsub(fmul(27.0f, n), f);
-                    float py = 0.f, pz = 0.f;
-                    uint32_t qy = 0, qz = 0;
-                    if (syh >= 0) { qy = psi_index(p, 1, syh, m, j, k, p.ha[1].P); py = p.psi_h_in[3][qy]; }
-                    if (szh >= 0) { qz = psi_index(p, 2, szh, m, j, k, p.ha[2].P); pz = p.psi_h_in[4][qz]; }
-                    const float dy = syh >= 0 ? d4h(ezm2, ezm1, e2z, ezp1) : 0.f;
-                    const float dz = szh >= 0 ? d4h(eym2, eym1, e2y, eyp1) : 0.f;
-                    for (int st = 0; st < nst; st++) {
-                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                        const Axis *A = st ? p.hb : p.ha;
-                        vx = fsub(vx, fmul(clch, d27));
-                        if (syh >= 0) vx = fsub(vx, sterm(A[1], syh, py, dy, cl, p.ch));
-                        if (szh >= 0) vx = fadd(vx, sterm(A[2], szh, pz, dz, cl, p.ch));
+                constexpr bool hh = HH;
+                V4 vx = hx0, vy = hy0, vz = hz0;
+                if (!yz_h && sxh < 0) {
+                    // no CPML term at any cell of the group on this plane
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        {   // hx: ez along y, ey along z (plane m)
+                            const float n = curl4(e2z.v[c], ezm1.v[c], wy.at(c), wy.at(c - 1));
+                            const float f = curl4(ezp1.v[c], ezm2.v[c], wy.at(c + 1), wy.at(c - 2));
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vx.v[c], fmul(p.clch_a, d27));
+                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
+                            if (jin_h && ((kin_h >> c) & 1)) vx.v[c] = v;
+                        }
+                        {   // hy: ex along z (plane m), ez along x (queue)
+                            const float n = curl4(e2x.v[c], wx.at(c - 1), e2z.v[c], e1z.v[c]);
+                            const float f = curl4(wx.at(c + 1), wx.at(c - 2), e3z.v[c], e0z.v[c]);
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vy.v[c], fmul(p.clch_a, d27));
+                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
+                            if (iin && ((kin_h >> c) & 1)) vy.v[c] = v;
+                        }
+                        {   // hz: ey along x (queue), ex along y (plane m)
+                            const float n = curl4(e2y.v[c], e1y.v[c], e2x.v[c], exm1.v[c]);
+                            const float f = curl4(e3y.v[c], e0y.v[c], exp1.v[c], exm2.v[c]);
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vz.v[c], fmul(p.clch_a, d27));
+                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
+                            if (iin && jin_h) vz.v[c] = v;
+                        }
                     }
-                    if (own && syh >= 0) p.psi_h_out[3][qy] = py;
-                    if (own && szh >= 0) p.psi_h_out[4][qz] = pz;
-                }
-                if (iin && kin_h) {  // hy: ex along z (plane m), ez along x (queue)
-                    const float exm2 = ex[e - 2], exm1 = ex[e - 1], exp1 = ex[e + 1];
-                    const float n = curl4(e2x, exm1, e2z, e1z);
-                    const float f = curl4(exp1, exm2, e3z, e0z);
-                    const float d27 = fsub(fmul(27.0f, n), f);
-                    float px = 0.f, pz = 0.f;
-                    uint32_t qx = 0, qz = 0;
-                    if (sxh >= 0) { qx = psi_index(p, 0, sxh, m, j, k, p.ha[0].P); px = p.psi_h_in[0][qx]; }
-                    if (szh >= 0) { qz = psi_index(p, 2, szh, m, j, k, p.ha[2].P); pz = p.psi_h_in[5][qz]; }
-                    const float dx = sxh >= 0 ? d4h(e0z, e1z, e2z, e3z) : 0.f;
-                    const float dz = szh >= 0 ? d4h(exm2, exm1, e2x, exp1) : 0.f;
-                    for (int st = 0; st < nst; st++) {
-                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                        const Axis *A = st ? p.hb : p.ha;
-                        vy = fsub(vy, fmul(clch, d27));
-                        if (sxh >= 0) vy = fadd(vy, sterm(A[0], sxh, px, dx, cl, p.ch));
-                        if (szh >= 0) vy = fsub(vy, sterm(A[2], szh, pz, dz, cl, p.ch));
+                } else {
+                    // CPML path, in the operation order of the stage kernels.  Each
+                    // component's psi values of the 4 cells are loaded together
+                    // (one memory latency per component), then the cells update.
+                    int szh[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        szh[c] = p.cpml && ((k_in >> c) & 1) ? slab(p.ha[2], kg + c, p.nz, false) : -1;
+                    {   // hx: ez along y, ey along z; y term subtracted, z term added
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && jin_h && ((kin_h >> c) & 1);
+                            ps1[c] = up && syh >= 0 ? __ldg(p.psi_h_in[3] + psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)) : 0.f;
+                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[4] + psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)) : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && jin_h && ((kin_h >> c) & 1);
+                            if (!up) continue;
+                            const float n = curl4(e2z.v[c], ezm1.v[c], wy.at(c), wy.at(c - 1));
+                            const float f = curl4(ezp1.v[c], ezm2.v[c], wy.at(c + 1), wy.at(c - 2));
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            const float d1 = syh >= 0 ? d4h(ezm2.v[c], ezm1.v[c], e2z.v[c], ezp1.v[c]) : 0.f;
+                            const float d2 = szh[c] >= 0 ? d4h(wy.at(c - 2), wy.at(c - 1), wy.at(c), wy.at(c + 1)) : 0.f;
+                            float v = fsub(vx.v[c], fmul(p.clch_a, d27));
+                            if (syh >= 0) v = fsub(v, sterm(tab(p.ha[1]), syh, ps1[c], d1, p.cl_a, p.ch));
+                            if (szh[c] >= 0) v = fadd(v, sterm(tab(p.ha[2]), szh[c], ps2[c], d2, p.cl_a, p.ch));
+                            if (hh) {
+                                v = fsub(v, fmul(p.clch_b, d27));
+                                if (syh >= 0) v = fsub(v, sterm(tab(p.hb[1]), syh, ps1[c], d1, p.cl_b, p.ch));
+                                if (szh[c] >= 0) v = fadd(v, sterm(tab(p.hb[2]), szh[c], ps2[c], d2, p.cl_b, p.ch));
+                            }
+                            vx.v[c] = v;
+                            if (own && syh >= 0) p.psi_h_out[3][psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)] = ps1[c];
+                            if (own && szh[c] >= 0) p.psi_h_out[4][psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)] = ps2[c];
+                        }
                     }
-                    if (own && sxh >= 0) p.psi_h_out[0][qx] = px;
-                    if (own && szh >= 0) p.psi_h_out[5][qz] = pz;
-                }
-                if (iin && jin_h) {  // hz: ey along x (queue), ex along y (plane m)
-                    const float exm2 = ex[e - 2 * BW], exm1 = ex[e - BW], exp1 = ex[e + BW];
-                    const float n = curl4(e2y, e1y, e2x, exm1);
-                    const float f = curl4(e3y, e0y, exp1, exm2);
-                    const float d27 = fsub(fmul(27.0f, n), f);
-                    float px = 0.f, py = 0.f;
-                    uint32_t qx = 0, qy = 0;
-                    if (sxh >= 0) { qx = psi_index(p, 0, sxh, m, j, k, p.ha[0].P); px = p.psi_h_in[1][qx]; }
-                    if (syh >= 0) { qy = psi_index(p, 1, syh, m, j, k, p.ha[1].P); py = p.psi_h_in[2][qy]; }
-                    const float dx = sxh >= 0 ? d4h(e0y, e1y, e2y, e3y) : 0.f;
-                    const float dy = syh >= 0 ? d4h(exm2, exm1, e2x, exp1) : 0.f;
-                    for (int st = 0; st < nst; st++) {
-                        const float cl = st ? p.cl_b : p.cl_a, clch = st ? p.clch_b : p.clch_a;
-                        const Axis *A = st ? p.hb : p.ha;
-                        vz = fsub(vz, fmul(clch, d27));
-                        if (sxh >= 0) vz = fsub(vz, sterm(A[0], sxh, px, dx, cl, p.ch));
-                        if (syh >= 0) vz = fadd(vz, sterm(A[1], syh, py, dy, cl, p.ch));
+                    {   // hy: ex along z (plane m), ez along x (queue); x term added, z term subtracted
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && ((kin_h >> c) & 1);
+                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[0] + psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)) : 0.f;
+                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[5] + psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)) : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && ((kin_h >> c) & 1);
+                            if (!up) continue;
+                            const float n = curl4(e2x.v[c], wx.at(c - 1), e2z.v[c], e1z.v[c]);
+                            const float f = curl4(wx.at(c + 1), wx.at(c - 2), e3z.v[c], e0z.v[c]);
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            const float d1 = sxh >= 0 ? d4h(e0z.v[c], e1z.v[c], e2z.v[c], e3z.v[c]) : 0.f;
+                            const float d2 = szh[c] >= 0 ? d4h(wx.at(c - 2), wx.at(c - 1), wx.at(c), wx.at(c + 1)) : 0.f;
+                            float v = fsub(vy.v[c], fmul(p.clch_a, d27));
+                            if (sxh >= 0) v = fadd(v, sterm(tab(p.ha[0]), sxh, ps1[c], d1, p.cl_a, p.ch));
+                            if (szh[c] >= 0) v = fsub(v, sterm(tab(p.ha[2]), szh[c], ps2[c], d2, p.cl_a, p.ch));
+                            if (hh) {
+                                v = fsub(v, fmul(p.clch_b, d27));
+                                if (sxh >= 0) v = fadd(v, sterm(tab(p.hb[0]), sxh, ps1[c], d1, p.cl_b, p.ch));
+                                if (szh[c] >= 0) v = fsub(v, sterm(tab(p.hb[2]), szh[c], ps2[c], d2, p.cl_b, p.ch));
+                            }
+                            vy.v[c] = v;
+                            if (own && sxh >= 0) p.psi_h_out[0][psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)] = ps1[c];
+                            if (own && szh[c] >= 0) p.psi_h_out[5][psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)] = ps2[c];
+                        }
                     }
-                    if (own && sxh >= 0) p.psi_h_out[1][qx] = px;
-                    if (own && syh >= 0) p.psi_h_out[2][qy] = py;
+                    {   // hz: ey along x (queue), ex along y (plane m); x term subtracted, y term added
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && jin_h;
+                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[1] + psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)) : 0.f;
+                            ps2[c] = up && syh >= 0 ? __ldg(p.psi_h_in[2] + psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)) : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && jin_h;
+                            if (!up) continue;
+                            const float n = curl4(e2y.v[c], e1y.v[c], e2x.v[c], exm1.v[c]);
+                            const float f = curl4(e3y.v[c], e0y.v[c], exp1.v[c], exm2.v[c]);
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            const float d1 = sxh >= 0 ? d4h(e0y.v[c], e1y.v[c], e2y.v[c], e3y.v[c]) : 0.f;
+                            const float d2 = syh >= 0 ? d4h(exm2.v[c], exm1.v[c], e2x.v[c], exp1.v[c]) : 0.f;
+                            float v = fsub(vz.v[c], fmul(p.clch_a, d27));
+                            if (sxh >= 0) v = fsub(v, sterm(tab(p.ha[0]), sxh, ps1[c], d1, p.cl_a, p.ch));
+                            if (syh >= 0) v = fadd(v, sterm(tab(p.ha[1]), syh, ps2[c], d2, p.cl_a, p.ch));
+                            if (hh) {
+                                v = fsub(v, fmul(p.clch_b, d27));
+                                if (sxh >= 0) v = fsub(v, sterm(tab(p.hb[0]), sxh, ps1[c], d1, p.cl_b, p.ch));
+                                if (syh >= 0) v = fadd(v, sterm(tab(p.hb[1]), syh, ps2[c], d2, p.cl_b, p.ch));
+                            }
+                            vz.v[c] = v;
+                            if (own && sxh >= 0) p.psi_h_out[1][psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)] = ps1[c];
+                            if (own && syh >= 0) p.psi_h_out[2][psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)] = ps2[c];
+                        }
+                    }
                 }
                 const int nsl = (m - (x0 - 1)) % NHN;
-                sN(nsl, 0)[no] = vx;
-                sN(nsl, 1)[no] = vy;
-                sN(nsl, 2)[no] = vz;
+                sts4(sN(nsl, 0) + ho, vx);
+                sts4(sN(nsl, 1) + ho, vy);
+                sts4(sN(nsl, 2) + ho, vz);
                 hny = vy;
                 hnz = vz;
                 if (own) {
-                    const uint32_t g = (uint32_t)m * p.sx + (uint32_t)j * p.sy + k;
-                    p.out[3][g] = vx;
-                    p.out[4][g] = vy;
-                    p.out[5][g] = vz;
+                    const uint32_t rowo = (uint32_t)m * p.sx + (uint32_t)j * p.sy;
+                    stg4(p.out[3] + rowo, kg, p.nz, vx);
+                    stg4(p.out[4] + rowo, kg, p.nz, vy);
+                    stg4(p.out[5] + rowo, kg, p.nz, vz);
                 }
             }
 
-            // ---- E_new(i), i = p - 3, at tile columns ----
+            // ---- E_new(i), i = p - 3, at tile groups ----
             const int i = pl - 3;
-            if (q >= 6 && own_col && col_in) {
-                // H_new at planes i-1 .. i+2 of this column: n0 (i-1), n1 (i), n2 (i+1), new (i+2);
+            if (q >= 6 && e_thread && row_in && (k_in & 1)) {
+                // H_new at planes i-1 .. i+2 of this group: n0 (i-1), n1 (i), n2 (i+1), hn (i+2);
                 // H_new(i) neighbours from the ring (written two iterations ago)
                 const int nsl = (i - (x0 - 1)) % NHN;
                 const float *hx = sN(nsl, 0), *hy = sN(nsl, 1), *hz = sN(nsl, 2);
                 const int cS = cslot(q);
-                const int h = no;
-                float vx = e0x, vy = e0y, vz = e0z;  // input E of plane i
+                const V4 cvx = lds4(sC(cS, 0) + co), cvy = lds4(sC(cS, 1) + co), cvz = lds4(sC(cS, 2) + co);
+                // rows j-1, j+1, j+2 of hz (ex) and hx (ez); z windows of hy (ex) and hx (ey)
+                const V4 hzm1 = lds4(hz + ho - BW), hzp1 = lds4(hz + ho + BW), hzp2 = lds4(hz + ho + 2 * BW);
+                const V4 hxm1 = lds4(hx + ho - BW), hxp1 = lds4(hx + ho + BW), hxp2 = lds4(hx + ho + 2 * BW);
+                const ZW wy{lds4(hy + ho - 4), n1y, lds4(hy + ho + 4)};
+                const ZW wx{lds4(hx + ho - 4), lds4(hx + ho), lds4(hx + ho + 4)};
+                V4 vx = e0x, vy = e0y, vz = e0z;  // input E of plane i
                 const bool iin = i > 0 && i < p.nx - 2;
                 const int sxe = p.cpml ? slab(p.ea[0], i, p.nx, true) : -1;
-                if (jin_e && kin_e) {  // ex: hz along y, hy along z (plane i)
-                    const float hzm1 = hz[h - HNP], hzp1 = hz[h + HNP], hzp2 = hz[h + 2 * HNP];
-                    const float hym1 = hy[h - 1], hyp1 = hy[h + 1], hyp2 = hy[h + 2];
-                    const float n = curl4(hzp1, n1z, hyp1, n1y);
-                    const float f = curl4(hzp2, hzm1, hyp2, hym1);
-                    const float cv = sC(cS, 0)[co];
-                    vx = fadd(vx, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                    if (sye >= 0) {
-                        const uint32_t qi = psi_index(p, 1, sye, i, j, k, p.ea[1].P);
-                        float ps = p.psi_e[3][qi];
-                        vx = fadd(vx, sterm(p.ea[1], sye, ps, d4e(hzm1, n1z, hzp1, hzp2), p.dl, cv));
-                        p.psi_e[3][qi] = ps;
+                if (!yz_e && sxe < 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        {   // ex: hz along y, hy along z (plane i)
+                            const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
+                            const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
+                            const float v = fadd(vx.v[c], fmul(fmul(p.dl, cvx.v[c]), fsub(fmul(27.0f, n), f)));
+                            if (jin_e && ((kin_e >> c) & 1)) vx.v[c] = v;
+                        }
+                        {   // ey: hx along z (plane i), hz along x (queue)
+                            const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
+                            const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
+                            const float v = fadd(vy.v[c], fmul(fmul(p.dl, cvy.v[c]), fsub(fmul(27.0f, n), f)));
+                            if (iin && ((kin_e >> c) & 1)) vy.v[c] = v;
+                        }
+                        {   // ez: hy along x (queue), hx along y (plane i)
+                            const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
+                            const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
+                            const float v = fadd(vz.v[c], fmul(fmul(p.dl, cvz.v[c]), fsub(fmul(27.0f, n), f)));
+                            if (iin && jin_e) vz.v[c] = v;
+                        }
                     }
-                    if (sze >= 0) {
-                        const uint32_t qi = psi_index(p, 2, sze, i, j, k, p.ea[2].P);
-                        float ps = p.psi_e[4][qi];
-                        vx = fsub(vx, sterm(p.ea[2], sze, ps, d4e(hym1, n1y, hyp1, hyp2), p.dl, cv));
-                        p.psi_e[4][qi] = ps;
+                } else {
+                    // CPML path (E psi in place: only this thread touches these values)
+                    int sze[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        sze[c] = p.cpml && ((k_in >> c) & 1) ? slab(p.ea[2], kg + c, p.nz, true) : -1;
+                    {   // ex: hz along y, hy along z; y term added, z term subtracted
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && jin_e && ((kin_e >> c) & 1);
+                            ps1[c] = up && sye >= 0 ? p.psi_e[3][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] : 0.f;
+                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[4][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && jin_e && ((kin_e >> c) & 1);
+                            if (!up) continue;
+                            const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
+                            const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
+                            const float cv = cvx.v[c];
+                            float v = fadd(vx.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                            if (sye >= 0) {
+                                v = fadd(v, sterm(tab(p.ea[1]), sye, ps1[c], d4e(hzm1.v[c], n1z.v[c], hzp1.v[c], hzp2.v[c]), p.dl, cv));
+                                p.psi_e[3][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] = ps1[c];
+                            }
+                            if (sze[c] >= 0) {
+                                v = fsub(v, sterm(tab(p.ea[2]), sze[c], ps2[c], d4e(wy.at(c - 1), n1y.v[c], wy.at(c + 1), wy.at(c + 2)), p.dl, cv));
+                                p.psi_e[4][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] = ps2[c];
+                            }
+                            vx.v[c] = v;
+                        }
                     }
-                }
-                if (iin && kin_e) {  // ey: hx along z (plane i), hz along x (queue)
-                    const float hx0 = hx[h], hxm1 = hx[h - 1], hxp1 = hx[h + 1], hxp2 = hx[h + 2];
-                    const float n = curl4(hxp1, hx0, n2z, n1z);
-                    const float f = curl4(hxp2, hxm1, hnz, n0z);
-                    const float cv = sC(cS, 1)[co];
-                    vy = fadd(vy, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                    if (sxe >= 0) {
-                        const uint32_t qi = psi_index(p, 0, sxe, i, j, k, p.ea[0].P);
-                        float ps = p.psi_e[0][qi];
-                        vy = fsub(vy, sterm(p.ea[0], sxe, ps, d4e(n0z, n1z, n2z, hnz), p.dl, cv));
-                        p.psi_e[0][qi] = ps;
+                    {   // ey: hx along z (plane i), hz along x (queue); x term subtracted, z term added
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && ((kin_e >> c) & 1);
+                            ps1[c] = up && sxe >= 0 ? p.psi_e[0][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] : 0.f;
+                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[5][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && ((kin_e >> c) & 1);
+                            if (!up) continue;
+                            const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
+                            const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
+                            const float cv = cvy.v[c];
+                            float v = fadd(vy.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                            if (sxe >= 0) {
+                                v = fsub(v, sterm(tab(p.ea[0]), sxe, ps1[c], d4e(n0z.v[c], n1z.v[c], n2z.v[c], hnz.v[c]), p.dl, cv));
+                                p.psi_e[0][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] = ps1[c];
+                            }
+                            if (sze[c] >= 0) {
+                                v = fadd(v, sterm(tab(p.ea[2]), sze[c], ps2[c], d4e(wx.at(c - 1), wx.at(c), wx.at(c + 1), wx.at(c + 2)), p.dl, cv));
+                                p.psi_e[5][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] = ps2[c];
+                            }
+                            vy.v[c] = v;
+                        }
                     }
-                    if (sze >= 0) {
-                        const uint32_t qi = psi_index(p, 2, sze, i, j, k, p.ea[2].P);
-                        float ps = p.psi_e[5][qi];
-                        vy = fadd(vy, sterm(p.ea[2], sze, ps, d4e(hxm1, hx0, hxp1, hxp2), p.dl, cv));
-                        p.psi_e[5][qi] = ps;
-                    }
-                }
-                if (iin && jin_e) {  // ez: hy along x (queue), hx along y (plane i)
-                    const float hx0 = hx[h], hxm1 = hx[h - HNP], hxp1 = hx[h + HNP], hxp2 = hx[h + 2 * HNP];
-                    const float n = curl4(n2y, n1y, hxp1, hx0);
-                    const float f = curl4(hny, n0y, hxp2, hxm1);
-                    const float cv = sC(cS, 2)[co];
-                    vz = fadd(vz, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                    if (sxe >= 0) {
-                        const uint32_t qi = psi_index(p, 0, sxe, i, j, k, p.ea[0].P);
-                        float ps = p.psi_e[1][qi];
-                        vz = fadd(vz, sterm(p.ea[0], sxe, ps, d4e(n0y, n1y, n2y, hny), p.dl, cv));
-                        p.psi_e[1][qi] = ps;
-                    }
-                    if (sye >= 0) {
-                        const uint32_t qi = psi_index(p, 1, sye, i, j, k, p.ea[1].P);
-                        float ps = p.psi_e[2][qi];
-                        vz = fsub(vz, sterm(p.ea[1], sye, ps, d4e(hxm1, hx0, hxp1, hxp2), p.dl, cv));
-                        p.psi_e[2][qi] = ps;
+                    {   // ez: hy along x (queue), hx along y (plane i); x term added, y term subtracted
+                        float ps1[4], ps2[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && jin_e;
+                            ps1[c] = up && sxe >= 0 ? p.psi_e[1][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] : 0.f;
+                            ps2[c] = up && sye >= 0 ? p.psi_e[2][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const bool up = ((k_in >> c) & 1) && iin && jin_e;
+                            if (!up) continue;
+                            const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
+                            const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
+                            const float cv = cvz.v[c];
+                            float v = fadd(vz.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                            if (sxe >= 0) {
+                                v = fadd(v, sterm(tab(p.ea[0]), sxe, ps1[c], d4e(n0y.v[c], n1y.v[c], n2y.v[c], hny.v[c]), p.dl, cv));
+                                p.psi_e[1][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] = ps1[c];
+                            }
+                            if (sye >= 0) {
+                                v = fsub(v, sterm(tab(p.ea[1]), sye, ps2[c], d4e(hxm1.v[c], wx.at(c), hxp1.v[c], hxp2.v[c]), p.dl, cv));
+                                p.psi_e[2][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] = ps2[c];
+                            }
+                            vz.v[c] = v;
+                        }
                     }
                 }
                 for (int s = 0; s < nls; s++) {  // soft sources, list order
-                    if (s_ls_i[s] != i || s_ls_j[s] != j || (s_ls_kc[s] >> 2) != k) continue;
+                    const int sk = s_ls_kc[s] >> 2;
+                    if (s_ls_i[s] != i || s_ls_j[s] != j || sk < kg || sk >= kg + 4) continue;
                     const float v = p.src_amp[(int64_t)s_ls_s[s] * p.namp + p.t];
-                    const int comp = s_ls_kc[s] & 3;
-                    if (comp == 0) vx = fadd(vx, v);
-                    else if (comp == 1) vy = fadd(vy, v);
-                    else vz = fadd(vz, v);
+                    const int comp = s_ls_kc[s] & 3, c = sk - kg;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (u != c) continue;
+                        if (comp == 0) vx.v[u] = fadd(vx.v[u], v);
+                        else if (comp == 1) vy.v[u] = fadd(vy.v[u], v);
+                        else vz.v[u] = fadd(vz.v[u], v);
+                    }
                 }
-                const uint32_t g = (uint32_t)i * p.sx + (uint32_t)j * p.sy + k;
-                p.out[0][g] = vx;
-                p.out[1][g] = vy;
-                p.out[2][g] = vz;
+                const uint32_t rowo = (uint32_t)i * p.sx + (uint32_t)j * p.sy;
+                stg4(p.out[0] + rowo, kg, p.nz, vx);
+                stg4(p.out[1] + rowo, kg, p.nz, vy);
+                stg4(p.out[2] + rowo, kg, p.nz, vz);
             }
             // advance the queues
             e0x = e1x; e0y = e1y; e0z = e1z;
@@ -515,21 +766,35 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         if (aborted) {
             if (producer) {
                 atomicExch(p.status, FDTD_ERR_TIMEOUT);
-                // let the copies in flight (iterations q and q+1) land before the
-                // shared memory is released; each wait bounded
+                // let the copies in flight land before the shared memory is
+                // released (E and H of iterations q, q+1; CE of iteration q),
+                // each wait bounded
                 for (int q = q_abort; q < Q && q < q_abort + 2; q++) {
                     mbar_wait(&bars[eslot(q)], ephase(q), nullptr);
                     if (q >= 3) mbar_wait(&bars[NE + hslot(q)], hphase(q), nullptr);
-                    if (q >= 6) mbar_wait(&bars[NE + NH + cslot(q)], cphase(q), nullptr);
                 }
+                if (q_abort >= 6) mbar_wait(&bars[NE + NH + cslot(q_abort)], cphase(q_abort), nullptr);
             }
             break;
         }
         gE += (uint32_t)Q;
         gH += (uint32_t)(Q - 3);
         gC += (uint32_t)(Q - 6);
+        // every thread read s_item before this item's first barrier
+        if (tid == 0) s_item = atomicAdd(&p.queue[0], 1);
+        __syncthreads();
+        item = s_item;
     }
     if (aborted) __syncthreads();
+    if (tid == 0) {
+        // the last CTA to finish clears the queue for the next launch
+        __threadfence();
+        if (atomicAdd(&p.queue[1], 1) == (int)gridDim.x - 1) {
+            p.queue[0] = 0;
+            p.queue[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace sp
@@ -581,8 +846,8 @@ extern "C" {
 
 int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const fdtd_symp_state *s,
                                const fdtd_sources *src, int32_t x_chunk, int32_t cur, int32_t *status_dev,
-                               void *stream) {
-    if (!out || !s || !status_dev || (cur != 0 && cur != 1)) return FDTD_ERR_ARG;
+                               int32_t *queue_dev, void *stream) {
+    if (!out || !s || !status_dev || !queue_dev || (cur != 0 && cur != 1)) return FDTD_ERR_ARG;
     *out = nullptr;
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
@@ -608,6 +873,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
     p.x_chunk = (int32_t)std::min<int64_t>(x_chunk > 0 ? x_chunk : 128, g.nx);
     p.nxc = (int32_t)((g.nx + p.x_chunk - 1) / p.x_chunk);
     p.status = status_dev;
+    p.queue = queue_dev;
     for (int b = 0; b < 2; b++)
         for (int q = 0; q < 6; q++) {
             pl->f[b][q] = s->f[b][q];
@@ -643,9 +909,15 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
     if (st != FDTD_OK) { delete pl; return st; }
     int dev = 0, nsm = 0, occ = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_symp_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    int occ1 = 0;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void *)k_symp_pair<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void *)k_symp_pair<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)k_symp_pair, THREADS, SMEM);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)k_symp_pair<false>, THREADS, SMEM);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, (const void *)k_symp_pair<true>, THREADS, SMEM);
+    occ = std::min(occ, occ1);
     if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
     if (occ < 1) { delete pl; return FDTD_ERR_UNSUPPORTED; }
     const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
@@ -695,11 +967,15 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
                         : p.psi_h_in[2 * ax] && p.psi_h_in[2 * ax + 1] && p.psi_h_out[2 * ax] && p.psi_h_out[2 * ax + 1]))
                     return FDTD_ERR_ARG;
                 p.cpml = 1;
+                if (ax > 0) p.edge_first = 1;
             }
             dst[w][ax] = A;
         }
     }
-    k_symp_pair<<<pl->nblocks, THREADS, SMEM, as_stream(stream)>>>(pl->maps[in], p);
+    if (two_h)
+        k_symp_pair<true><<<pl->nblocks, THREADS, SMEM, as_stream(stream)>>>(pl->maps[in], p);
+    else
+        k_symp_pair<false><<<pl->nblocks, THREADS, SMEM, as_stream(stream)>>>(pl->maps[in], p);
     FDTD_TRY(check_launch());
     pl->cur = ob;
     return FDTD_OK;

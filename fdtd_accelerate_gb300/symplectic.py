@@ -266,12 +266,14 @@ class SymplecticSolver:
             st.ce[q] = self.ce[q].data_ptr()
         if not hasattr(self, "_status"):
             self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if not hasattr(self, "_queue"):
+            self._queue = torch.zeros(2, dtype=torch.int32, device=self.device)
         h = C.c_void_p()
         src = self._src.struct()
         with torch.cuda.device(self.device):
             N.call("fdtd_symp_pair_plan_create", C.byref(h), C.byref(grid_of(self._buf[0][0])), C.byref(st),
                    C.byref(src), int(self.x_chunk), int(self._cur), C.c_void_p(self._status.data_ptr()),
-                   stream_of(self._buf[0][0]))
+                   C.c_void_p(self._queue.data_ptr()), stream_of(self._buf[0][0]))
         self._pair, self._pair_src = h, self._src
         return h
 

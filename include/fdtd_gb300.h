@@ -290,10 +290,14 @@ typedef struct {
 typedef struct fdtd_symp_plan fdtd_symp_plan;
 
 /* x_chunk: x planes per work item (0: 128); cur: buffer holding the state;
- * the source positions are read on `stream` (the call waits for it once). */
+ * status_dev: device int32 set non-zero when a bounded wait expires;
+ * queue_dev: device int32[2], zero at plan creation, the work queue the
+ * CTAs draw items from (the kernel leaves it zero after each run; runs of
+ * plans sharing it must not overlap); the source positions are read on
+ * `stream` (the call waits for it once). */
 int fdtd_symp_pair_plan_create(fdtd_symp_plan **plan, const fdtd_grid *g, const fdtd_symp_state *st,
                                const fdtd_sources *src, int32_t x_chunk, int32_t cur,
-                               int32_t *status_dev, void *stream);
+                               int32_t *status_dev, int32_t *queue_dev, void *stream);
 /* One pass: the H stage cl_a (with two_h = 1, then the H stage cl_b), the E
  * stage dl, then the sources at amplitude index src_t, reading buffer cur and
  * writing the other.  Each stage's CPML tables come from its fdtd_cpml (the

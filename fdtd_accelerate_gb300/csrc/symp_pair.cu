@@ -419,10 +419,10 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         const bool yz_h = __any_sync(0xffffffffu, syh >= 0 || zh_any);
         const bool yz_e = __any_sync(0xffffffffu, sye >= 0 || ze_any);
 
-        // register queues of the group: input E of planes p-3 .. p-1 (ex, ey, ez),
-        // own H_new of planes p-4 .. p-2 (hy, hz)
-        V4 e0x{}, e0y{}, e0z{}, e1x{}, e1y{}, e1z{}, e2x{}, e2y{}, e2z{};
-        V4 n0y{}, n0z{}, n1y{}, n1z{}, n2y{}, n2z{};
+        // register queue of the group: input E of planes p-3 and p-2 (ex, ey,
+        // ez); planes p-1 and p are still in the E ring, and the group's own
+        // H_new of the planes around E_new(i) in the H_new ring
+        V4 e0x{}, e0y{}, e0z{}, e1x{}, e1y{}, e1z{};
         int q_abort = 0;
         for (int q = 0; q < Q; q++) {
             const int pl = x0 - 3 + q;
@@ -444,12 +444,26 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 if (q + 1 < Q && q + 1 >= 6) issue_c(q + 1);
             }
 
-            // input E of plane p at this group
-            V4 e3x{}, e3y{}, e3z{};
+            // input E of planes p-1 and p at this group
+            V4 e2x{}, e2y{}, e2z{}, e3x{}, e3y{}, e3z{};
             if (h_thread) {
                 e3x = lds4(sE(eS, 0) + eo);
                 e3y = lds4(sE(eS, 1) + eo);
                 e3z = lds4(sE(eS, 2) + eo);
+                if (q >= 1) {
+                    const int eSp = eslot(q - 1);
+                    e2x = lds4(sE(eSp, 0) + eo);
+                    e2y = lds4(sE(eSp, 1) + eo);
+                    e2z = lds4(sE(eSp, 2) + eo);
+                }
+            }
+            // own H_new (hy, hz) of plane p-4 for E_new(p-3): its ring slot
+            // takes H_new(p-1) below
+            V4 n0y{}, n0z{};
+            if (q >= 6 && e_thread) {
+                const int nsl0 = (pl - 4 - (x0 - 1)) % NHN;
+                n0y = lds4(sN(nsl0, 1) + ho);
+                n0z = lds4(sN(nsl0, 2) + ho);
             }
             // ---- H_new(m), m = p - 1, at this group ----
             const int m = pl - 1;
@@ -498,101 +512,121 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                         }
                     }
                 } else {
-                    // CPML path, in the operation order of the stage kernels.  Each
-                    // component's psi values of the 4 cells are loaded together
-                    // (one memory latency per component), then the cells update.
+                    // CPML path: per component the main term of the 4 cells, then
+                    // the CPML terms on the slab cells, stage by stage (the
+                    // operation order of the stage kernels).  psi offsets: the x
+                    // and y slabs hold the group's cells contiguously, the z slab
+                    // at the cells' slab indices.
+                    const uint32_t ux = jin_h ? kin_h : 0u, uy = iin ? kin_h : 0u, uz = iin && jin_h ? k_in : 0u;
+                    const uint32_t offx = sxh >= 0 ? ((uint32_t)sxh * p.ny + j) * p.nz + kg : 0u;
+                    const uint32_t offy = syh >= 0 ? ((uint32_t)m * (2u * p.ha[1].P) + syh) * p.nz + kg : 0u;
+                    const uint32_t offz = ((uint32_t)m * p.ny + j) * (2u * p.ha[2].P);
                     int szh[4];
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        szh[c] = p.cpml && ((k_in >> c) & 1) ? slab(p.ha[2], kg + c, p.nz, false) : -1;
+                    for (int c = 0; c < 4; c++) szh[c] = slab(p.ha[2], kg + c, p.nz, false);
                     {   // hx: ez along y, ey along z; y term subtracted, z term added
-                        float ps1[4], ps2[4];
+                        float ps1[4], ps2[4], d27[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && jin_h && ((kin_h >> c) & 1);
-                            ps1[c] = up && syh >= 0 ? __ldg(p.psi_h_in[3] + psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)) : 0.f;
-                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[4] + psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)) : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && jin_h && ((kin_h >> c) & 1);
-                            if (!up) continue;
+                            const bool up = (ux >> c) & 1;
+                            ps1[c] = up && syh >= 0 ? __ldg(p.psi_h_in[3] + offy + c) : 0.f;
+                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[4] + offz + szh[c]) : 0.f;
                             const float n = curl4(e2z.v[c], ezm1.v[c], wy.at(c), wy.at(c - 1));
                             const float f = curl4(ezp1.v[c], ezm2.v[c], wy.at(c + 1), wy.at(c - 2));
-                            const float d27 = fsub(fmul(27.0f, n), f);
-                            const float d1 = syh >= 0 ? d4h(ezm2.v[c], ezm1.v[c], e2z.v[c], ezp1.v[c]) : 0.f;
-                            const float d2 = szh[c] >= 0 ? d4h(wy.at(c - 2), wy.at(c - 1), wy.at(c), wy.at(c + 1)) : 0.f;
-                            float v = fsub(vx.v[c], fmul(p.clch_a, d27));
-                            if (syh >= 0) v = fsub(v, sterm(tab(p.ha[1]), syh, ps1[c], d1, p.cl_a, p.ch));
-                            if (szh[c] >= 0) v = fadd(v, sterm(tab(p.ha[2]), szh[c], ps2[c], d2, p.cl_a, p.ch));
-                            if (hh) {
-                                v = fsub(v, fmul(p.clch_b, d27));
-                                if (syh >= 0) v = fsub(v, sterm(tab(p.hb[1]), syh, ps1[c], d1, p.cl_b, p.ch));
-                                if (szh[c] >= 0) v = fadd(v, sterm(tab(p.hb[2]), szh[c], ps2[c], d2, p.cl_b, p.ch));
+                            d27[c] = fsub(fmul(27.0f, n), f);
+                        }
+#pragma unroll
+                        for (int st = 0; st < (HH ? 2 : 1); st++) {
+                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
+                            const Tab T1 = tab_h(p, st, 1), T2 = tab_h(p, st, 2);
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((ux >> c) & 1)) continue;
+                                float v = fsub(vx.v[c], fmul(clch, d27[c]));
+                                if (syh >= 0)
+                                    v = fsub(v, sterm(T1, syh, ps1[c], d4h(ezm2.v[c], ezm1.v[c], e2z.v[c], ezp1.v[c]), cl, p.ch));
+                                if (szh[c] >= 0)
+                                    v = fadd(v, sterm(T2, szh[c], ps2[c], d4h(wy.at(c - 2), wy.at(c - 1), wy.at(c), wy.at(c + 1)), cl, p.ch));
+                                vx.v[c] = v;
                             }
-                            vx.v[c] = v;
-                            if (own && syh >= 0) p.psi_h_out[3][psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)] = ps1[c];
-                            if (own && szh[c] >= 0) p.psi_h_out[4][psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)] = ps2[c];
+                        }
+                        if (own) {
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((ux >> c) & 1)) continue;
+                                if (syh >= 0) p.psi_h_out[3][offy + c] = ps1[c];
+                                if (szh[c] >= 0) p.psi_h_out[4][offz + szh[c]] = ps2[c];
+                            }
                         }
                     }
                     {   // hy: ex along z (plane m), ez along x (queue); x term added, z term subtracted
-                        float ps1[4], ps2[4];
+                        float ps1[4], ps2[4], d27[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && ((kin_h >> c) & 1);
-                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[0] + psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)) : 0.f;
-                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[5] + psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)) : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && ((kin_h >> c) & 1);
-                            if (!up) continue;
+                            const bool up = (uy >> c) & 1;
+                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[0] + offx + c) : 0.f;
+                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[5] + offz + szh[c]) : 0.f;
                             const float n = curl4(e2x.v[c], wx.at(c - 1), e2z.v[c], e1z.v[c]);
                             const float f = curl4(wx.at(c + 1), wx.at(c - 2), e3z.v[c], e0z.v[c]);
-                            const float d27 = fsub(fmul(27.0f, n), f);
-                            const float d1 = sxh >= 0 ? d4h(e0z.v[c], e1z.v[c], e2z.v[c], e3z.v[c]) : 0.f;
-                            const float d2 = szh[c] >= 0 ? d4h(wx.at(c - 2), wx.at(c - 1), wx.at(c), wx.at(c + 1)) : 0.f;
-                            float v = fsub(vy.v[c], fmul(p.clch_a, d27));
-                            if (sxh >= 0) v = fadd(v, sterm(tab(p.ha[0]), sxh, ps1[c], d1, p.cl_a, p.ch));
-                            if (szh[c] >= 0) v = fsub(v, sterm(tab(p.ha[2]), szh[c], ps2[c], d2, p.cl_a, p.ch));
-                            if (hh) {
-                                v = fsub(v, fmul(p.clch_b, d27));
-                                if (sxh >= 0) v = fadd(v, sterm(tab(p.hb[0]), sxh, ps1[c], d1, p.cl_b, p.ch));
-                                if (szh[c] >= 0) v = fsub(v, sterm(tab(p.hb[2]), szh[c], ps2[c], d2, p.cl_b, p.ch));
+                            d27[c] = fsub(fmul(27.0f, n), f);
+                        }
+#pragma unroll
+                        for (int st = 0; st < (HH ? 2 : 1); st++) {
+                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
+                            const Tab T0 = tab_h(p, st, 0), T2 = tab_h(p, st, 2);
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((uy >> c) & 1)) continue;
+                                float v = fsub(vy.v[c], fmul(clch, d27[c]));
+                                if (sxh >= 0)
+                                    v = fadd(v, sterm(T0, sxh, ps1[c], d4h(e0z.v[c], e1z.v[c], e2z.v[c], e3z.v[c]), cl, p.ch));
+                                if (szh[c] >= 0)
+                                    v = fsub(v, sterm(T2, szh[c], ps2[c], d4h(wx.at(c - 2), wx.at(c - 1), wx.at(c), wx.at(c + 1)), cl, p.ch));
+                                vy.v[c] = v;
                             }
-                            vy.v[c] = v;
-                            if (own && sxh >= 0) p.psi_h_out[0][psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)] = ps1[c];
-                            if (own && szh[c] >= 0) p.psi_h_out[5][psi_index(p, 2, szh[c], m, j, kg + c, p.ha[2].P)] = ps2[c];
+                        }
+                        if (own) {
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((uy >> c) & 1)) continue;
+                                if (sxh >= 0) p.psi_h_out[0][offx + c] = ps1[c];
+                                if (szh[c] >= 0) p.psi_h_out[5][offz + szh[c]] = ps2[c];
+                            }
                         }
                     }
                     {   // hz: ey along x (queue), ex along y (plane m); x term subtracted, y term added
-                        float ps1[4], ps2[4];
+                        float ps1[4], ps2[4], d27[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && jin_h;
-                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[1] + psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)) : 0.f;
-                            ps2[c] = up && syh >= 0 ? __ldg(p.psi_h_in[2] + psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)) : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && jin_h;
-                            if (!up) continue;
+                            const bool up = (uz >> c) & 1;
+                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[1] + offx + c) : 0.f;
+                            ps2[c] = up && syh >= 0 ? __ldg(p.psi_h_in[2] + offy + c) : 0.f;
                             const float n = curl4(e2y.v[c], e1y.v[c], e2x.v[c], exm1.v[c]);
                             const float f = curl4(e3y.v[c], e0y.v[c], exp1.v[c], exm2.v[c]);
-                            const float d27 = fsub(fmul(27.0f, n), f);
-                            const float d1 = sxh >= 0 ? d4h(e0y.v[c], e1y.v[c], e2y.v[c], e3y.v[c]) : 0.f;
-                            const float d2 = syh >= 0 ? d4h(exm2.v[c], exm1.v[c], e2x.v[c], exp1.v[c]) : 0.f;
-                            float v = fsub(vz.v[c], fmul(p.clch_a, d27));
-                            if (sxh >= 0) v = fsub(v, sterm(tab(p.ha[0]), sxh, ps1[c], d1, p.cl_a, p.ch));
-                            if (syh >= 0) v = fadd(v, sterm(tab(p.ha[1]), syh, ps2[c], d2, p.cl_a, p.ch));
-                            if (hh) {
-                                v = fsub(v, fmul(p.clch_b, d27));
-                                if (sxh >= 0) v = fsub(v, sterm(tab(p.hb[0]), sxh, ps1[c], d1, p.cl_b, p.ch));
-                                if (syh >= 0) v = fadd(v, sterm(tab(p.hb[1]), syh, ps2[c], d2, p.cl_b, p.ch));
+                            d27[c] = fsub(fmul(27.0f, n), f);
+                        }
+#pragma unroll
+                        for (int st = 0; st < (HH ? 2 : 1); st++) {
+                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
+                            const Tab T0 = tab_h(p, st, 0), T1 = tab_h(p, st, 1);
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((uz >> c) & 1)) continue;
+                                float v = fsub(vz.v[c], fmul(clch, d27[c]));
+                                if (sxh >= 0)
+                                    v = fsub(v, sterm(T0, sxh, ps1[c], d4h(e0y.v[c], e1y.v[c], e2y.v[c], e3y.v[c]), cl, p.ch));
+                                if (syh >= 0)
+                                    v = fadd(v, sterm(T1, syh, ps2[c], d4h(exm2.v[c], exm1.v[c], e2x.v[c], exp1.v[c]), cl, p.ch));
+                                vz.v[c] = v;
                             }
-                            vz.v[c] = v;
-                            if (own && sxh >= 0) p.psi_h_out[1][psi_index(p, 0, sxh, m, j, kg + c, p.ha[0].P)] = ps1[c];
-                            if (own && syh >= 0) p.psi_h_out[2][psi_index(p, 1, syh, m, j, kg + c, p.ha[1].P)] = ps2[c];
+                        }
+                        if (own) {
+#pragma unroll
+                            for (int c = 0; c < 4; c++) {
+                                if (!((uz >> c) & 1)) continue;
+                                if (sxh >= 0) p.psi_h_out[1][offx + c] = ps1[c];
+                                if (syh >= 0) p.psi_h_out[2][offy + c] = ps2[c];
+                            }
                         }
                     }
                 }
@@ -615,8 +649,10 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
             if (q >= 6 && e_thread && row_in && (k_in & 1)) {
                 // H_new at planes i-1 .. i+2 of this group: n0 (i-1), n1 (i), n2 (i+1), hn (i+2);
                 // H_new(i) neighbours from the ring (written two iterations ago)
-                const int nsl = (i - (x0 - 1)) % NHN;
+                const int nsl = (i - (x0 - 1)) % NHN, nsl2 = (i + 1 - (x0 - 1)) % NHN;
                 const float *hx = sN(nsl, 0), *hy = sN(nsl, 1), *hz = sN(nsl, 2);
+                const V4 n1y = lds4(hy + ho), n1z = lds4(hz + ho);                      // plane i
+                const V4 n2y = lds4(sN(nsl2, 1) + ho), n2z = lds4(sN(nsl2, 2) + ho);  // plane i+1
                 const int cS = cslot(q);
                 const V4 cvx = lds4(sC(cS, 0) + co), cvy = lds4(sC(cS, 1) + co), cvz = lds4(sC(cS, 2) + co);
                 // rows j-1, j+1, j+2 of hz (ex) and hx (ez); z windows of hy (ex) and hx (ey)
@@ -651,33 +687,36 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                     }
                 } else {
                     // CPML path (E psi in place: only this thread touches these values)
+                    const uint32_t ux = jin_e ? kin_e : 0u, uy = iin ? kin_e : 0u, uz = iin && jin_e ? k_in : 0u;
+                    const uint32_t offx = sxe >= 0 ? ((uint32_t)sxe * p.ny + j) * p.nz + kg : 0u;
+                    const uint32_t offy = sye >= 0 ? ((uint32_t)i * (2u * p.ea[1].P) + sye) * p.nz + kg : 0u;
+                    const uint32_t offz = ((uint32_t)i * p.ny + j) * (2u * p.ea[2].P);
                     int sze[4];
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        sze[c] = p.cpml && ((k_in >> c) & 1) ? slab(p.ea[2], kg + c, p.nz, true) : -1;
+                    for (int c = 0; c < 4; c++) sze[c] = slab(p.ea[2], kg + c, p.nz, true);
+                    const Tab T0 = tab(p.ea[0]), T1 = tab(p.ea[1]), T2 = tab(p.ea[2]);
                     {   // ex: hz along y, hy along z; y term added, z term subtracted
                         float ps1[4], ps2[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && jin_e && ((kin_e >> c) & 1);
-                            ps1[c] = up && sye >= 0 ? p.psi_e[3][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] : 0.f;
-                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[4][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] : 0.f;
+                            const bool up = (ux >> c) & 1;
+                            ps1[c] = up && sye >= 0 ? p.psi_e[3][offy + c] : 0.f;
+                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[4][offz + sze[c]] : 0.f;
                         }
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && jin_e && ((kin_e >> c) & 1);
-                            if (!up) continue;
+                            if (!((ux >> c) & 1)) continue;
                             const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
                             const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
                             const float cv = cvx.v[c];
                             float v = fadd(vx.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
                             if (sye >= 0) {
-                                v = fadd(v, sterm(tab(p.ea[1]), sye, ps1[c], d4e(hzm1.v[c], n1z.v[c], hzp1.v[c], hzp2.v[c]), p.dl, cv));
-                                p.psi_e[3][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] = ps1[c];
+                                v = fadd(v, sterm(T1, sye, ps1[c], d4e(hzm1.v[c], n1z.v[c], hzp1.v[c], hzp2.v[c]), p.dl, cv));
+                                p.psi_e[3][offy + c] = ps1[c];
                             }
                             if (sze[c] >= 0) {
-                                v = fsub(v, sterm(tab(p.ea[2]), sze[c], ps2[c], d4e(wy.at(c - 1), n1y.v[c], wy.at(c + 1), wy.at(c + 2)), p.dl, cv));
-                                p.psi_e[4][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] = ps2[c];
+                                v = fsub(v, sterm(T2, sze[c], ps2[c], d4e(wy.at(c - 1), n1y.v[c], wy.at(c + 1), wy.at(c + 2)), p.dl, cv));
+                                p.psi_e[4][offz + sze[c]] = ps2[c];
                             }
                             vx.v[c] = v;
                         }
@@ -686,25 +725,24 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                         float ps1[4], ps2[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && ((kin_e >> c) & 1);
-                            ps1[c] = up && sxe >= 0 ? p.psi_e[0][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] : 0.f;
-                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[5][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] : 0.f;
+                            const bool up = (uy >> c) & 1;
+                            ps1[c] = up && sxe >= 0 ? p.psi_e[0][offx + c] : 0.f;
+                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[5][offz + sze[c]] : 0.f;
                         }
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && ((kin_e >> c) & 1);
-                            if (!up) continue;
+                            if (!((uy >> c) & 1)) continue;
                             const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
                             const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
                             const float cv = cvy.v[c];
                             float v = fadd(vy.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
                             if (sxe >= 0) {
-                                v = fsub(v, sterm(tab(p.ea[0]), sxe, ps1[c], d4e(n0z.v[c], n1z.v[c], n2z.v[c], hnz.v[c]), p.dl, cv));
-                                p.psi_e[0][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] = ps1[c];
+                                v = fsub(v, sterm(T0, sxe, ps1[c], d4e(n0z.v[c], n1z.v[c], n2z.v[c], hnz.v[c]), p.dl, cv));
+                                p.psi_e[0][offx + c] = ps1[c];
                             }
                             if (sze[c] >= 0) {
-                                v = fadd(v, sterm(tab(p.ea[2]), sze[c], ps2[c], d4e(wx.at(c - 1), wx.at(c), wx.at(c + 1), wx.at(c + 2)), p.dl, cv));
-                                p.psi_e[5][psi_index(p, 2, sze[c], i, j, kg + c, p.ea[2].P)] = ps2[c];
+                                v = fadd(v, sterm(T2, sze[c], ps2[c], d4e(wx.at(c - 1), wx.at(c), wx.at(c + 1), wx.at(c + 2)), p.dl, cv));
+                                p.psi_e[5][offz + sze[c]] = ps2[c];
                             }
                             vy.v[c] = v;
                         }
@@ -713,25 +751,24 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                         float ps1[4], ps2[4];
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && jin_e;
-                            ps1[c] = up && sxe >= 0 ? p.psi_e[1][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] : 0.f;
-                            ps2[c] = up && sye >= 0 ? p.psi_e[2][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] : 0.f;
+                            const bool up = (uz >> c) & 1;
+                            ps1[c] = up && sxe >= 0 ? p.psi_e[1][offx + c] : 0.f;
+                            ps2[c] = up && sye >= 0 ? p.psi_e[2][offy + c] : 0.f;
                         }
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const bool up = ((k_in >> c) & 1) && iin && jin_e;
-                            if (!up) continue;
+                            if (!((uz >> c) & 1)) continue;
                             const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
                             const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
                             const float cv = cvz.v[c];
                             float v = fadd(vz.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
                             if (sxe >= 0) {
-                                v = fadd(v, sterm(tab(p.ea[0]), sxe, ps1[c], d4e(n0y.v[c], n1y.v[c], n2y.v[c], hny.v[c]), p.dl, cv));
-                                p.psi_e[1][psi_index(p, 0, sxe, i, j, kg + c, p.ea[0].P)] = ps1[c];
+                                v = fadd(v, sterm(T0, sxe, ps1[c], d4e(n0y.v[c], n1y.v[c], n2y.v[c], hny.v[c]), p.dl, cv));
+                                p.psi_e[1][offx + c] = ps1[c];
                             }
                             if (sye >= 0) {
-                                v = fsub(v, sterm(tab(p.ea[1]), sye, ps2[c], d4e(hxm1.v[c], wx.at(c), hxp1.v[c], hxp2.v[c]), p.dl, cv));
-                                p.psi_e[2][psi_index(p, 1, sye, i, j, kg + c, p.ea[1].P)] = ps2[c];
+                                v = fsub(v, sterm(T1, sye, ps2[c], d4e(hxm1.v[c], wx.at(c), hxp1.v[c], hxp2.v[c]), p.dl, cv));
+                                p.psi_e[2][offy + c] = ps2[c];
                             }
                             vz.v[c] = v;
                         }
@@ -755,13 +792,9 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 stg4(p.out[1] + rowo, kg, p.nz, vy);
                 stg4(p.out[2] + rowo, kg, p.nz, vz);
             }
-            // advance the queues
+            // advance the queue
             e0x = e1x; e0y = e1y; e0z = e1z;
             e1x = e2x; e1y = e2y; e1z = e2z;
-            e2x = e3x; e2y = e3y; e2z = e3z;
-            n0y = n1y; n0z = n1z;
-            n1y = n2y; n1z = n2z;
-            n2y = hny; n2z = hnz;
         }
         if (aborted) {
             if (producer) {

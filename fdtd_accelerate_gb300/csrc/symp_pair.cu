@@ -9,36 +9,37 @@
 //   fdtd_symplectic_stage_f32(E, dl), sources,
 // with the same round-to-nearest operations, so the result is bit-identical.
 //
-// Design (2.5-D blocking, 4 z cells per thread)
-//  * Ping-pong state: the pass reads buffer `cur` (E, H) and writes `1-cur`;
-//    the H psi slabs ping-pong too (halo H cells are recomputed from the
-//    input psi), the E psi slabs are updated in place (only their owner
-//    touches them).
-//  * A CTA owns TZ = 32 (z) x TY = 16 (y) cells for a chunk of x planes and
-//    marches along x.  E_new(i) needs H_new on planes i-1 .. i+2 and on the
-//    rows/columns -1 .. +2 around the tile, so H_new is computed on the rows
-//    j0-1 .. j0+TY+1 and the columns k0-4 .. k0+TZ+3, in groups of 4 z cells:
-//    one thread per group, the 128 tile groups first (those threads also
-//    compute E_new of their group), then the 62 halo groups.  Every group is
-//    16-byte aligned, so its z window (the group and the neighbouring
-//    groups) is three 16-byte shared loads.
-//  * Each thread keeps the x neighbours it needs in registers: the input E of
-//    planes m-3 .. m-1 for H_new(m-1), and its own H_new (hy, hz) of planes
-//    i-1 .. i+1 for E_new(i).  Shared memory holds one plane with its y/z
-//    halo: input E boxes (4-slot ring) and H boxes (3-slot ring), both issued
-//    two planes ahead, CE boxes (2-slot ring, one plane ahead) and H_new
-//    (3-slot ring).  About 108 KB, two CTAs per SM.
+// Design: the pair kernel on the grid's inside, edge kernels on a thin shell
+//  * Ping-pong state: a pass reads buffer `cur` (E, H) and writes `1-cur`;
+//    the H psi slabs ping-pong too, the E psi slabs are updated in place
+//    (only their owner touches them).
+//  * Split: the pair kernel owns rows [j_lo, j_hi) and columns [k_lo, k_hi),
+//    every x plane, with j_lo = P+2 and j_hi = ny-P-2 (and the same along z,
+//    k_lo rounded up to 4): E_new there needs H_new of rows j_lo-1 .. j_hi+1,
+//    where no y or z CPML node lies.  So the pair kernel carries the x-slab
+//    terms only.  The rest of the grid (the y and z slabs plus two cells) is
+//    the edge shell, advanced by one-thread-per-cell kernels (k_edge_*), out
+//    of place, after the pair kernel has written the inside H_new.
+//  * Pair kernel, 2.5-D blocking: a CTA owns TZ = 32 (z) x TY = 16 (y) cells
+//    for a chunk of x planes and marches along x.  E_new(i) needs H_new on
+//    planes i-1 .. i+2 and on the rows/columns -1 .. +2 around the tile, so
+//    H_new is computed on the rows j0-1 .. j0+TY+1 and the columns
+//    k0-4 .. k0+TZ+3, in groups of 4 z cells: one thread per group, the 128
+//    tile groups first (those threads also compute E_new of their group),
+//    then the 62 halo groups.  Every group is 16-byte aligned, so its z window
+//    (the group and the neighbouring groups) is three 16-byte shared loads.
+//    z tiles keep TZ-column boundaries (128-byte rows); cells outside the
+//    kernel's columns are computed but not written.
+//  * Registers hold the input E of planes p-3 and p-2 of the group; shared
+//    memory holds one plane with its y/z halo: input E boxes (4-slot ring)
+//    and H boxes (3-slot ring), both issued two planes ahead, CE boxes (2-slot
+//    ring, one plane ahead) and H_new (3-slot ring).  About 108 KB, two CTAs
+//    per SM.
 //  * Iteration q: input plane p arrives; every thread computes H_new(p-1) for
 //    its group; tile threads then compute E_new(p-3).  One CTA barrier per
 //    iteration: H_new(p-1) is read by neighbours two iterations later.
-//  * Warps whose groups lie in no CPML slab on a plane outside the x slabs
-//    take a path without psi code; the others run the CPML terms cell by
-//    cell in the operation order of the stage kernels, each component's psi
-//    values of the 4 cells loaded together.
 //  * CTAs draw work items from a device queue (two ints the caller provides,
-//    cleared by the last CTA of each launch).  With y or z slabs the edge
-//    tiles, which carry them, are handed out first, so a launch ends on
-//    interior tiles.
+//    cleared by the last CTA of each launch).
 //  * Lane 31 of the last warp is the producer: it waits on the mbarriers and
 //    issues the copies.  Every wait is bounded (1 s); on expiry the CTA
 //    records FDTD_ERR_TIMEOUT, drains its copies and stops.
@@ -100,7 +101,14 @@ struct Params {
     float clch_a, clch_b;     // cl * ch as one single-precision product
     int32_t hh;               // 1: two H stages (a then b) before the E stage
     int32_t cpml;             // any slab
-    int32_t edge_first;       // y or z slabs: edge tiles first in the work order
+    // this kernel's region: rows [j_lo, j_hi), columns [k_lo, k_hi) (k_lo a
+    // multiple of 4), every x plane, tiled from (j_lo, k_lo) into nty_in x
+    // ntz_in tiles; its H regions hold no y or z CPML node.  The rest of the
+    // grid is the edge shell of the edge kernels.
+    int32_t j_lo, j_hi, k_lo, k_hi, nty_in, ntz_in;
+    int32_t kt0;              // first z tile origin (k_lo rounded down to TZ)
+    const float *in[6];       // ex, ey, ez, hx, hy, hz of the input buffer (edge kernels)
+    const float *ce[3];
     int32_t nsrc;
     const int32_t *src_ijk, *src_comp;
     const float *src_amp;
@@ -216,51 +224,24 @@ struct ZW {
     }
 };
 
-// global store of a group's 4 values (cells k .. k+3 of a row); cells at
-// z >= nz are not stored
-__device__ __forceinline__ void stg4(float *row, int k, int nz, const V4 &a) {
-    if (k + 3 < nz) {
+// global store of a group's 4 values (cells k .. k+3 of a row): the cells
+// whose bit is set in mask (all four: one 16-byte store)
+__device__ __forceinline__ void stg4(float *row, int k, uint32_t mask, const V4 &a) {
+    if (mask == 0xFu) {
         *reinterpret_cast<float4 *>(row + k) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
     } else {
 #pragma unroll
         for (int c = 0; c < 4; c++)
-            if (k + c < nz) row[k + c] = a.v[c];
+            if ((mask >> c) & 1) row[k + c] = a.v[c];
     }
 }
 
-// Work item u -> tile (tzi, tyi) and x chunk xci.  The y/z edge tiles (first
-// or last tile row or column) of every x chunk come first, then the interior
-// tiles; inside each part the z tile runs fastest, then the y tile, then the
-// x chunk.
+// Work item u -> tile (tzi, tyi) and x chunk xci over the kernel's tiles:
+// z tile fastest, then y tile, then x chunk.
 __device__ __forceinline__ void item_tile(const Params &p, int u, int &tzi, int &tyi, int &xci) {
-    const int nz = p.ntz, ny = p.nty;
-    const int ni = (nz > 2 && ny > 2) ? (nz - 2) * (ny - 2) : 0;  // interior tiles per chunk
-    const int ne = nz * ny - ni;                                   // edge tiles per chunk
-    if (!p.edge_first) {  // z tile fastest, then y tile, then x chunk
-        tzi = u % nz;
-        tyi = (u / nz) % ny;
-        xci = u / (nz * ny);
-        return;
-    }
-    if (u < ne * p.nxc) {
-        xci = u / ne;
-        const int e = u - xci * ne;
-        if (e < 2 * nz || ni == 0) {  // the first and last tile rows (all tiles when ni == 0)
-            const int r = ni == 0 ? e / nz : (e < nz ? 0 : ny - 1);
-            tyi = r;
-            tzi = ni == 0 ? e - r * nz : (e < nz ? e : e - nz);
-        } else {                      // the first and last tile of each inner row
-            const int f = e - 2 * nz;
-            tyi = 1 + (f >> 1);
-            tzi = (f & 1) ? nz - 1 : 0;
-        }
-    } else {
-        const int v = u - ne * p.nxc;
-        xci = v / ni;
-        const int r = v - xci * ni;
-        tyi = 1 + r / (nz - 2);
-        tzi = 1 + r % (nz - 2);
-    }
+    tzi = u % p.ntz_in;
+    tyi = (u / p.ntz_in) % p.nty_in;
+    xci = u / (p.ntz_in * p.nty_in);
 }
 
 // HH: two H stages before the E stage (the pass that merges the closing H
@@ -319,16 +300,15 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
 
     uint32_t gE = 0, gH = 0, gC = 0;  // ring uses before the current item
     bool aborted = false;
-    const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
-    // items from the work queue (item_tile gives the order: the y/z edge tiles,
-    // which carry the y and z CPML slabs, first): CTAs that drew cheaper tiles
-    // take more of them, and the last items of a launch are interior tiles
+    const int64_t nitems = (int64_t)p.ntz_in * p.nty_in * p.nxc;
+    // items from the work queue: CTAs that drew cheaper items (no x slab
+    // plane, no source) take more of them
     if (tid == 0) s_item = atomicAdd(&p.queue[0], 1);
     __syncthreads();
     for (int64_t item = s_item; item < nitems && !aborted;) {
         int tzi, tyi, xci;
         item_tile(p, (int)item, tzi, tyi, xci);
-        const int k0 = tzi * TZ, j0 = tyi * TY, x0 = xci * p.x_chunk;
+        const int k0 = p.kt0 + tzi * TZ, j0 = p.j_lo + tyi * TY, x0 = xci * p.x_chunk;
         const int x1 = min(x0 + p.x_chunk, p.nx);
         // iteration q: input plane p = x0 - 3 + q arrives; H_new(p-1) for
         // q >= 3, E_new(p-3) for q >= 6
@@ -367,7 +347,8 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
             if (p.t >= 0 && p.t < p.namp)
                 for (int s = 0; s < p.nsrc; s++) {
                     const int si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
-                    if (si >= x0 && si < x1 && sj >= j0 && sj < j0 + TY && sk >= k0 && sk < k0 + TZ) {
+                    if (si >= x0 && si < x1 && sj >= j0 && sj < min(j0 + TY, p.j_hi) && sk >= max(k0, p.k_lo) &&
+                        sk < min(k0 + TZ, p.k_hi)) {
                         if (n < MAX_SRC) {
                             s_ls_i[n] = si;
                             s_ls_j[n] = sj;
@@ -391,33 +372,19 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
         const int nls = s_nls;
         const int j = j0 - 1 + hr, kg = k0 - 4 + col;   // row and first z cell of the group
         const bool row_in = h_thread && j >= 0 && j < p.ny;
+        const bool own_row = e_thread && row_in && j < p.j_hi;  // rows this kernel writes
         const bool jin_h = j > 1 && j < p.ny - 1, jin_e = j > 0 && j < p.ny - 2;
-        // per-cell z masks of the group (bit c: cell kg+c)
-        uint32_t kin_h = 0, kin_e = 0, k_in = 0;
+        // per-cell z masks of the group (bit c: cell kg+c); kown: cells this kernel writes
+        const int kmax = min(p.nz, p.k_hi);
+        uint32_t kin_h = 0, kin_e = 0, k_in = 0, kown = 0;
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             const int k = kg + c;
             kin_h |= (uint32_t)(k > 1 && k < p.nz - 1) << c;
             kin_e |= (uint32_t)(k > 0 && k < p.nz - 2) << c;
             k_in |= (uint32_t)(k >= 0 && k < p.nz) << c;
+            kown |= (uint32_t)(own_row && k >= p.k_lo && k < kmax) << c;
         }
-        // CPML: y slab of the row (H and E nodes); any z-slab cell in the group
-        int syh = -1, sye = -1;
-        bool zh_any = false, ze_any = false;
-        if (p.cpml && row_in) {
-            syh = slab(p.ha[1], j, p.ny, false);
-            sye = slab(p.ea[1], j, p.ny, true);
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                zh_any |= slab(p.ha[2], kg + c, p.nz, false) >= 0;
-                ze_any |= slab(p.ea[2], kg + c, p.nz, true) >= 0;
-            }
-        }
-        // the path choice is made per warp: a warp with any slab cell runs the
-        // CPML path for all its lanes (it handles plain cells as well), so it
-        // never runs both paths one after the other
-        const bool yz_h = __any_sync(0xffffffffu, syh >= 0 || zh_any);
-        const bool yz_e = __any_sync(0xffffffffu, sye >= 0 || ze_any);
 
         // register queue of the group: input E of planes p-3 and p-2 (ex, ey,
         // ez); planes p-1 and p are still in the E ring, and the group's own
@@ -466,24 +433,34 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 n0z = lds4(sN(nsl0, 2) + ho);
             }
             // ---- H_new(m), m = p - 1, at this group ----
+            // The kernel's tiles meet no y or z slab; on an x-slab plane hy and
+            // hz take their x term after the main term (the operation order of
+            // the stage kernels), stage by stage.
             const int m = pl - 1;
             V4 hny{}, hnz{};
             if (q >= 3 && row_in && m >= 0 && m < p.nx) {
                 const int eSm = eslot(q - 1), hS = hslot(q);
                 const float *ex = sE(eSm, 0), *ey = sE(eSm, 1), *ez = sE(eSm, 2);
-                const V4 hx0 = lds4(sH(hS, 0) + ho), hy0 = lds4(sH(hS, 1) + ho), hz0 = lds4(sH(hS, 2) + ho);
+                V4 vx = lds4(sH(hS, 0) + ho), vy = lds4(sH(hS, 1) + ho), vz = lds4(sH(hS, 2) + ho);
                 // rows j-2, j-1, j+1 of ez (hx) and ex (hz); z windows of ey (hx) and ex (hy)
                 const V4 ezm2 = lds4(ez + eo - 2 * BW), ezm1 = lds4(ez + eo - BW), ezp1 = lds4(ez + eo + BW);
                 const V4 exm2 = lds4(ex + eo - 2 * BW), exm1 = lds4(ex + eo - BW), exp1 = lds4(ex + eo + BW);
                 const ZW wy{lds4(ey + eo - col + colL), e2y, lds4(ey + eo - col + colR)};
                 const ZW wx{lds4(ex + eo - col + colL), e2x, lds4(ex + eo - col + colR)};
                 const bool iin = m > 1 && m < p.nx - 1;
-                const bool own = e_thread && m >= x0 && m < x1;
-                const int sxh = p.cpml ? slab(p.ha[0], m, p.nx, false) : -1;
-                constexpr bool hh = HH;
-                V4 vx = hx0, vy = hy0, vz = hz0;
-                if (!yz_h && sxh < 0) {
-                    // no CPML term at any cell of the group on this plane
+                const bool own = own_row && m >= x0 && m < x1;
+                const int sxh = p.cpml ? slab(p.ha[0], m, p.nx, false) : -1;  // uniform over the CTA
+                const uint32_t ux = jin_h ? kin_h : 0u, uy = iin ? kin_h : 0u, uz = iin && jin_h ? k_in : 0u;
+                const uint32_t offx = sxh >= 0 ? ((uint32_t)sxh * p.ny + j) * p.nz + kg : 0u;
+                float py[4], pz[4];  // x psi of hy and hz (x-slab planes)
+                if (sxh >= 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        py[c] = (uy >> c) & 1 ? __ldg(p.psi_h_in[0] + offx + c) : 0.f;
+                        pz[c] = (uz >> c) & 1 ? __ldg(p.psi_h_in[1] + offx + c) : 0.f;
+                    }
+                }
+                if (sxh < 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
                         {   // hx: ez along y, ey along z (plane m)
@@ -491,143 +468,78 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                             const float f = curl4(ezp1.v[c], ezm2.v[c], wy.at(c + 1), wy.at(c - 2));
                             const float d27 = fsub(fmul(27.0f, n), f);
                             float v = fsub(vx.v[c], fmul(p.clch_a, d27));
-                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
-                            if (jin_h && ((kin_h >> c) & 1)) vx.v[c] = v;
+                            if (HH) v = fsub(v, fmul(p.clch_b, d27));
+                            if ((ux >> c) & 1) vx.v[c] = v;
                         }
-                        {   // hy: ex along z (plane m), ez along x (queue)
+                        {   // hy: ex along z (plane m), ez along x (queue); x term added
                             const float n = curl4(e2x.v[c], wx.at(c - 1), e2z.v[c], e1z.v[c]);
                             const float f = curl4(wx.at(c + 1), wx.at(c - 2), e3z.v[c], e0z.v[c]);
                             const float d27 = fsub(fmul(27.0f, n), f);
                             float v = fsub(vy.v[c], fmul(p.clch_a, d27));
-                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
-                            if (iin && ((kin_h >> c) & 1)) vy.v[c] = v;
+                            if (HH) v = fsub(v, fmul(p.clch_b, d27));
+                            if ((uy >> c) & 1) vy.v[c] = v;
                         }
-                        {   // hz: ey along x (queue), ex along y (plane m)
+                        {   // hz: ey along x (queue), ex along y (plane m); x term subtracted
                             const float n = curl4(e2y.v[c], e1y.v[c], e2x.v[c], exm1.v[c]);
                             const float f = curl4(e3y.v[c], e0y.v[c], exp1.v[c], exm2.v[c]);
                             const float d27 = fsub(fmul(27.0f, n), f);
                             float v = fsub(vz.v[c], fmul(p.clch_a, d27));
-                            if (hh) v = fsub(v, fmul(p.clch_b, d27));
-                            if (iin && jin_h) vz.v[c] = v;
+                            if (HH) v = fsub(v, fmul(p.clch_b, d27));
+                            if ((uz >> c) & 1) vz.v[c] = v;
                         }
                     }
                 } else {
-                    // CPML path: per component the main term of the 4 cells, then
-                    // the CPML terms on the slab cells, stage by stage (the
-                    // operation order of the stage kernels).  psi offsets: the x
-                    // and y slabs hold the group's cells contiguously, the z slab
-                    // at the cells' slab indices.
-                    const uint32_t ux = jin_h ? kin_h : 0u, uy = iin ? kin_h : 0u, uz = iin && jin_h ? k_in : 0u;
-                    const uint32_t offx = sxh >= 0 ? ((uint32_t)sxh * p.ny + j) * p.nz + kg : 0u;
-                    const uint32_t offy = syh >= 0 ? ((uint32_t)m * (2u * p.ha[1].P) + syh) * p.nz + kg : 0u;
-                    const uint32_t offz = ((uint32_t)m * p.ny + j) * (2u * p.ha[2].P);
-                    int szh[4];
 #pragma unroll
-                    for (int c = 0; c < 4; c++) szh[c] = slab(p.ha[2], kg + c, p.nz, false);
-                    {   // hx: ez along y, ey along z; y term subtracted, z term added
-                        float ps1[4], ps2[4], d27[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (ux >> c) & 1;
-                            ps1[c] = up && syh >= 0 ? __ldg(p.psi_h_in[3] + offy + c) : 0.f;
-                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[4] + offz + szh[c]) : 0.f;
+                    for (int c = 0; c < 4; c++) {
+                        {   // hx: ez along y, ey along z (plane m)
                             const float n = curl4(e2z.v[c], ezm1.v[c], wy.at(c), wy.at(c - 1));
                             const float f = curl4(ezp1.v[c], ezm2.v[c], wy.at(c + 1), wy.at(c - 2));
-                            d27[c] = fsub(fmul(27.0f, n), f);
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vx.v[c], fmul(p.clch_a, d27));
+                            if (HH) v = fsub(v, fmul(p.clch_b, d27));
+                            if ((ux >> c) & 1) vx.v[c] = v;
                         }
-#pragma unroll
-                        for (int st = 0; st < (HH ? 2 : 1); st++) {
-                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
-                            const Tab T1 = tab_h(p, st, 1), T2 = tab_h(p, st, 2);
-#pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((ux >> c) & 1)) continue;
-                                float v = fsub(vx.v[c], fmul(clch, d27[c]));
-                                if (syh >= 0)
-                                    v = fsub(v, sterm(T1, syh, ps1[c], d4h(ezm2.v[c], ezm1.v[c], e2z.v[c], ezp1.v[c]), cl, p.ch));
-                                if (szh[c] >= 0)
-                                    v = fadd(v, sterm(T2, szh[c], ps2[c], d4h(wy.at(c - 2), wy.at(c - 1), wy.at(c), wy.at(c + 1)), cl, p.ch));
-                                vx.v[c] = v;
-                            }
-                        }
-                        if (own) {
-#pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((ux >> c) & 1)) continue;
-                                if (syh >= 0) p.psi_h_out[3][offy + c] = ps1[c];
-                                if (szh[c] >= 0) p.psi_h_out[4][offz + szh[c]] = ps2[c];
-                            }
-                        }
-                    }
-                    {   // hy: ex along z (plane m), ez along x (queue); x term added, z term subtracted
-                        float ps1[4], ps2[4], d27[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (uy >> c) & 1;
-                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[0] + offx + c) : 0.f;
-                            ps2[c] = up && szh[c] >= 0 ? __ldg(p.psi_h_in[5] + offz + szh[c]) : 0.f;
+                        {   // hy: ex along z (plane m), ez along x (queue); x term added
                             const float n = curl4(e2x.v[c], wx.at(c - 1), e2z.v[c], e1z.v[c]);
                             const float f = curl4(wx.at(c + 1), wx.at(c - 2), e3z.v[c], e0z.v[c]);
-                            d27[c] = fsub(fmul(27.0f, n), f);
-                        }
-#pragma unroll
-                        for (int st = 0; st < (HH ? 2 : 1); st++) {
-                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
-                            const Tab T0 = tab_h(p, st, 0), T2 = tab_h(p, st, 2);
-#pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((uy >> c) & 1)) continue;
-                                float v = fsub(vy.v[c], fmul(clch, d27[c]));
-                                if (sxh >= 0)
-                                    v = fadd(v, sterm(T0, sxh, ps1[c], d4h(e0z.v[c], e1z.v[c], e2z.v[c], e3z.v[c]), cl, p.ch));
-                                if (szh[c] >= 0)
-                                    v = fsub(v, sterm(T2, szh[c], ps2[c], d4h(wx.at(c - 2), wx.at(c - 1), wx.at(c), wx.at(c + 1)), cl, p.ch));
-                                vy.v[c] = v;
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vy.v[c], fmul(p.clch_a, d27));
+                            if (sxh >= 0) {
+                                const float d = d4h(e0z.v[c], e1z.v[c], e2z.v[c], e3z.v[c]);
+                                v = fadd(v, sterm(tab(p.ha[0]), sxh, py[c], d, p.cl_a, p.ch));
+                                if (HH) {
+                                    v = fsub(v, fmul(p.clch_b, d27));
+                                    v = fadd(v, sterm(tab(p.hb[0]), sxh, py[c], d, p.cl_b, p.ch));
+                                }
+                            } else if (HH) {
+                                v = fsub(v, fmul(p.clch_b, d27));
                             }
+                            if ((uy >> c) & 1) vy.v[c] = v;
                         }
-                        if (own) {
-#pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((uy >> c) & 1)) continue;
-                                if (sxh >= 0) p.psi_h_out[0][offx + c] = ps1[c];
-                                if (szh[c] >= 0) p.psi_h_out[5][offz + szh[c]] = ps2[c];
-                            }
-                        }
-                    }
-                    {   // hz: ey along x (queue), ex along y (plane m); x term subtracted, y term added
-                        float ps1[4], ps2[4], d27[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (uz >> c) & 1;
-                            ps1[c] = up && sxh >= 0 ? __ldg(p.psi_h_in[1] + offx + c) : 0.f;
-                            ps2[c] = up && syh >= 0 ? __ldg(p.psi_h_in[2] + offy + c) : 0.f;
+                        {   // hz: ey along x (queue), ex along y (plane m); x term subtracted
                             const float n = curl4(e2y.v[c], e1y.v[c], e2x.v[c], exm1.v[c]);
                             const float f = curl4(e3y.v[c], e0y.v[c], exp1.v[c], exm2.v[c]);
-                            d27[c] = fsub(fmul(27.0f, n), f);
-                        }
-#pragma unroll
-                        for (int st = 0; st < (HH ? 2 : 1); st++) {
-                            const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
-                            const Tab T0 = tab_h(p, st, 0), T1 = tab_h(p, st, 1);
-#pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((uz >> c) & 1)) continue;
-                                float v = fsub(vz.v[c], fmul(clch, d27[c]));
-                                if (sxh >= 0)
-                                    v = fsub(v, sterm(T0, sxh, ps1[c], d4h(e0y.v[c], e1y.v[c], e2y.v[c], e3y.v[c]), cl, p.ch));
-                                if (syh >= 0)
-                                    v = fadd(v, sterm(T1, syh, ps2[c], d4h(exm2.v[c], exm1.v[c], e2x.v[c], exp1.v[c]), cl, p.ch));
-                                vz.v[c] = v;
+                            const float d27 = fsub(fmul(27.0f, n), f);
+                            float v = fsub(vz.v[c], fmul(p.clch_a, d27));
+                            if (sxh >= 0) {
+                                const float d = d4h(e0y.v[c], e1y.v[c], e2y.v[c], e3y.v[c]);
+                                v = fsub(v, sterm(tab(p.ha[0]), sxh, pz[c], d, p.cl_a, p.ch));
+                                if (HH) {
+                                    v = fsub(v, fmul(p.clch_b, d27));
+                                    v = fsub(v, sterm(tab(p.hb[0]), sxh, pz[c], d, p.cl_b, p.ch));
+                                }
+                            } else if (HH) {
+                                v = fsub(v, fmul(p.clch_b, d27));
                             }
+                            if ((uz >> c) & 1) vz.v[c] = v;
                         }
-                        if (own) {
+                    }
+                }
+                if (own && sxh >= 0) {
 #pragma unroll
-                            for (int c = 0; c < 4; c++) {
-                                if (!((uz >> c) & 1)) continue;
-                                if (sxh >= 0) p.psi_h_out[1][offx + c] = ps1[c];
-                                if (syh >= 0) p.psi_h_out[2][offy + c] = ps2[c];
-                            }
-                        }
+                    for (int c = 0; c < 4; c++) {
+                        if ((uy & kown) >> c & 1) p.psi_h_out[0][offx + c] = py[c];
+                        if ((uz & kown) >> c & 1) p.psi_h_out[1][offx + c] = pz[c];
                     }
                 }
                 const int nsl = (m - (x0 - 1)) % NHN;
@@ -638,15 +550,15 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 hnz = vz;
                 if (own) {
                     const uint32_t rowo = (uint32_t)m * p.sx + (uint32_t)j * p.sy;
-                    stg4(p.out[3] + rowo, kg, p.nz, vx);
-                    stg4(p.out[4] + rowo, kg, p.nz, vy);
-                    stg4(p.out[5] + rowo, kg, p.nz, vz);
+                    stg4(p.out[3] + rowo, kg, kown, vx);
+                    stg4(p.out[4] + rowo, kg, kown, vy);
+                    stg4(p.out[5] + rowo, kg, kown, vz);
                 }
             }
 
             // ---- E_new(i), i = p - 3, at tile groups ----
             const int i = pl - 3;
-            if (q >= 6 && e_thread && row_in && (k_in & 1)) {
+            if (q >= 6 && own_row && kown) {
                 // H_new at planes i-1 .. i+2 of this group: n0 (i-1), n1 (i), n2 (i+1), hn (i+2);
                 // H_new(i) neighbours from the ring (written two iterations ago)
                 const int nsl = (i - (x0 - 1)) % NHN, nsl2 = (i + 1 - (x0 - 1)) % NHN;
@@ -662,116 +574,76 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 const ZW wx{lds4(hx + ho - 4), lds4(hx + ho), lds4(hx + ho + 4)};
                 V4 vx = e0x, vy = e0y, vz = e0z;  // input E of plane i
                 const bool iin = i > 0 && i < p.nx - 2;
-                const int sxe = p.cpml ? slab(p.ea[0], i, p.nx, true) : -1;
-                if (!yz_e && sxe < 0) {
+                const int sxe = p.cpml ? slab(p.ea[0], i, p.nx, true) : -1;  // uniform over the CTA
+                const uint32_t ux = jin_e ? kin_e : 0u, uy = (iin ? kin_e : 0u) & kown,
+                               uz = (iin && jin_e ? k_in : 0u) & kown;
+                const uint32_t offx = sxe >= 0 ? ((uint32_t)sxe * p.ny + j) * p.nz + kg : 0u;
+                float py[4], pz[4];  // x psi of ey and ez (x-slab planes), in place
+                if (sxe >= 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        py[c] = (uy >> c) & 1 ? p.psi_e[0][offx + c] : 0.f;
+                        pz[c] = (uz >> c) & 1 ? p.psi_e[1][offx + c] : 0.f;
+                    }
+                }
+                if (sxe < 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
                         {   // ex: hz along y, hy along z (plane i)
                             const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
                             const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
                             const float v = fadd(vx.v[c], fmul(fmul(p.dl, cvx.v[c]), fsub(fmul(27.0f, n), f)));
-                            if (jin_e && ((kin_e >> c) & 1)) vx.v[c] = v;
+                            if ((ux >> c) & 1) vx.v[c] = v;
                         }
-                        {   // ey: hx along z (plane i), hz along x (queue)
-                            const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
-                            const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
-                            const float v = fadd(vy.v[c], fmul(fmul(p.dl, cvy.v[c]), fsub(fmul(27.0f, n), f)));
-                            if (iin && ((kin_e >> c) & 1)) vy.v[c] = v;
-                        }
-                        {   // ez: hy along x (queue), hx along y (plane i)
-                            const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
-                            const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
-                            const float v = fadd(vz.v[c], fmul(fmul(p.dl, cvz.v[c]), fsub(fmul(27.0f, n), f)));
-                            if (iin && jin_e) vz.v[c] = v;
-                        }
-                    }
-                } else {
-                    // CPML path (E psi in place: only this thread touches these values)
-                    const uint32_t ux = jin_e ? kin_e : 0u, uy = iin ? kin_e : 0u, uz = iin && jin_e ? k_in : 0u;
-                    const uint32_t offx = sxe >= 0 ? ((uint32_t)sxe * p.ny + j) * p.nz + kg : 0u;
-                    const uint32_t offy = sye >= 0 ? ((uint32_t)i * (2u * p.ea[1].P) + sye) * p.nz + kg : 0u;
-                    const uint32_t offz = ((uint32_t)i * p.ny + j) * (2u * p.ea[2].P);
-                    int sze[4];
-#pragma unroll
-                    for (int c = 0; c < 4; c++) sze[c] = slab(p.ea[2], kg + c, p.nz, true);
-                    const Tab T0 = tab(p.ea[0]), T1 = tab(p.ea[1]), T2 = tab(p.ea[2]);
-                    {   // ex: hz along y, hy along z; y term added, z term subtracted
-                        float ps1[4], ps2[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (ux >> c) & 1;
-                            ps1[c] = up && sye >= 0 ? p.psi_e[3][offy + c] : 0.f;
-                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[4][offz + sze[c]] : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            if (!((ux >> c) & 1)) continue;
-                            const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
-                            const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
-                            const float cv = cvx.v[c];
-                            float v = fadd(vx.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                            if (sye >= 0) {
-                                v = fadd(v, sterm(T1, sye, ps1[c], d4e(hzm1.v[c], n1z.v[c], hzp1.v[c], hzp2.v[c]), p.dl, cv));
-                                p.psi_e[3][offy + c] = ps1[c];
-                            }
-                            if (sze[c] >= 0) {
-                                v = fsub(v, sterm(T2, sze[c], ps2[c], d4e(wy.at(c - 1), n1y.v[c], wy.at(c + 1), wy.at(c + 2)), p.dl, cv));
-                                p.psi_e[4][offz + sze[c]] = ps2[c];
-                            }
-                            vx.v[c] = v;
-                        }
-                    }
-                    {   // ey: hx along z (plane i), hz along x (queue); x term subtracted, z term added
-                        float ps1[4], ps2[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (uy >> c) & 1;
-                            ps1[c] = up && sxe >= 0 ? p.psi_e[0][offx + c] : 0.f;
-                            ps2[c] = up && sze[c] >= 0 ? p.psi_e[5][offz + sze[c]] : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            if (!((uy >> c) & 1)) continue;
+                        {   // ey: hx along z (plane i), hz along x; x term subtracted
                             const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
                             const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
                             const float cv = cvy.v[c];
                             float v = fadd(vy.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                            if (sxe >= 0) {
-                                v = fsub(v, sterm(T0, sxe, ps1[c], d4e(n0z.v[c], n1z.v[c], n2z.v[c], hnz.v[c]), p.dl, cv));
-                                p.psi_e[0][offx + c] = ps1[c];
-                            }
-                            if (sze[c] >= 0) {
-                                v = fadd(v, sterm(T2, sze[c], ps2[c], d4e(wx.at(c - 1), wx.at(c), wx.at(c + 1), wx.at(c + 2)), p.dl, cv));
-                                p.psi_e[5][offz + sze[c]] = ps2[c];
-                            }
-                            vy.v[c] = v;
+                            if ((uy >> c) & 1) vy.v[c] = v;
                         }
-                    }
-                    {   // ez: hy along x (queue), hx along y (plane i); x term added, y term subtracted
-                        float ps1[4], ps2[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const bool up = (uz >> c) & 1;
-                            ps1[c] = up && sxe >= 0 ? p.psi_e[1][offx + c] : 0.f;
-                            ps2[c] = up && sye >= 0 ? p.psi_e[2][offy + c] : 0.f;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            if (!((uz >> c) & 1)) continue;
+                        {   // ez: hy along x, hx along y (plane i); x term added
                             const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
                             const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
                             const float cv = cvz.v[c];
                             float v = fadd(vz.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
-                            if (sxe >= 0) {
-                                v = fadd(v, sterm(T0, sxe, ps1[c], d4e(n0y.v[c], n1y.v[c], n2y.v[c], hny.v[c]), p.dl, cv));
-                                p.psi_e[1][offx + c] = ps1[c];
-                            }
-                            if (sye >= 0) {
-                                v = fsub(v, sterm(T1, sye, ps2[c], d4e(hxm1.v[c], wx.at(c), hxp1.v[c], hxp2.v[c]), p.dl, cv));
-                                p.psi_e[2][offy + c] = ps2[c];
-                            }
-                            vz.v[c] = v;
+                            if ((uz >> c) & 1) vz.v[c] = v;
                         }
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        {   // ex: hz along y, hy along z (plane i)
+                            const float n = curl4(hzp1.v[c], n1z.v[c], wy.at(c + 1), n1y.v[c]);
+                            const float f = curl4(hzp2.v[c], hzm1.v[c], wy.at(c + 2), wy.at(c - 1));
+                            const float v = fadd(vx.v[c], fmul(fmul(p.dl, cvx.v[c]), fsub(fmul(27.0f, n), f)));
+                            if ((ux >> c) & 1) vx.v[c] = v;
+                        }
+                        {   // ey: hx along z (plane i), hz along x; x term subtracted
+                            const float n = curl4(wx.at(c + 1), wx.at(c), n2z.v[c], n1z.v[c]);
+                            const float f = curl4(wx.at(c + 2), wx.at(c - 1), hnz.v[c], n0z.v[c]);
+                            const float cv = cvy.v[c];
+                            float v = fadd(vy.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                            if (sxe >= 0)
+                                v = fsub(v, sterm(tab(p.ea[0]), sxe, py[c], d4e(n0z.v[c], n1z.v[c], n2z.v[c], hnz.v[c]), p.dl, cv));
+                            if ((uy >> c) & 1) vy.v[c] = v;
+                        }
+                        {   // ez: hy along x, hx along y (plane i); x term added
+                            const float n = curl4(n2y.v[c], n1y.v[c], hxp1.v[c], wx.at(c));
+                            const float f = curl4(hny.v[c], n0y.v[c], hxp2.v[c], hxm1.v[c]);
+                            const float cv = cvz.v[c];
+                            float v = fadd(vz.v[c], fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+                            if (sxe >= 0)
+                                v = fadd(v, sterm(tab(p.ea[0]), sxe, pz[c], d4e(n0y.v[c], n1y.v[c], n2y.v[c], hny.v[c]), p.dl, cv));
+                            if ((uz >> c) & 1) vz.v[c] = v;
+                        }
+                    }
+                }
+                if (sxe >= 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        if ((uy >> c) & 1) p.psi_e[0][offx + c] = py[c];
+                        if ((uz >> c) & 1) p.psi_e[1][offx + c] = pz[c];
                     }
                 }
                 for (int s = 0; s < nls; s++) {  // soft sources, list order
@@ -788,9 +660,9 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                     }
                 }
                 const uint32_t rowo = (uint32_t)i * p.sx + (uint32_t)j * p.sy;
-                stg4(p.out[0] + rowo, kg, p.nz, vx);
-                stg4(p.out[1] + rowo, kg, p.nz, vy);
-                stg4(p.out[2] + rowo, kg, p.nz, vz);
+                stg4(p.out[0] + rowo, kg, kown, vx);
+                stg4(p.out[1] + rowo, kg, kown, vy);
+                stg4(p.out[2] + rowo, kg, kown, vz);
             }
             // advance the queue
             e0x = e1x; e0y = e1y; e0z = e1z;
@@ -827,6 +699,212 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
             p.queue[1] = 0;
             __threadfence();
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Edge shell: the cells outside the pair kernel's tiles (the y and z CPML
+// slabs and a tile of margin), one thread per cell, out of place:
+//   k_edge_h<false>  H_out = H_in - clch_a curl4(E_in) with its CPML terms
+//                    (psi_h_in -> psi_h_out);
+//   k_edge_h<true>   the second H stage of a two-H pass, in place on H_out
+//                    (psi_h_out in place);
+//   k_edge_e         E_out = E_in + dl ce curl4(H_out) with its CPML terms
+//                    (psi_e in place), once the pair kernel has written the
+//                    interior H_out;
+//   k_edge_src       the soft sources on edge cells, in list order.
+// Same expressions and operation order as the stage kernels.  The pair
+// kernel's tiles never read a y or z slab cell, so the two parts meet only
+// through H_out, which k_edge_e reads after both have written it.
+// ---------------------------------------------------------------------------
+struct Edge {
+    int32_t n;                           // boxes
+    int32_t j0[4], j1[4], k0[4], k1[4];  // rows [j0, j1), columns [k0, k1), every x plane
+    int64_t off[5];                      // first cell of each box in the flattened launch
+};
+constexpr int EDGE_BLOCK = 256;
+
+__device__ __forceinline__ bool edge_cell(const Params &p, const Edge &eb, int64_t u, int &i, int &j, int &k) {
+    if (u >= eb.off[eb.n]) return false;
+    int b = 0;
+    while (b + 1 < eb.n && u >= eb.off[b + 1]) b++;
+    const int64_t v = u - eb.off[b];
+    const int nk = eb.k1[b] - eb.k0[b], nj = eb.j1[b] - eb.j0[b];
+    k = eb.k0[b] + (int)(v % nk);
+    const int64_t w = v / nk;
+    j = eb.j0[b] + (int)(w % nj);
+    i = (int)(w / nj);
+    return true;
+}
+
+template <bool B>
+__global__ void __launch_bounds__(EDGE_BLOCK)
+k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
+    int i, j, k;
+    if (!edge_cell(p, eb, (int64_t)blockIdx.x * EDGE_BLOCK + threadIdx.x, i, j, k)) return;
+    const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
+    const float *ex = p.in[0], *ey = p.in[1], *ez = p.in[2];
+    const float *const *pin = B ? const_cast<const float *const *>(p.psi_h_out) : p.psi_h_in;
+    const float clch = B ? p.clch_b : p.clch_a, cl = B ? p.cl_b : p.cl_a;
+    const Tab T0 = tab_h(p, B, 0), T1 = tab_h(p, B, 1), T2 = tab_h(p, B, 2);
+    const bool jin = j > 1 && j < p.ny - 1, kin = k > 1 && k < p.nz - 1, iin = i > 1 && i < p.nx - 1;
+    const int sx = slab(p.ha[0], i, p.nx, false), sy = slab(p.ha[1], j, p.ny, false),
+              sz = slab(p.ha[2], k, p.nz, false);
+    {   // hx: y term subtracted, z term added
+        float v = B ? p.out[3][c] : p.in[3][c];
+        if (jin && kin) {
+            const float n = curl4(ez[c], ez[c - Y], ey[c], ey[c - 1]);
+            const float f = curl4(ez[c + Y], ez[c - 2 * Y], ey[c + 1], ey[c - 2]);
+            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
+            if (sy >= 0) {
+                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
+                float ps = pin[3][q];
+                v = fsub(v, sterm(T1, sy, ps, d4h(ez[c - 2 * Y], ez[c - Y], ez[c], ez[c + Y]), cl, p.ch));
+                p.psi_h_out[3][q] = ps;
+            }
+            if (sz >= 0) {
+                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
+                float ps = pin[4][q];
+                v = fadd(v, sterm(T2, sz, ps, d4h(ey[c - 2], ey[c - 1], ey[c], ey[c + 1]), cl, p.ch));
+                p.psi_h_out[4][q] = ps;
+            }
+        }
+        p.out[3][c] = v;
+    }
+    {   // hy: x term added, z term subtracted
+        float v = B ? p.out[4][c] : p.in[4][c];
+        if (iin && kin) {
+            const float n = curl4(ex[c], ex[c - 1], ez[c], ez[c - X]);
+            const float f = curl4(ex[c + 1], ex[c - 2], ez[c + X], ez[c - 2 * X]);
+            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
+            if (sx >= 0) {
+                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
+                float ps = pin[0][q];
+                v = fadd(v, sterm(T0, sx, ps, d4h(ez[c - 2 * X], ez[c - X], ez[c], ez[c + X]), cl, p.ch));
+                p.psi_h_out[0][q] = ps;
+            }
+            if (sz >= 0) {
+                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
+                float ps = pin[5][q];
+                v = fsub(v, sterm(T2, sz, ps, d4h(ex[c - 2], ex[c - 1], ex[c], ex[c + 1]), cl, p.ch));
+                p.psi_h_out[5][q] = ps;
+            }
+        }
+        p.out[4][c] = v;
+    }
+    {   // hz: x term subtracted, y term added
+        float v = B ? p.out[5][c] : p.in[5][c];
+        if (iin && jin) {
+            const float n = curl4(ey[c], ey[c - X], ex[c], ex[c - Y]);
+            const float f = curl4(ey[c + X], ey[c - 2 * X], ex[c + Y], ex[c - 2 * Y]);
+            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
+            if (sx >= 0) {
+                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
+                float ps = pin[1][q];
+                v = fsub(v, sterm(T0, sx, ps, d4h(ey[c - 2 * X], ey[c - X], ey[c], ey[c + X]), cl, p.ch));
+                p.psi_h_out[1][q] = ps;
+            }
+            if (sy >= 0) {
+                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
+                float ps = pin[2][q];
+                v = fadd(v, sterm(T1, sy, ps, d4h(ex[c - 2 * Y], ex[c - Y], ex[c], ex[c + Y]), cl, p.ch));
+                p.psi_h_out[2][q] = ps;
+            }
+        }
+        p.out[5][c] = v;
+    }
+}
+
+__global__ void __launch_bounds__(EDGE_BLOCK)
+k_edge_e(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
+    int i, j, k;
+    if (!edge_cell(p, eb, (int64_t)blockIdx.x * EDGE_BLOCK + threadIdx.x, i, j, k)) return;
+    const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
+    const float *hx = p.out[3], *hy = p.out[4], *hz = p.out[5];
+    const Tab T0 = tab(p.ea[0]), T1 = tab(p.ea[1]), T2 = tab(p.ea[2]);
+    const bool jin = j > 0 && j < p.ny - 2, kin = k > 0 && k < p.nz - 2, iin = i > 0 && i < p.nx - 2;
+    const int sx = slab(p.ea[0], i, p.nx, true), sy = slab(p.ea[1], j, p.ny, true),
+              sz = slab(p.ea[2], k, p.nz, true);
+    {   // ex: y term added, z term subtracted
+        float v = p.in[0][c];
+        if (jin && kin) {
+            const float n = curl4(hz[c + Y], hz[c], hy[c + 1], hy[c]);
+            const float f = curl4(hz[c + 2 * Y], hz[c - Y], hy[c + 2], hy[c - 1]);
+            const float cv = p.ce[0][c];
+            v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+            if (sy >= 0) {
+                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
+                float ps = p.psi_e[3][q];
+                v = fadd(v, sterm(T1, sy, ps, d4e(hz[c - Y], hz[c], hz[c + Y], hz[c + 2 * Y]), p.dl, cv));
+                p.psi_e[3][q] = ps;
+            }
+            if (sz >= 0) {
+                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
+                float ps = p.psi_e[4][q];
+                v = fsub(v, sterm(T2, sz, ps, d4e(hy[c - 1], hy[c], hy[c + 1], hy[c + 2]), p.dl, cv));
+                p.psi_e[4][q] = ps;
+            }
+        }
+        p.out[0][c] = v;
+    }
+    {   // ey: x term subtracted, z term added
+        float v = p.in[1][c];
+        if (iin && kin) {
+            const float n = curl4(hx[c + 1], hx[c], hz[c + X], hz[c]);
+            const float f = curl4(hx[c + 2], hx[c - 1], hz[c + 2 * X], hz[c - X]);
+            const float cv = p.ce[1][c];
+            v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+            if (sx >= 0) {
+                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
+                float ps = p.psi_e[0][q];
+                v = fsub(v, sterm(T0, sx, ps, d4e(hz[c - X], hz[c], hz[c + X], hz[c + 2 * X]), p.dl, cv));
+                p.psi_e[0][q] = ps;
+            }
+            if (sz >= 0) {
+                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
+                float ps = p.psi_e[5][q];
+                v = fadd(v, sterm(T2, sz, ps, d4e(hx[c - 1], hx[c], hx[c + 1], hx[c + 2]), p.dl, cv));
+                p.psi_e[5][q] = ps;
+            }
+        }
+        p.out[1][c] = v;
+    }
+    {   // ez: x term added, y term subtracted
+        float v = p.in[2][c];
+        if (iin && jin) {
+            const float n = curl4(hy[c + X], hy[c], hx[c + Y], hx[c]);
+            const float f = curl4(hy[c + 2 * X], hy[c - X], hx[c + 2 * Y], hx[c - Y]);
+            const float cv = p.ce[2][c];
+            v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
+            if (sx >= 0) {
+                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
+                float ps = p.psi_e[1][q];
+                v = fadd(v, sterm(T0, sx, ps, d4e(hy[c - X], hy[c], hy[c + X], hy[c + 2 * X]), p.dl, cv));
+                p.psi_e[1][q] = ps;
+            }
+            if (sy >= 0) {
+                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
+                float ps = p.psi_e[2][q];
+                v = fsub(v, sterm(T1, sy, ps, d4e(hx[c - Y], hx[c], hx[c + Y], hx[c + 2 * Y]), p.dl, cv));
+                p.psi_e[2][q] = ps;
+            }
+        }
+        p.out[2][c] = v;
+    }
+}
+
+// soft sources on edge cells, list order (one thread: a list holds a few sources)
+__global__ void k_edge_src(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || p.t < 0 || p.t >= p.namp) return;
+    for (int s = 0; s < p.nsrc; s++) {
+        const int si = p.src_ijk[3 * s], sj = p.src_ijk[3 * s + 1], sk = p.src_ijk[3 * s + 2];
+        bool in = false;
+        for (int b = 0; b < eb.n; b++)
+            in |= sj >= eb.j0[b] && sj < eb.j1[b] && sk >= eb.k0[b] && sk < eb.k1[b];
+        if (!in) continue;
+        float *f = p.out[p.src_comp[s]];
+        const int64_t c = (int64_t)si * p.sx + (int64_t)sj * p.sy + sk;
+        f[c] = fadd(f[c], p.src_amp[(int64_t)s * p.namp + p.t]);
     }
 }
 
@@ -871,7 +949,8 @@ struct fdtd_symp_plan {
     Params base;
     float *f[2][6];
     const float *psi_h[2][6];
-    int nblocks;
+    std::vector<int32_t> src_ijk;  // host copy of the source positions
+    int slots;                     // resident CTAs of the pair kernel (SMs x CTAs per SM)
     int cur;
 };
 
@@ -905,6 +984,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
     if (x_chunk < 0) { delete pl; return FDTD_ERR_ARG; }
     p.x_chunk = (int32_t)std::min<int64_t>(x_chunk > 0 ? x_chunk : 128, g.nx);
     p.nxc = (int32_t)((g.nx + p.x_chunk - 1) / p.x_chunk);
+    for (int q = 0; q < 3; q++) p.ce[q] = s->ce[q];
     p.status = status_dev;
     p.queue = queue_dev;
     for (int b = 0; b < 2; b++)
@@ -922,6 +1002,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
                                         as_stream(stream));
         if (e == cudaSuccess) e = cudaStreamSynchronize(as_stream(stream));
         if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
+        pl->src_ijk = h;
         std::vector<int> count((size_t)p.ntz * p.nty * p.nxc, 0);
         for (int a = 0; a < src->nsrc; a++) {
             const int64_t si = h[3 * a], sj = h[3 * a + 1], sk = h[3 * a + 2];
@@ -953,8 +1034,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
     occ = std::min(occ, occ1);
     if (e != cudaSuccess) { set_cuda_error(e); delete pl; return FDTD_ERR_CUDA; }
     if (occ < 1) { delete pl; return FDTD_ERR_UNSUPPORTED; }
-    const int64_t nitems = (int64_t)p.ntz * p.nty * p.nxc;
-    pl->nblocks = (int)std::min<int64_t>(nitems, (int64_t)nsm * occ);
+    pl->slots = nsm * occ;
     *out = pl;
     return FDTD_OK;
 }
@@ -1000,15 +1080,86 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
                         : p.psi_h_in[2 * ax] && p.psi_h_in[2 * ax + 1] && p.psi_h_out[2 * ax] && p.psi_h_out[2 * ax + 1]))
                     return FDTD_ERR_ARG;
                 p.cpml = 1;
-                if (ax > 0) p.edge_first = 1;
             }
             dst[w][ax] = A;
         }
     }
-    if (two_h)
-        k_symp_pair<true><<<pl->nblocks, THREADS, SMEM, as_stream(stream)>>>(pl->maps[in], p);
-    else
-        k_symp_pair<false><<<pl->nblocks, THREADS, SMEM, as_stream(stream)>>>(pl->maps[in], p);
+    for (int q = 0; q < 6; q++) p.in[q] = pl->f[in][q];
+    // the pair kernel's region: E_new of rows [j_lo, j_hi) needs H_new of rows
+    // j_lo-1 .. j_hi+1, which must hold no y-slab node of any stage (front
+    // nodes 1 .. P, back nodes n-P-1 .. n-1): j_lo = P+2, j_hi = n-P-2; the
+    // same along z, with k_lo rounded up to 4 cells (16-byte TMA boxes)
+    auto pf = [&](int ax) {
+        int v = 0;
+        for (const Axis *A : {&p.ha[ax], &p.hb[ax], &p.ea[ax]}) v = std::max(v, A->front ? A->P : 0);
+        return v;
+    };
+    auto pb = [&](int ax) {
+        int v = 0;
+        for (const Axis *A : {&p.ha[ax], &p.hb[ax], &p.ea[ax]}) v = std::max(v, A->back ? A->P : 0);
+        return v;
+    };
+    const int64_t ny = pl->g.ny, nz = pl->g.nz;
+    p.j_lo = pf(1) > 0 ? pf(1) + 2 : 0;
+    p.j_hi = (int32_t)(pb(1) > 0 ? ny - pb(1) - 2 : ny);
+    p.k_lo = pf(2) > 0 ? (pf(2) + 2 + 3) / 4 * 4 : 0;
+    p.k_hi = (int32_t)(pb(2) > 0 ? nz - pb(2) - 2 : nz);
+    p.nty_in = p.j_hi > p.j_lo ? (p.j_hi - p.j_lo + TY - 1) / TY : 0;
+    // z tiles stay on TZ-column boundaries (128-byte rows for the boxes and the
+    // stores): they start at k_lo rounded down and mask the columns outside
+    // [k_lo, k_hi)
+    p.kt0 = p.k_lo / TZ * TZ;
+    p.ntz_in = p.k_hi > p.k_lo ? (p.k_hi - p.kt0 + TZ - 1) / TZ : 0;
+    // the edge shell: rows outside [j_lo, j_hi), then the columns outside
+    // [k_lo, k_hi) of those rows (every x plane)
+    Edge eb{};
+    auto add_box = [&](int64_t j0, int64_t j1, int64_t k0, int64_t k1) {
+        if (j1 <= j0 || k1 <= k0) return;
+        eb.j0[eb.n] = (int)j0; eb.j1[eb.n] = (int)j1; eb.k0[eb.n] = (int)k0; eb.k1[eb.n] = (int)k1;
+        eb.off[eb.n + 1] = eb.off[eb.n] + pl->g.nx * (j1 - j0) * (k1 - k0);
+        eb.n++;
+    };
+    if (p.nty_in == 0 || p.ntz_in == 0) {
+        p.nty_in = p.ntz_in = 0;
+        add_box(0, ny, 0, nz);
+    } else {
+        add_box(0, p.j_lo, 0, nz);
+        add_box(p.j_hi, ny, 0, nz);
+        add_box(p.j_lo, p.j_hi, 0, p.k_lo);
+        add_box(p.j_lo, p.j_hi, p.k_hi, nz);
+    }
+    // sources per tile of this tiling (the kernel stages at most MAX_SRC per tile)
+    if (p.nty_in > 0 && p.ntz_in > 0 && pl->src_ijk.size() / 3 > (size_t)MAX_SRC) {
+        std::vector<int> count((size_t)p.nty_in * p.ntz_in * p.nxc, 0);
+        for (size_t a = 0; a + 2 < pl->src_ijk.size(); a += 3) {
+            const int si = pl->src_ijk[a], sj = pl->src_ijk[a + 1], sk = pl->src_ijk[a + 2];
+            if (sj < p.j_lo || sj >= p.j_hi || sk < p.k_lo || sk >= p.k_hi) continue;
+            const size_t it = ((size_t)(si / p.x_chunk) * p.nty_in + (sj - p.j_lo) / TY) * p.ntz_in + (sk - p.kt0) / TZ;
+            if (++count[it] > MAX_SRC) return FDTD_ERR_CAPACITY;
+        }
+    }
+    cudaStream_t st = as_stream(stream);
+    const int64_t items = (int64_t)p.nty_in * p.ntz_in * p.nxc;
+    if (items > 0) {
+        const int nb = (int)std::min<int64_t>(items, pl->slots);
+        if (two_h)
+            k_symp_pair<true><<<nb, THREADS, SMEM, st>>>(pl->maps[in], p);
+        else
+            k_symp_pair<false><<<nb, THREADS, SMEM, st>>>(pl->maps[in], p);
+    }
+    const int64_t ecells = eb.off[eb.n];
+    if (ecells > 0) {
+        const unsigned nb = (unsigned)((ecells + EDGE_BLOCK - 1) / EDGE_BLOCK);
+        k_edge_h<false><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
+        if (two_h) k_edge_h<true><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
+        k_edge_e<<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
+        bool esrc = false;
+        for (size_t a = 0; a + 2 < pl->src_ijk.size(); a += 3)
+            for (int b = 0; b < eb.n; b++)
+                esrc |= pl->src_ijk[a + 1] >= eb.j0[b] && pl->src_ijk[a + 1] < eb.j1[b] &&
+                        pl->src_ijk[a + 2] >= eb.k0[b] && pl->src_ijk[a + 2] < eb.k1[b];
+        if (esrc && src_t >= 0 && src_t < p.namp) k_edge_src<<<1, 32, 0, st>>>(p, eb);
+    }
     FDTD_TRY(check_launch());
     pl->cur = ob;
     return FDTD_OK;

@@ -196,6 +196,11 @@ def test_symplectic_cpml_absorbs(S):
     ((28, 20, 36), 3, 0x2A, 7, 3),        # back faces only
     ((36, 18, 40), 0, 0x3F, 9, 3),        # no CPML
     ((24, 50, 100), 6, 0x3F, 0, 1),       # one step: no merged H stages
+    # grids with tiles clear of the y/z slabs (the pair kernel) and an edge shell
+    ((40, 60, 132), 5, 0x3F, 0, 3),       # merged H stages on both parts
+    ((33, 64, 100), 4, 0x15, 7, 2),       # front faces only
+    ((36, 70, 164), 6, 0x30, 0, 2),       # z faces only: no y edge rows
+    ((30, 80, 68), 3, 0x0C, 9, 2),        # y faces only
 ])
 def test_stage_pairs_equal_stage_kernels(S, shape, npml, faces, x_chunk, steps):
     """The fused stage pairs (one pass per H+E stage pair, the closing and

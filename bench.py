@@ -490,7 +490,7 @@ def run_symp512(args):
     dev = torch.device("cuda", 0)
     shape, npml = tuple(args.symp_shape), 10
     s = configs.symp512_solver(shape, device=dev, max_steps=args.warmup + args.steps + 2, npml=npml,
-                               fused=args.symp_fused)
+                               fused=not args.symp_stages)
     stream = torch.cuda.current_stream(dev)
     s.step(args.warmup)
     torch.cuda.synchronize()
@@ -512,11 +512,16 @@ def run_symp512(args):
     alg_pair = symplectic_pair_bytes_per_step(shape, npml)
     alg_fused = algorithmic_bytes_per_step(shape, npml)
     peak, psrc = measured_peak()
-    achieved = alg / (avg / 1e3) / 1e9
     pair = s.pair_path()
-    # launches: four stage-pair passes per step and the run's last H stage, or
-    # per step 5 H and 4 E stage launches and a source launch after each E stage
-    launches = 4 * args.steps + 1 if pair else args.steps * (5 + 4 * 2)
+    # the roofline of the path that ran: the stage-pair byte count (four passes
+    # of 60 B/cell) or the stage-by-stage one (372 B/cell)
+    alg_run = alg_pair if pair else alg
+    achieved = alg_run / (avg / 1e3) / 1e9
+    # launches: per pass the pair kernel, the edge H and E kernels (a second
+    # edge H kernel in the n-1 passes that merge two H stages), and the run's
+    # last H stage; or per step 5 H and 4 E stage launches and a source launch
+    # after each E stage
+    launches = 4 * args.steps * 3 + (args.steps - 1) + 1 if pair else args.steps * (5 + 4 * 2)
     accuracy = None
     if args.accuracy_steps:
         from fdtd_accelerate_gb300.fp64 import SympRun64, family_errors
@@ -534,14 +539,19 @@ def run_symp512(args):
     line = _base_line("Mcell-updates/s (4th-order symplectic %dx%dx%d, 10-cell CPML, FP32)" % shape, cells / (avg / 1e3) / 1e6,
                       UNIT, args, avg, "f32", "4th-order symplectic %dx%dx%d, 10-cell CPML, 60 spheres eps_r " % shape +
                       "U[1,4], Ez dipole; 4 E + 5 H stages per step, " +
-                      ("four fused stage-pair passes per step (k_symp_pair) in one %d-step run" % args.steps
+                      ("four stage-pair passes per step (k_symp_pair inside, k_edge_* on the y/z CPML shell) "
+                       "in one %d-step run" % args.steps
                        if pair else "one launch per stage with its CPML slabs") +
                       " (6 fields + 3 coefficient arrays: %.1f GB >> L2)" % (9 * cells * 4 / 1e9),
                       {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                     "frac": achieved / peak, "traffic": None, "peak_source": psrc,
-                                    "alg_bytes_per_launch": alg,
-                                    "scope": "one time step on the stage-by-stage byte count of the workload "
-                                             "(372 B/cell + 144 B per slab cell)",
+                                    "alg_bytes_per_launch": alg_run,
+                                    "scope": ("one time step on the stage-pair byte count (four passes of "
+                                              "60 B/cell + 128 B per slab cell)") if pair else
+                                             ("one time step on the stage-by-stage byte count of the workload "
+                                              "(372 B/cell + 144 B per slab cell)"),
+                                    "frac_of_stage_bytes": alg / (avg / 1e3) / 1e9 / peak,
+                                    "stage_bytes_per_step": alg,
                                     "frac_of_pair_pass_bytes": alg_pair / (avg / 1e3) / 1e9 / peak,
                                     "pair_pass_bytes_per_step": alg_pair,
                                     "frac_of_fused_step_bytes": alg_fused / (avg / 1e3) / 1e9 / peak},
@@ -821,8 +831,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--symp-shape", type=lambda s: tuple(int(v) for v in s.split(",")), default=(512, 512, 512),
                     help="grid of --workload symp512 (a smaller one for profiling)")
-    ap.add_argument("--symp-fused", action="store_true",
-                    help="--workload symp512 on the fused stage-pair kernel instead of the per-stage kernels")
+    ap.add_argument("--symp-stages", action="store_true",
+                    help="--workload symp512 on the per-stage kernels instead of the stage-pair path")
     ap.add_argument("--shape", type=lambda s: tuple(int(v) for v in s.split(",")), default=SHAPE,
                     help="grid (default 1024,1024,512); other sizes scale the same workload")
     ap.add_argument("--tile", type=lambda s: tuple(int(v) for v in s.split(",")), default=None)

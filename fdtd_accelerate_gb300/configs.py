@@ -146,7 +146,7 @@ def adjoint256(steps=3000, shape=(256, 256, 128), region=(128, 128, 64), npml=12
                            tuple(shape), steps, npml, eps, design, sources, [("ez", p) for p in probes], segment)
 
 
-def symp512_solver(shape=(512, 512, 512), device="cuda", max_steps=0, npml=10, seed=20261206, fused=False):
+def symp512_solver(shape=(512, 512, 512), device="cuda", max_steps=0, npml=10, seed=20261206, fused=True):
     """The 4th-order workload: 512^3, 10-cell CPML, 60 seeded spheres (radius
     5..40, eps_r U[1,4]), ce = (S/24)/eps_r, ch = S/24, an Ez dipole at the
     centre with the Gaussian-modulated sine (f dt = 0.05, width 30, t0 = 150)

@@ -720,20 +720,22 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
 struct Edge {
     int32_t n;                           // boxes
     int32_t j0[4], j1[4], k0[4], k1[4];  // rows [j0, j1), columns [k0, k1), every x plane
-    int64_t off[5];                      // first cell of each box in the flattened launch
+    uint32_t off[5];                     // first cell of each box within one x plane
 };
 constexpr int EDGE_BLOCK = 256;
 
-__device__ __forceinline__ bool edge_cell(const Params &p, const Edge &eb, int64_t u, int &i, int &j, int &k) {
+// launch: blockIdx.y = x plane, blockIdx.x * EDGE_BLOCK + threadIdx.x = cell of
+// the plane's part of the shell (box by box, z fastest)
+__device__ __forceinline__ bool edge_cell(const Edge &eb, int &i, int &j, int &k) {
+    const uint32_t u = blockIdx.x * EDGE_BLOCK + threadIdx.x;
     if (u >= eb.off[eb.n]) return false;
     int b = 0;
     while (b + 1 < eb.n && u >= eb.off[b + 1]) b++;
-    const int64_t v = u - eb.off[b];
-    const int nk = eb.k1[b] - eb.k0[b], nj = eb.j1[b] - eb.j0[b];
-    k = eb.k0[b] + (int)(v % nk);
-    const int64_t w = v / nk;
-    j = eb.j0[b] + (int)(w % nj);
-    i = (int)(w / nj);
+    const uint32_t v = u - eb.off[b], nk = (uint32_t)(eb.k1[b] - eb.k0[b]);
+    const uint32_t r = v / nk;
+    k = eb.k0[b] + (int)(v - r * nk);
+    j = eb.j0[b] + (int)r;
+    i = blockIdx.y;
     return true;
 }
 
@@ -741,7 +743,7 @@ template <bool B>
 __global__ void __launch_bounds__(EDGE_BLOCK)
 k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     int i, j, k;
-    if (!edge_cell(p, eb, (int64_t)blockIdx.x * EDGE_BLOCK + threadIdx.x, i, j, k)) return;
+    if (!edge_cell(eb, i, j, k)) return;
     const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
     const float *ex = p.in[0], *ey = p.in[1], *ez = p.in[2];
     const float *const *pin = B ? const_cast<const float *const *>(p.psi_h_out) : p.psi_h_in;
@@ -751,63 +753,63 @@ k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     const int sx = slab(p.ha[0], i, p.nx, false), sy = slab(p.ha[1], j, p.ny, false),
               sz = slab(p.ha[2], k, p.nz, false);
     {   // hx: y term subtracted, z term added
-        float v = B ? p.out[3][c] : p.in[3][c];
+        float v = B ? p.out[3][c] : __ldg(p.in[3] + c);
         if (jin && kin) {
-            const float n = curl4(ez[c], ez[c - Y], ey[c], ey[c - 1]);
-            const float f = curl4(ez[c + Y], ez[c - 2 * Y], ey[c + 1], ey[c - 2]);
+            const float n = curl4(__ldg(ez + (c)), __ldg(ez + (c - Y)), __ldg(ey + (c)), __ldg(ey + (c - 1)));
+            const float f = curl4(__ldg(ez + (c + Y)), __ldg(ez + (c - 2 * Y)), __ldg(ey + (c + 1)), __ldg(ey + (c - 2)));
             v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
                 float ps = pin[3][q];
-                v = fsub(v, sterm(T1, sy, ps, d4h(ez[c - 2 * Y], ez[c - Y], ez[c], ez[c + Y]), cl, p.ch));
+                v = fsub(v, sterm(T1, sy, ps, d4h(__ldg(ez + (c - 2 * Y)), __ldg(ez + (c - Y)), __ldg(ez + (c)), __ldg(ez + (c + Y))), cl, p.ch));
                 p.psi_h_out[3][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
                 float ps = pin[4][q];
-                v = fadd(v, sterm(T2, sz, ps, d4h(ey[c - 2], ey[c - 1], ey[c], ey[c + 1]), cl, p.ch));
+                v = fadd(v, sterm(T2, sz, ps, d4h(__ldg(ey + (c - 2)), __ldg(ey + (c - 1)), __ldg(ey + (c)), __ldg(ey + (c + 1))), cl, p.ch));
                 p.psi_h_out[4][q] = ps;
             }
         }
         p.out[3][c] = v;
     }
     {   // hy: x term added, z term subtracted
-        float v = B ? p.out[4][c] : p.in[4][c];
+        float v = B ? p.out[4][c] : __ldg(p.in[4] + c);
         if (iin && kin) {
-            const float n = curl4(ex[c], ex[c - 1], ez[c], ez[c - X]);
-            const float f = curl4(ex[c + 1], ex[c - 2], ez[c + X], ez[c - 2 * X]);
+            const float n = curl4(__ldg(ex + (c)), __ldg(ex + (c - 1)), __ldg(ez + (c)), __ldg(ez + (c - X)));
+            const float f = curl4(__ldg(ex + (c + 1)), __ldg(ex + (c - 2)), __ldg(ez + (c + X)), __ldg(ez + (c - 2 * X)));
             v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
                 float ps = pin[0][q];
-                v = fadd(v, sterm(T0, sx, ps, d4h(ez[c - 2 * X], ez[c - X], ez[c], ez[c + X]), cl, p.ch));
+                v = fadd(v, sterm(T0, sx, ps, d4h(__ldg(ez + (c - 2 * X)), __ldg(ez + (c - X)), __ldg(ez + (c)), __ldg(ez + (c + X))), cl, p.ch));
                 p.psi_h_out[0][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
                 float ps = pin[5][q];
-                v = fsub(v, sterm(T2, sz, ps, d4h(ex[c - 2], ex[c - 1], ex[c], ex[c + 1]), cl, p.ch));
+                v = fsub(v, sterm(T2, sz, ps, d4h(__ldg(ex + (c - 2)), __ldg(ex + (c - 1)), __ldg(ex + (c)), __ldg(ex + (c + 1))), cl, p.ch));
                 p.psi_h_out[5][q] = ps;
             }
         }
         p.out[4][c] = v;
     }
     {   // hz: x term subtracted, y term added
-        float v = B ? p.out[5][c] : p.in[5][c];
+        float v = B ? p.out[5][c] : __ldg(p.in[5] + c);
         if (iin && jin) {
-            const float n = curl4(ey[c], ey[c - X], ex[c], ex[c - Y]);
-            const float f = curl4(ey[c + X], ey[c - 2 * X], ex[c + Y], ex[c - 2 * Y]);
+            const float n = curl4(__ldg(ey + (c)), __ldg(ey + (c - X)), __ldg(ex + (c)), __ldg(ex + (c - Y)));
+            const float f = curl4(__ldg(ey + (c + X)), __ldg(ey + (c - 2 * X)), __ldg(ex + (c + Y)), __ldg(ex + (c - 2 * Y)));
             v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
                 float ps = pin[1][q];
-                v = fsub(v, sterm(T0, sx, ps, d4h(ey[c - 2 * X], ey[c - X], ey[c], ey[c + X]), cl, p.ch));
+                v = fsub(v, sterm(T0, sx, ps, d4h(__ldg(ey + (c - 2 * X)), __ldg(ey + (c - X)), __ldg(ey + (c)), __ldg(ey + (c + X))), cl, p.ch));
                 p.psi_h_out[1][q] = ps;
             }
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
                 float ps = pin[2][q];
-                v = fadd(v, sterm(T1, sy, ps, d4h(ex[c - 2 * Y], ex[c - Y], ex[c], ex[c + Y]), cl, p.ch));
+                v = fadd(v, sterm(T1, sy, ps, d4h(__ldg(ex + (c - 2 * Y)), __ldg(ex + (c - Y)), __ldg(ex + (c)), __ldg(ex + (c + Y))), cl, p.ch));
                 p.psi_h_out[2][q] = ps;
             }
         }
@@ -818,7 +820,7 @@ k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
 __global__ void __launch_bounds__(EDGE_BLOCK)
 k_edge_e(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     int i, j, k;
-    if (!edge_cell(p, eb, (int64_t)blockIdx.x * EDGE_BLOCK + threadIdx.x, i, j, k)) return;
+    if (!edge_cell(eb, i, j, k)) return;
     const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
     const float *hx = p.out[3], *hy = p.out[4], *hz = p.out[5];
     const Tab T0 = tab(p.ea[0]), T1 = tab(p.ea[1]), T2 = tab(p.ea[2]);
@@ -826,66 +828,66 @@ k_edge_e(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     const int sx = slab(p.ea[0], i, p.nx, true), sy = slab(p.ea[1], j, p.ny, true),
               sz = slab(p.ea[2], k, p.nz, true);
     {   // ex: y term added, z term subtracted
-        float v = p.in[0][c];
+        float v = __ldg(p.in[0] + c);
         if (jin && kin) {
-            const float n = curl4(hz[c + Y], hz[c], hy[c + 1], hy[c]);
-            const float f = curl4(hz[c + 2 * Y], hz[c - Y], hy[c + 2], hy[c - 1]);
-            const float cv = p.ce[0][c];
+            const float n = curl4(__ldg(hz + (c + Y)), __ldg(hz + (c)), __ldg(hy + (c + 1)), __ldg(hy + (c)));
+            const float f = curl4(__ldg(hz + (c + 2 * Y)), __ldg(hz + (c - Y)), __ldg(hy + (c + 2)), __ldg(hy + (c - 1)));
+            const float cv = __ldg(p.ce[0] + c);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
                 float ps = p.psi_e[3][q];
-                v = fadd(v, sterm(T1, sy, ps, d4e(hz[c - Y], hz[c], hz[c + Y], hz[c + 2 * Y]), p.dl, cv));
+                v = fadd(v, sterm(T1, sy, ps, d4e(__ldg(hz + (c - Y)), __ldg(hz + (c)), __ldg(hz + (c + Y)), __ldg(hz + (c + 2 * Y))), p.dl, cv));
                 p.psi_e[3][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
                 float ps = p.psi_e[4][q];
-                v = fsub(v, sterm(T2, sz, ps, d4e(hy[c - 1], hy[c], hy[c + 1], hy[c + 2]), p.dl, cv));
+                v = fsub(v, sterm(T2, sz, ps, d4e(__ldg(hy + (c - 1)), __ldg(hy + (c)), __ldg(hy + (c + 1)), __ldg(hy + (c + 2))), p.dl, cv));
                 p.psi_e[4][q] = ps;
             }
         }
         p.out[0][c] = v;
     }
     {   // ey: x term subtracted, z term added
-        float v = p.in[1][c];
+        float v = __ldg(p.in[1] + c);
         if (iin && kin) {
-            const float n = curl4(hx[c + 1], hx[c], hz[c + X], hz[c]);
-            const float f = curl4(hx[c + 2], hx[c - 1], hz[c + 2 * X], hz[c - X]);
-            const float cv = p.ce[1][c];
+            const float n = curl4(__ldg(hx + (c + 1)), __ldg(hx + (c)), __ldg(hz + (c + X)), __ldg(hz + (c)));
+            const float f = curl4(__ldg(hx + (c + 2)), __ldg(hx + (c - 1)), __ldg(hz + (c + 2 * X)), __ldg(hz + (c - X)));
+            const float cv = __ldg(p.ce[1] + c);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
                 float ps = p.psi_e[0][q];
-                v = fsub(v, sterm(T0, sx, ps, d4e(hz[c - X], hz[c], hz[c + X], hz[c + 2 * X]), p.dl, cv));
+                v = fsub(v, sterm(T0, sx, ps, d4e(__ldg(hz + (c - X)), __ldg(hz + (c)), __ldg(hz + (c + X)), __ldg(hz + (c + 2 * X))), p.dl, cv));
                 p.psi_e[0][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
                 float ps = p.psi_e[5][q];
-                v = fadd(v, sterm(T2, sz, ps, d4e(hx[c - 1], hx[c], hx[c + 1], hx[c + 2]), p.dl, cv));
+                v = fadd(v, sterm(T2, sz, ps, d4e(__ldg(hx + (c - 1)), __ldg(hx + (c)), __ldg(hx + (c + 1)), __ldg(hx + (c + 2))), p.dl, cv));
                 p.psi_e[5][q] = ps;
             }
         }
         p.out[1][c] = v;
     }
     {   // ez: x term added, y term subtracted
-        float v = p.in[2][c];
+        float v = __ldg(p.in[2] + c);
         if (iin && jin) {
-            const float n = curl4(hy[c + X], hy[c], hx[c + Y], hx[c]);
-            const float f = curl4(hy[c + 2 * X], hy[c - X], hx[c + 2 * Y], hx[c - Y]);
-            const float cv = p.ce[2][c];
+            const float n = curl4(__ldg(hy + (c + X)), __ldg(hy + (c)), __ldg(hx + (c + Y)), __ldg(hx + (c)));
+            const float f = curl4(__ldg(hy + (c + 2 * X)), __ldg(hy + (c - X)), __ldg(hx + (c + 2 * Y)), __ldg(hx + (c - Y)));
+            const float cv = __ldg(p.ce[2] + c);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
                 float ps = p.psi_e[1][q];
-                v = fadd(v, sterm(T0, sx, ps, d4e(hy[c - X], hy[c], hy[c + X], hy[c + 2 * X]), p.dl, cv));
+                v = fadd(v, sterm(T0, sx, ps, d4e(__ldg(hy + (c - X)), __ldg(hy + (c)), __ldg(hy + (c + X)), __ldg(hy + (c + 2 * X))), p.dl, cv));
                 p.psi_e[1][q] = ps;
             }
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
                 float ps = p.psi_e[2][q];
-                v = fsub(v, sterm(T1, sy, ps, d4e(hx[c - Y], hx[c], hx[c + Y], hx[c + 2 * Y]), p.dl, cv));
+                v = fsub(v, sterm(T1, sy, ps, d4e(__ldg(hx + (c - Y)), __ldg(hx + (c)), __ldg(hx + (c + Y)), __ldg(hx + (c + 2 * Y))), p.dl, cv));
                 p.psi_e[2][q] = ps;
             }
         }
@@ -1088,7 +1090,7 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
     // the pair kernel's region: E_new of rows [j_lo, j_hi) needs H_new of rows
     // j_lo-1 .. j_hi+1, which must hold no y-slab node of any stage (front
     // nodes 1 .. P, back nodes n-P-1 .. n-1): j_lo = P+2, j_hi = n-P-2; the
-    // same along z, with k_lo rounded up to 4 cells (16-byte TMA boxes)
+    // same along z
     auto pf = [&](int ax) {
         int v = 0;
         for (const Axis *A : {&p.ha[ax], &p.hb[ax], &p.ea[ax]}) v = std::max(v, A->front ? A->P : 0);
@@ -1102,8 +1104,10 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
     const int64_t ny = pl->g.ny, nz = pl->g.nz;
     p.j_lo = pf(1) > 0 ? pf(1) + 2 : 0;
     p.j_hi = (int32_t)(pb(1) > 0 ? ny - pb(1) - 2 : ny);
-    p.k_lo = pf(2) > 0 ? (pf(2) + 2 + 3) / 4 * 4 : 0;
-    p.k_hi = (int32_t)(pb(2) > 0 ? nz - pb(2) - 2 : nz);
+    // z edge boxes of whole 64-byte row segments: k_lo rounded up and k_hi
+    // rounded down to 16 cells
+    p.k_lo = pf(2) > 0 ? (pf(2) + 2 + 15) / 16 * 16 : 0;
+    p.k_hi = (int32_t)(pb(2) > 0 ? (nz - pb(2) - 2) / 16 * 16 : nz);
     p.nty_in = p.j_hi > p.j_lo ? (p.j_hi - p.j_lo + TY - 1) / TY : 0;
     // z tiles stay on TZ-column boundaries (128-byte rows for the boxes and the
     // stores): they start at k_lo rounded down and mask the columns outside
@@ -1116,7 +1120,7 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
     auto add_box = [&](int64_t j0, int64_t j1, int64_t k0, int64_t k1) {
         if (j1 <= j0 || k1 <= k0) return;
         eb.j0[eb.n] = (int)j0; eb.j1[eb.n] = (int)j1; eb.k0[eb.n] = (int)k0; eb.k1[eb.n] = (int)k1;
-        eb.off[eb.n + 1] = eb.off[eb.n] + pl->g.nx * (j1 - j0) * (k1 - k0);
+        eb.off[eb.n + 1] = eb.off[eb.n] + (uint32_t)((j1 - j0) * (k1 - k0));
         eb.n++;
     };
     if (p.nty_in == 0 || p.ntz_in == 0) {
@@ -1147,9 +1151,9 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
         else
             k_symp_pair<false><<<nb, THREADS, SMEM, st>>>(pl->maps[in], p);
     }
-    const int64_t ecells = eb.off[eb.n];
+    const int64_t ecells = eb.off[eb.n];  // per x plane
     if (ecells > 0) {
-        const unsigned nb = (unsigned)((ecells + EDGE_BLOCK - 1) / EDGE_BLOCK);
+        const dim3 nb((unsigned)((ecells + EDGE_BLOCK - 1) / EDGE_BLOCK), (unsigned)pl->g.nx);
         k_edge_h<false><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
         if (two_h) k_edge_h<true><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
         k_edge_e<<<nb, EDGE_BLOCK, 0, st>>>(p, eb);

@@ -184,15 +184,16 @@ class SymplecticSolver:
     (uniform, default S/24) or three arrays; sources: (component, (i, j, k),
     amplitude) with amplitude a callable of continuous time t (FP64), added
     after every E stage at t = tn + sn/5 (PyCUDA/100-base.py:136).
-    fused: take the stage-pair kernel (one pass per H + E stage pair) where
-    pair_path() allows; it is bit-identical to the per-stage kernels but
-    currently slower than them on the 512^3 workload, so the default is the
-    one-launch-per-stage path; x_chunk: x planes per work item of the pair
-    kernel (0: 128).
+    fused: take the stage-pair path (one pass per H + E stage pair: the pair
+    kernel inside, the edge kernels on the y/z CPML shell) where pair_path()
+    allows; bit-identical to the per-stage kernels and faster than them
+    (9.2 against 12.3 ms per step on the 512^3 workload); fused=False keeps
+    the one-launch-per-stage path.  x_chunk: x planes per work item of the
+    pair kernel (0: 128).
     """
 
     def __init__(self, shape, ce=None, ch=None, npml=0, faces=0x3F, sources=(), device="cuda",
-                 S=COURANT, cpml_params=None, max_steps=0, fused=False, x_chunk=0):
+                 S=COURANT, cpml_params=None, max_steps=0, fused=True, x_chunk=0):
         self.shape = tuple(int(v) for v in shape)
         self.device = torch.device(device)
         dev = self.device

@@ -517,11 +517,10 @@ def run_symp512(args):
     # of 60 B/cell) or the stage-by-stage one (372 B/cell)
     alg_run = alg_pair if pair else alg
     achieved = alg_run / (avg / 1e3) / 1e9
-    # launches: per pass the pair kernel, the edge H and E kernels (a second
-    # edge H kernel in the n-1 passes that merge two H stages), and the run's
-    # last H stage; or per step 5 H and 4 E stage launches and a source launch
-    # after each E stage
-    launches = 4 * args.steps * 3 + (args.steps - 1) + 1 if pair else args.steps * (5 + 4 * 2)
+    # launches: per pass the pair kernel and the shell's H and E kernels, and
+    # the run's last H stage; or per step 5 H and 4 E stage launches and a
+    # source launch after each E stage
+    launches = 4 * args.steps * 3 + 1 if pair else args.steps * (5 + 4 * 2)
     accuracy = None
     if args.accuracy_steps:
         from fdtd_accelerate_gb300.fp64 import SympRun64, family_errors

@@ -2,12 +2,15 @@
 
 The library is loaded from this package directory.  There is no CPU
 fallback: if the library is missing or CUDA is unavailable, the calls raise.
+With FDTD_GB300_CHECKED=1 in the environment the bounds-checked debug build
+(libfdtd_gb300_check.so, buildlib.build(check=True)) is loaded instead.
 """
 import ctypes as C
 import os
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libfdtd_gb300.so")
+CHECKED = os.environ.get("FDTD_GB300_CHECKED", "") == "1"
+LIB_PATH = os.path.join(PKG, "libfdtd_gb300_check.so" if CHECKED else "libfdtd_gb300.so")
 
 FDTD_OK = 0
 FDTD_ERR_ARG = 1
@@ -115,6 +118,7 @@ _SIGS = {
     "fdtd_yee_plan_current": (C.c_int, [P]),
     "fdtd_yee_plan_set_current": (C.c_int, [P, I32]),
     "fdtd_yee_plan_test_timeout": (C.c_int, [P, I64, I32]),
+    "fdtd_debug_check": (C.c_int, [C.POINTER(C.c_uint64)]),
     "fdtd_yee_plan_info": (C.c_int, [P, P, I32]),
     "fdtd_yee_plan_destroy": (C.c_int, [P]),
     "fdtd_yee_step_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(YeeState), C.POINTER(Cpml), C.POINTER(Sources), P,

@@ -6,7 +6,9 @@ multiply-add contraction anywhere: every kernel reproduces the separately
 rounded products and sums of the reference's FP32 arithmetic); the objects are
 linked into fdtd_accelerate_gb300/libfdtd_gb300.so next to this file.
 Object files live in fdtd_accelerate_gb300/_build/.  A unit is rebuilt
-when it or any header is newer than its object.
+when it or any header is newer than its object.  build(check=True) makes the
+bounds-checked debug build (-DFDTD_CHECK) as libfdtd_gb300_check.so, objects
+in _build_check/.
 """
 import glob
 import os
@@ -46,14 +48,18 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, extra_flags=(), check=False):
+    build_dir = BUILD + "_check" if check else BUILD
+    lib = LIB[:-3] + "_check.so" if check else LIB
+    if check:
+        extra_flags = tuple(extra_flags) + ("-DFDTD_CHECK",)
+    os.makedirs(build_dir, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdrs = _headers()
     jobs = []
     objs = []
     for src in srcs:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj])
@@ -70,12 +76,12 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    if force or jobs or _stale(lib, objs):
+        tmp = lib + ".tmp"
         run([nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-ldl", "-o", tmp])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, check="--check" in sys.argv))

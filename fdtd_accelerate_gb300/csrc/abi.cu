@@ -1,9 +1,22 @@
-// Status strings and the per-thread record of the last CUDA error.
+// Status strings, the per-thread record of the last CUDA error, and the
+// check words of the bounds-checked debug build.
+#include <vector>
+
 #include "common.cuh"
 
 namespace fdtd {
 static thread_local int g_last_cuda_error = 0;
 void set_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
+#ifdef FDTD_CHECK
+static std::vector<int (*)(unsigned long long *)> &check_readers() {
+    static std::vector<int (*)(unsigned long long *)> v;
+    return v;
+}
+int check_register(int (*read)(unsigned long long *)) {
+    check_readers().push_back(read);
+    return 0;
+}
+#endif
 }  // namespace fdtd
 
 extern "C" {
@@ -23,5 +36,20 @@ const char *fdtd_status_string(int status) {
 }
 
 int fdtd_last_cuda_error(void) { return fdtd::g_last_cuda_error; }
+
+int fdtd_debug_check(uint64_t *first_bad) {
+    if (!first_bad) return FDTD_ERR_ARG;
+    *first_bad = 0;
+#ifdef FDTD_CHECK
+    for (auto read : fdtd::check_readers()) {
+        unsigned long long v = 0;
+        FDTD_TRY(read(&v));
+        if (v && !*first_bad) *first_bad = v;
+    }
+    return FDTD_OK;
+#else
+    return FDTD_ERR_UNSUPPORTED;
+#endif
+}
 
 }  // extern "C"

@@ -8,6 +8,37 @@
 
 namespace fdtd {
 
+// Bounds-checked debug build (-DFDTD_CHECK, libfdtd_gb300_check.so): every
+// global access wrapped in FDTD_IN compares its element index with the extent
+// of its array.  A miss records (1 << 63 | source line << 40 | index) in the
+// translation unit's check word, the first one only, and the access is skipped
+// instead of faulting; fdtd_debug_check() reads and clears the words of every
+// unit.  In the product build FDTD_IN is the constant true.
+#ifdef FDTD_CHECK
+static __device__ unsigned long long g_check_word;
+__device__ __forceinline__ bool check_index(long long i, long long n, int line) {
+    if (i >= 0 && i < n) return true;
+    atomicCAS(&g_check_word, 0ull,
+              (1ull << 63) | ((unsigned long long)(line & 0x7FFFFF) << 40) | ((unsigned long long)i & 0xFFFFFFFFFFull));
+    return false;
+}
+#define FDTD_IN(i, n) ::fdtd::check_index((long long)(i), (long long)(n), __LINE__)
+int check_register(int (*read)(unsigned long long *));  // abi.cu
+static int check_read_unit(unsigned long long *w) {
+    unsigned long long v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_check_word, sizeof(v));
+    if (e == cudaSuccess && v) {
+        const unsigned long long z = 0;
+        e = cudaMemcpyToSymbol(g_check_word, &z, sizeof(z));
+    }
+    *w = v;
+    return e == cudaSuccess ? FDTD_OK : FDTD_ERR_CUDA;
+}
+static const int g_check_registered = check_register(check_read_unit);
+#else
+#define FDTD_IN(i, n) true
+#endif
+
 // NVTX range around one step (or stage) of an entry point, for Nsight
 // Systems timelines and `ncu --nvtx` filters.  Header-only NVTX v3: without
 // an attached tool a push/pop pair is a call through a no-op pointer.

@@ -204,6 +204,15 @@ __device__ __forceinline__ float d4e(float fm1, float f0, float fp1, float fp2) 
     return fsub(fmul(27.0f, fsub(fp1, f0)), fsub(fp2, fm1));
 }
 
+// extents (elements) of a field array and of a psi slab array along axis ax
+// with P cells per face, for the bounds-checked build
+__device__ __forceinline__ int64_t fext(const Params &p) { return (int64_t)p.nx * p.sx; }
+__device__ __forceinline__ int64_t pext(const Params &p, int ax, int P) {
+    return ax == 0 ? 2LL * P * p.ny * p.nz : (ax == 1 ? 2LL * p.nx * P * p.nz : 2LL * p.nx * p.ny * P);
+}
+// a read-only global load through the non-coherent path, checked in the debug build
+#define LDG(a, i, n) (FDTD_IN(i, n) ? __ldg((a) + (i)) : 0.f)
+
 // four consecutive floats of shared memory (16-byte aligned)
 struct V4 {
     float v[4];
@@ -224,15 +233,16 @@ struct ZW {
     }
 };
 
-// global store of a group's 4 values (cells k .. k+3 of a row): the cells
-// whose bit is set in mask (all four: one 16-byte store)
-__device__ __forceinline__ void stg4(float *row, int k, uint32_t mask, const V4 &a) {
+// global store of a group's 4 values (elements g .. g+3 of a field array of
+// n elements): the cells whose bit is set in mask (all four: one 16-byte store)
+__device__ __forceinline__ void stg4(float *f, int64_t g, uint32_t mask, const V4 &a, int64_t n) {
     if (mask == 0xFu) {
-        *reinterpret_cast<float4 *>(row + k) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
+        if (FDTD_IN(g + 3, n) && FDTD_IN(g, n))
+            *reinterpret_cast<float4 *>(f + g) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);
     } else {
 #pragma unroll
         for (int c = 0; c < 4; c++)
-            if ((mask >> c) & 1) row[k + c] = a.v[c];
+            if (((mask >> c) & 1) && FDTD_IN(g + c, n)) f[g + c] = a.v[c];
     }
 }
 
@@ -456,8 +466,8 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 if (sxh >= 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        py[c] = (uy >> c) & 1 ? __ldg(p.psi_h_in[0] + offx + c) : 0.f;
-                        pz[c] = (uz >> c) & 1 ? __ldg(p.psi_h_in[1] + offx + c) : 0.f;
+                        py[c] = (uy >> c) & 1 ? LDG(p.psi_h_in[0], offx + c, pext(p, 0, p.ha[0].P)) : 0.f;
+                        pz[c] = (uz >> c) & 1 ? LDG(p.psi_h_in[1], offx + c, pext(p, 0, p.ha[0].P)) : 0.f;
                     }
                 }
                 if (sxh < 0) {
@@ -538,8 +548,10 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 if (own && sxh >= 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        if ((uy & kown) >> c & 1) p.psi_h_out[0][offx + c] = py[c];
-                        if ((uz & kown) >> c & 1) p.psi_h_out[1][offx + c] = pz[c];
+                        if (((uy & kown) >> c & 1) && FDTD_IN(offx + c, pext(p, 0, p.ha[0].P)))
+                            p.psi_h_out[0][offx + c] = py[c];
+                        if (((uz & kown) >> c & 1) && FDTD_IN(offx + c, pext(p, 0, p.ha[0].P)))
+                            p.psi_h_out[1][offx + c] = pz[c];
                     }
                 }
                 const int nsl = (m - (x0 - 1)) % NHN;
@@ -550,9 +562,9 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 hnz = vz;
                 if (own) {
                     const uint32_t rowo = (uint32_t)m * p.sx + (uint32_t)j * p.sy;
-                    stg4(p.out[3] + rowo, kg, kown, vx);
-                    stg4(p.out[4] + rowo, kg, kown, vy);
-                    stg4(p.out[5] + rowo, kg, kown, vz);
+                    stg4(p.out[3], (int64_t)rowo + kg, kown, vx, fext(p));
+                    stg4(p.out[4], (int64_t)rowo + kg, kown, vy, fext(p));
+                    stg4(p.out[5], (int64_t)rowo + kg, kown, vz, fext(p));
                 }
             }
 
@@ -582,8 +594,8 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 if (sxe >= 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        py[c] = (uy >> c) & 1 ? p.psi_e[0][offx + c] : 0.f;
-                        pz[c] = (uz >> c) & 1 ? p.psi_e[1][offx + c] : 0.f;
+                        py[c] = ((uy >> c) & 1) && FDTD_IN(offx + c, pext(p, 0, p.ea[0].P)) ? p.psi_e[0][offx + c] : 0.f;
+                        pz[c] = ((uz >> c) & 1) && FDTD_IN(offx + c, pext(p, 0, p.ea[0].P)) ? p.psi_e[1][offx + c] : 0.f;
                     }
                 }
                 if (sxe < 0) {
@@ -642,8 +654,8 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                 if (sxe >= 0) {
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        if ((uy >> c) & 1) p.psi_e[0][offx + c] = py[c];
-                        if ((uz >> c) & 1) p.psi_e[1][offx + c] = pz[c];
+                        if (((uy >> c) & 1) && FDTD_IN(offx + c, pext(p, 0, p.ea[0].P))) p.psi_e[0][offx + c] = py[c];
+                        if (((uz >> c) & 1) && FDTD_IN(offx + c, pext(p, 0, p.ea[0].P))) p.psi_e[1][offx + c] = pz[c];
                     }
                 }
                 for (int s = 0; s < nls; s++) {  // soft sources, list order
@@ -660,9 +672,9 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
                     }
                 }
                 const uint32_t rowo = (uint32_t)i * p.sx + (uint32_t)j * p.sy;
-                stg4(p.out[0] + rowo, kg, kown, vx);
-                stg4(p.out[1] + rowo, kg, kown, vy);
-                stg4(p.out[2] + rowo, kg, kown, vz);
+                stg4(p.out[0], (int64_t)rowo + kg, kown, vx, fext(p));
+                stg4(p.out[1], (int64_t)rowo + kg, kown, vy, fext(p));
+                stg4(p.out[2], (int64_t)rowo + kg, kown, vz, fext(p));
             }
             // advance the queue
             e0x = e1x; e0y = e1y; e0z = e1z;
@@ -705,10 +717,9 @@ k_symp_pair(const __grid_constant__ Maps mk, const __grid_constant__ Params p) {
 // ---------------------------------------------------------------------------
 // Edge shell: the cells outside the pair kernel's tiles (the y and z CPML
 // slabs and a tile of margin), one thread per cell, out of place:
-//   k_edge_h<false>  H_out = H_in - clch_a curl4(E_in) with its CPML terms
-//                    (psi_h_in -> psi_h_out);
-//   k_edge_h<true>   the second H stage of a two-H pass, in place on H_out
-//                    (psi_h_out in place);
+//   k_edge_h         H_out = H_in - clch_a curl4(E_in) with its CPML terms
+//                    (psi_h_in -> psi_h_out); in a two-H pass the second
+//                    stage follows in registers (same E_in, psi carried);
 //   k_edge_e         E_out = E_in + dl ce curl4(H_out) with its CPML terms
 //                    (psi_e in place), once the pair kernel has written the
 //                    interior H_out;
@@ -739,81 +750,89 @@ __device__ __forceinline__ bool edge_cell(const Edge &eb, int &i, int &j, int &k
     return true;
 }
 
-template <bool B>
+template <bool HH>
 __global__ void __launch_bounds__(EDGE_BLOCK)
 k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     int i, j, k;
     if (!edge_cell(eb, i, j, k)) return;
     const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
     const float *ex = p.in[0], *ey = p.in[1], *ez = p.in[2];
-    const float *const *pin = B ? const_cast<const float *const *>(p.psi_h_out) : p.psi_h_in;
-    const float clch = B ? p.clch_b : p.clch_a, cl = B ? p.cl_b : p.cl_a;
-    const Tab T0 = tab_h(p, B, 0), T1 = tab_h(p, B, 1), T2 = tab_h(p, B, 2);
+    [[maybe_unused]] const int64_t FE = fext(p);
+    [[maybe_unused]] const int64_t PE0 = pext(p, 0, p.ha[0].P), PE1 = PE0, PE2 = pext(p, 1, p.ha[1].P),
+                                   PE3 = PE2, PE4 = pext(p, 2, p.ha[2].P), PE5 = PE4;
     const bool jin = j > 1 && j < p.ny - 1, kin = k > 1 && k < p.nz - 1, iin = i > 1 && i < p.nx - 1;
     const int sx = slab(p.ha[0], i, p.nx, false), sy = slab(p.ha[1], j, p.ny, false),
               sz = slab(p.ha[2], k, p.nz, false);
-    {   // hx: y term subtracted, z term added
-        float v = B ? p.out[3][c] : __ldg(p.in[3] + c);
-        if (jin && kin) {
-            const float n = curl4(__ldg(ez + (c)), __ldg(ez + (c - Y)), __ldg(ey + (c)), __ldg(ey + (c - 1)));
-            const float f = curl4(__ldg(ez + (c + Y)), __ldg(ez + (c - 2 * Y)), __ldg(ey + (c + 1)), __ldg(ey + (c - 2)));
-            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
-            if (sy >= 0) {
-                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
-                float ps = pin[3][q];
-                v = fsub(v, sterm(T1, sy, ps, d4h(__ldg(ez + (c - 2 * Y)), __ldg(ez + (c - Y)), __ldg(ez + (c)), __ldg(ez + (c + Y))), cl, p.ch));
-                p.psi_h_out[3][q] = ps;
+    // One component: the input H, then per stage (a, then b in a two-H pass)
+    // the main term and the two CPML terms (signs s1, s2: +1 adds), psi
+    // carried from stage a to stage b in registers; E_in is the same for both
+    // stages, so are d27 and the one-axis differences.
+    auto comp = [&](int q, bool upd, float d27, int a1, int s1, int q1, float d1, int a2, int s2, int q2, float d2) {
+        float v = LDG(p.in[3 + q], c, FE);
+        if (upd) {
+            const int sl1 = a1 == 0 ? sx : (a1 == 1 ? sy : sz), sl2 = a2 == 0 ? sx : (a2 == 1 ? sy : sz);
+            [[maybe_unused]] const int64_t pe1 = a1 == 0 ? PE0 : (a1 == 1 ? PE2 : PE4),
+                                           pe2 = a2 == 0 ? PE0 : (a2 == 1 ? PE2 : PE4);
+            uint32_t i1 = 0, i2 = 0;
+            float ps1 = 0.f, ps2 = 0.f;
+            if (sl1 >= 0) {
+                i1 = psi_index(p, a1, sl1, i, j, k, p.ha[a1].P);
+                ps1 = FDTD_IN(i1, pe1) ? p.psi_h_in[q1][i1] : 0.f;
             }
-            if (sz >= 0) {
-                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
-                float ps = pin[4][q];
-                v = fadd(v, sterm(T2, sz, ps, d4h(__ldg(ey + (c - 2)), __ldg(ey + (c - 1)), __ldg(ey + (c)), __ldg(ey + (c + 1))), cl, p.ch));
-                p.psi_h_out[4][q] = ps;
+            if (sl2 >= 0) {
+                i2 = psi_index(p, a2, sl2, i, j, k, p.ha[a2].P);
+                ps2 = FDTD_IN(i2, pe2) ? p.psi_h_in[q2][i2] : 0.f;
             }
+#pragma unroll
+            for (int st = 0; st < (HH ? 2 : 1); st++) {
+                const float clch = st ? p.clch_b : p.clch_a, cl = st ? p.cl_b : p.cl_a;
+                v = fsub(v, fmul(clch, d27));
+                if (sl1 >= 0) {
+                    const float t = sterm(tab_h(p, st, a1), sl1, ps1, d1, cl, p.ch);
+                    v = s1 > 0 ? fadd(v, t) : fsub(v, t);
+                }
+                if (sl2 >= 0) {
+                    const float t = sterm(tab_h(p, st, a2), sl2, ps2, d2, cl, p.ch);
+                    v = s2 > 0 ? fadd(v, t) : fsub(v, t);
+                }
+            }
+            if (sl1 >= 0 && FDTD_IN(i1, pe1)) p.psi_h_out[q1][i1] = ps1;
+            if (sl2 >= 0 && FDTD_IN(i2, pe2)) p.psi_h_out[q2][i2] = ps2;
         }
-        p.out[3][c] = v;
+        if (FDTD_IN(c, FE)) p.out[3 + q][c] = v;
+    };
+    {   // hx: y term subtracted, z term added
+        float d27 = 0.f, dy = 0.f, dz = 0.f;
+        if (jin && kin) {
+            const float n = curl4(LDG(ez, c, FE), LDG(ez, c - Y, FE), LDG(ey, c, FE), LDG(ey, c - 1, FE));
+            const float f = curl4(LDG(ez, c + Y, FE), LDG(ez, c - 2 * Y, FE), LDG(ey, c + 1, FE), LDG(ey, c - 2, FE));
+            d27 = fsub(fmul(27.0f, n), f);
+            if (sy >= 0) dy = d4h(LDG(ez, c - 2 * Y, FE), LDG(ez, c - Y, FE), LDG(ez, c, FE), LDG(ez, c + Y, FE));
+            if (sz >= 0) dz = d4h(LDG(ey, c - 2, FE), LDG(ey, c - 1, FE), LDG(ey, c, FE), LDG(ey, c + 1, FE));
+        }
+        comp(0, jin && kin, d27, 1, -1, 3, dy, 2, +1, 4, dz);
     }
     {   // hy: x term added, z term subtracted
-        float v = B ? p.out[4][c] : __ldg(p.in[4] + c);
+        float d27 = 0.f, dx = 0.f, dz = 0.f;
         if (iin && kin) {
-            const float n = curl4(__ldg(ex + (c)), __ldg(ex + (c - 1)), __ldg(ez + (c)), __ldg(ez + (c - X)));
-            const float f = curl4(__ldg(ex + (c + 1)), __ldg(ex + (c - 2)), __ldg(ez + (c + X)), __ldg(ez + (c - 2 * X)));
-            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
-            if (sx >= 0) {
-                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
-                float ps = pin[0][q];
-                v = fadd(v, sterm(T0, sx, ps, d4h(__ldg(ez + (c - 2 * X)), __ldg(ez + (c - X)), __ldg(ez + (c)), __ldg(ez + (c + X))), cl, p.ch));
-                p.psi_h_out[0][q] = ps;
-            }
-            if (sz >= 0) {
-                const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ha[2].P);
-                float ps = pin[5][q];
-                v = fsub(v, sterm(T2, sz, ps, d4h(__ldg(ex + (c - 2)), __ldg(ex + (c - 1)), __ldg(ex + (c)), __ldg(ex + (c + 1))), cl, p.ch));
-                p.psi_h_out[5][q] = ps;
-            }
+            const float n = curl4(LDG(ex, c, FE), LDG(ex, c - 1, FE), LDG(ez, c, FE), LDG(ez, c - X, FE));
+            const float f = curl4(LDG(ex, c + 1, FE), LDG(ex, c - 2, FE), LDG(ez, c + X, FE), LDG(ez, c - 2 * X, FE));
+            d27 = fsub(fmul(27.0f, n), f);
+            if (sx >= 0) dx = d4h(LDG(ez, c - 2 * X, FE), LDG(ez, c - X, FE), LDG(ez, c, FE), LDG(ez, c + X, FE));
+            if (sz >= 0) dz = d4h(LDG(ex, c - 2, FE), LDG(ex, c - 1, FE), LDG(ex, c, FE), LDG(ex, c + 1, FE));
         }
-        p.out[4][c] = v;
+        comp(1, iin && kin, d27, 0, +1, 0, dx, 2, -1, 5, dz);
     }
     {   // hz: x term subtracted, y term added
-        float v = B ? p.out[5][c] : __ldg(p.in[5] + c);
+        float d27 = 0.f, dx = 0.f, dy = 0.f;
         if (iin && jin) {
-            const float n = curl4(__ldg(ey + (c)), __ldg(ey + (c - X)), __ldg(ex + (c)), __ldg(ex + (c - Y)));
-            const float f = curl4(__ldg(ey + (c + X)), __ldg(ey + (c - 2 * X)), __ldg(ex + (c + Y)), __ldg(ex + (c - 2 * Y)));
-            v = fsub(v, fmul(clch, fsub(fmul(27.0f, n), f)));
-            if (sx >= 0) {
-                const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ha[0].P);
-                float ps = pin[1][q];
-                v = fsub(v, sterm(T0, sx, ps, d4h(__ldg(ey + (c - 2 * X)), __ldg(ey + (c - X)), __ldg(ey + (c)), __ldg(ey + (c + X))), cl, p.ch));
-                p.psi_h_out[1][q] = ps;
-            }
-            if (sy >= 0) {
-                const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ha[1].P);
-                float ps = pin[2][q];
-                v = fadd(v, sterm(T1, sy, ps, d4h(__ldg(ex + (c - 2 * Y)), __ldg(ex + (c - Y)), __ldg(ex + (c)), __ldg(ex + (c + Y))), cl, p.ch));
-                p.psi_h_out[2][q] = ps;
-            }
+            const float n = curl4(LDG(ey, c, FE), LDG(ey, c - X, FE), LDG(ex, c, FE), LDG(ex, c - Y, FE));
+            const float f = curl4(LDG(ey, c + X, FE), LDG(ey, c - 2 * X, FE), LDG(ex, c + Y, FE), LDG(ex, c - 2 * Y, FE));
+            d27 = fsub(fmul(27.0f, n), f);
+            if (sx >= 0) dx = d4h(LDG(ey, c - 2 * X, FE), LDG(ey, c - X, FE), LDG(ey, c, FE), LDG(ey, c + X, FE));
+            if (sy >= 0) dy = d4h(LDG(ex, c - 2 * Y, FE), LDG(ex, c - Y, FE), LDG(ex, c, FE), LDG(ex, c + Y, FE));
         }
-        p.out[5][c] = v;
+        comp(2, iin && jin, d27, 0, -1, 1, dx, 1, +1, 2, dy);
     }
 }
 
@@ -823,75 +842,78 @@ k_edge_e(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     if (!edge_cell(eb, i, j, k)) return;
     const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
     const float *hx = p.out[3], *hy = p.out[4], *hz = p.out[5];
+    [[maybe_unused]] const int64_t FE = fext(p);
+    [[maybe_unused]] const int64_t PE0 = pext(p, 0, p.ea[0].P), PE1 = PE0, PE2 = pext(p, 1, p.ea[1].P),
+                                   PE3 = PE2, PE4 = pext(p, 2, p.ea[2].P), PE5 = PE4;
     const Tab T0 = tab(p.ea[0]), T1 = tab(p.ea[1]), T2 = tab(p.ea[2]);
     const bool jin = j > 0 && j < p.ny - 2, kin = k > 0 && k < p.nz - 2, iin = i > 0 && i < p.nx - 2;
     const int sx = slab(p.ea[0], i, p.nx, true), sy = slab(p.ea[1], j, p.ny, true),
               sz = slab(p.ea[2], k, p.nz, true);
     {   // ex: y term added, z term subtracted
-        float v = __ldg(p.in[0] + c);
+        float v = LDG(p.in[0], c, FE);
         if (jin && kin) {
-            const float n = curl4(__ldg(hz + (c + Y)), __ldg(hz + (c)), __ldg(hy + (c + 1)), __ldg(hy + (c)));
-            const float f = curl4(__ldg(hz + (c + 2 * Y)), __ldg(hz + (c - Y)), __ldg(hy + (c + 2)), __ldg(hy + (c - 1)));
-            const float cv = __ldg(p.ce[0] + c);
+            const float n = curl4(LDG(hz, c + Y, FE), LDG(hz, c, FE), LDG(hy, c + 1, FE), LDG(hy, c, FE));
+            const float f = curl4(LDG(hz, c + 2 * Y, FE), LDG(hz, c - Y, FE), LDG(hy, c + 2, FE), LDG(hy, c - 1, FE));
+            const float cv = LDG(p.ce[0], c, FE);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
-                float ps = p.psi_e[3][q];
-                v = fadd(v, sterm(T1, sy, ps, d4e(__ldg(hz + (c - Y)), __ldg(hz + (c)), __ldg(hz + (c + Y)), __ldg(hz + (c + 2 * Y))), p.dl, cv));
-                p.psi_e[3][q] = ps;
+                float ps = FDTD_IN(q, PE3) ? p.psi_e[3][q] : 0.f;
+                v = fadd(v, sterm(T1, sy, ps, d4e(LDG(hz, c - Y, FE), LDG(hz, c, FE), LDG(hz, c + Y, FE), LDG(hz, c + 2 * Y, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE3)) p.psi_e[3][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
-                float ps = p.psi_e[4][q];
-                v = fsub(v, sterm(T2, sz, ps, d4e(__ldg(hy + (c - 1)), __ldg(hy + (c)), __ldg(hy + (c + 1)), __ldg(hy + (c + 2))), p.dl, cv));
-                p.psi_e[4][q] = ps;
+                float ps = FDTD_IN(q, PE4) ? p.psi_e[4][q] : 0.f;
+                v = fsub(v, sterm(T2, sz, ps, d4e(LDG(hy, c - 1, FE), LDG(hy, c, FE), LDG(hy, c + 1, FE), LDG(hy, c + 2, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE4)) p.psi_e[4][q] = ps;
             }
         }
-        p.out[0][c] = v;
+        if (FDTD_IN(c, FE)) p.out[0][c] = v;
     }
     {   // ey: x term subtracted, z term added
-        float v = __ldg(p.in[1] + c);
+        float v = LDG(p.in[1], c, FE);
         if (iin && kin) {
-            const float n = curl4(__ldg(hx + (c + 1)), __ldg(hx + (c)), __ldg(hz + (c + X)), __ldg(hz + (c)));
-            const float f = curl4(__ldg(hx + (c + 2)), __ldg(hx + (c - 1)), __ldg(hz + (c + 2 * X)), __ldg(hz + (c - X)));
-            const float cv = __ldg(p.ce[1] + c);
+            const float n = curl4(LDG(hx, c + 1, FE), LDG(hx, c, FE), LDG(hz, c + X, FE), LDG(hz, c, FE));
+            const float f = curl4(LDG(hx, c + 2, FE), LDG(hx, c - 1, FE), LDG(hz, c + 2 * X, FE), LDG(hz, c - X, FE));
+            const float cv = LDG(p.ce[1], c, FE);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
-                float ps = p.psi_e[0][q];
-                v = fsub(v, sterm(T0, sx, ps, d4e(__ldg(hz + (c - X)), __ldg(hz + (c)), __ldg(hz + (c + X)), __ldg(hz + (c + 2 * X))), p.dl, cv));
-                p.psi_e[0][q] = ps;
+                float ps = FDTD_IN(q, PE0) ? p.psi_e[0][q] : 0.f;
+                v = fsub(v, sterm(T0, sx, ps, d4e(LDG(hz, c - X, FE), LDG(hz, c, FE), LDG(hz, c + X, FE), LDG(hz, c + 2 * X, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE0)) p.psi_e[0][q] = ps;
             }
             if (sz >= 0) {
                 const uint32_t q = psi_index(p, 2, sz, i, j, k, p.ea[2].P);
-                float ps = p.psi_e[5][q];
-                v = fadd(v, sterm(T2, sz, ps, d4e(__ldg(hx + (c - 1)), __ldg(hx + (c)), __ldg(hx + (c + 1)), __ldg(hx + (c + 2))), p.dl, cv));
-                p.psi_e[5][q] = ps;
+                float ps = FDTD_IN(q, PE5) ? p.psi_e[5][q] : 0.f;
+                v = fadd(v, sterm(T2, sz, ps, d4e(LDG(hx, c - 1, FE), LDG(hx, c, FE), LDG(hx, c + 1, FE), LDG(hx, c + 2, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE5)) p.psi_e[5][q] = ps;
             }
         }
-        p.out[1][c] = v;
+        if (FDTD_IN(c, FE)) p.out[1][c] = v;
     }
     {   // ez: x term added, y term subtracted
-        float v = __ldg(p.in[2] + c);
+        float v = LDG(p.in[2], c, FE);
         if (iin && jin) {
-            const float n = curl4(__ldg(hy + (c + X)), __ldg(hy + (c)), __ldg(hx + (c + Y)), __ldg(hx + (c)));
-            const float f = curl4(__ldg(hy + (c + 2 * X)), __ldg(hy + (c - X)), __ldg(hx + (c + 2 * Y)), __ldg(hx + (c - Y)));
-            const float cv = __ldg(p.ce[2] + c);
+            const float n = curl4(LDG(hy, c + X, FE), LDG(hy, c, FE), LDG(hx, c + Y, FE), LDG(hx, c, FE));
+            const float f = curl4(LDG(hy, c + 2 * X, FE), LDG(hy, c - X, FE), LDG(hx, c + 2 * Y, FE), LDG(hx, c - Y, FE));
+            const float cv = LDG(p.ce[2], c, FE);
             v = fadd(v, fmul(fmul(p.dl, cv), fsub(fmul(27.0f, n), f)));
             if (sx >= 0) {
                 const uint32_t q = psi_index(p, 0, sx, i, j, k, p.ea[0].P);
-                float ps = p.psi_e[1][q];
-                v = fadd(v, sterm(T0, sx, ps, d4e(__ldg(hy + (c - X)), __ldg(hy + (c)), __ldg(hy + (c + X)), __ldg(hy + (c + 2 * X))), p.dl, cv));
-                p.psi_e[1][q] = ps;
+                float ps = FDTD_IN(q, PE1) ? p.psi_e[1][q] : 0.f;
+                v = fadd(v, sterm(T0, sx, ps, d4e(LDG(hy, c - X, FE), LDG(hy, c, FE), LDG(hy, c + X, FE), LDG(hy, c + 2 * X, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE1)) p.psi_e[1][q] = ps;
             }
             if (sy >= 0) {
                 const uint32_t q = psi_index(p, 1, sy, i, j, k, p.ea[1].P);
-                float ps = p.psi_e[2][q];
-                v = fsub(v, sterm(T1, sy, ps, d4e(__ldg(hx + (c - Y)), __ldg(hx + (c)), __ldg(hx + (c + Y)), __ldg(hx + (c + 2 * Y))), p.dl, cv));
-                p.psi_e[2][q] = ps;
+                float ps = FDTD_IN(q, PE2) ? p.psi_e[2][q] : 0.f;
+                v = fsub(v, sterm(T1, sy, ps, d4e(LDG(hx, c - Y, FE), LDG(hx, c, FE), LDG(hx, c + Y, FE), LDG(hx, c + 2 * Y, FE)), p.dl, cv));
+                if (FDTD_IN(q, PE2)) p.psi_e[2][q] = ps;
             }
         }
-        p.out[2][c] = v;
+        if (FDTD_IN(c, FE)) p.out[2][c] = v;
     }
 }
 
@@ -906,7 +928,7 @@ __global__ void k_edge_src(const __grid_constant__ Params p, const __grid_consta
         if (!in) continue;
         float *f = p.out[p.src_comp[s]];
         const int64_t c = (int64_t)si * p.sx + (int64_t)sj * p.sy + sk;
-        f[c] = fadd(f[c], p.src_amp[(int64_t)s * p.namp + p.t]);
+        if (FDTD_IN(c, fext(p))) f[c] = fadd(f[c], p.src_amp[(int64_t)s * p.namp + p.t]);
     }
 }
 
@@ -1154,8 +1176,10 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
     const int64_t ecells = eb.off[eb.n];  // per x plane
     if (ecells > 0) {
         const dim3 nb((unsigned)((ecells + EDGE_BLOCK - 1) / EDGE_BLOCK), (unsigned)pl->g.nx);
-        k_edge_h<false><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
-        if (two_h) k_edge_h<true><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
+        if (two_h)
+            k_edge_h<true><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
+        else
+            k_edge_h<false><<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
         k_edge_e<<<nb, EDGE_BLOCK, 0, st>>>(p, eb);
         bool esrc = false;
         for (size_t a = 0; a + 2 < pl->src_ijk.size(); a += 3)

@@ -136,6 +136,15 @@ struct Params {
     int32_t test_withhold;
 };
 
+// extents (elements) of a field array and of psi array q (0, 1: x slab;
+// 2, 3: y slab; 4, 5: z slab), for the bounds-checked build
+__host__ __device__ __forceinline__ int64_t fext_y(const Params &p) { return p.nx * p.sx; }
+__host__ __device__ __forceinline__ int64_t pext_y(const Params &p, int q) {
+    const int ax = q / 2;
+    const int64_t P2 = 2 * (int64_t)p.P[ax];
+    return ax == 0 ? P2 * p.ny * p.nz : (ax == 1 ? p.nx * P2 * p.nz : p.nx * p.ny * P2);
+}
+
 // Many independent grids advanced by one launch: work items of all grids are
 // numbered consecutively; item_off[s] is the first item of grid s.
 struct BatchDesc {
@@ -770,15 +779,15 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
                             if (e ? k1_lt : k0_lt) {
-                                float psi = xm ? sP(psl, 0)[er * EC + 4 + eko + e] : p.psi_e_in[0][qb + e];
+                                float psi = xm ? sP(psl, 0)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 0)) ? p.psi_e_in[0][qb + e] : 0.f);
                                 const float tc = corr(psi, c, fsub(get(hz1, e), get(hz, e)));
-                                if (own) p.psi_e_out[0][qb + e] = psi;
+                                if (own) if (FDTD_IN(qb + e, pext_y(p, 0))) p.psi_e_out[0][qb + e] = psi;
                                 set(ey, e, fsub(get(ey, e), fmul(get(cey, e), tc)));
                             }
                             if (j_lt) {
-                                float psi = xm ? sP(psl, 1)[er * EC + 4 + eko + e] : p.psi_e_in[1][qb + e];
+                                float psi = xm ? sP(psl, 1)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 1)) ? p.psi_e_in[1][qb + e] : 0.f);
                                 const float tc = corr(psi, c, fsub(get(hy1, e), get(hy, e)));
-                                if (own) p.psi_e_out[1][qb + e] = psi;
+                                if (own) if (FDTD_IN(qb + e, pext_y(p, 1))) p.psi_e_out[1][qb + e] = psi;
                                 set(ez, e, fadd(get(ez, e), fmul(get(cez, e), tc)));
                             }
                         }
@@ -790,15 +799,15 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                         for (int e = 0; e < 2; e++) {
                             if (!(e ? in1 : in0)) continue;
                             if (i_lt) {
-                                float psi = ym ? sP(psl, 0)[er * EC + 4 + eko + e] : p.psi_e_in[2][qb + e];
+                                float psi = ym ? sP(psl, 0)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 2)) ? p.psi_e_in[2][qb + e] : 0.f);
                                 const float tc = corr(psi, cye, fsub(get(hxj1, e), get(hx, e)));
-                                if (own) p.psi_e_out[2][qb + e] = psi;
+                                if (own) if (FDTD_IN(qb + e, pext_y(p, 2))) p.psi_e_out[2][qb + e] = psi;
                                 set(ez, e, fsub(get(ez, e), fmul(get(cez, e), tc)));
                             }
                             if (e ? k1_lt : k0_lt) {
-                                float psi = ym ? sP(psl, 1)[er * EC + 4 + eko + e] : p.psi_e_in[3][qb + e];
+                                float psi = ym ? sP(psl, 1)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 3)) ? p.psi_e_in[3][qb + e] : 0.f);
                                 const float tc = corr(psi, cye, fsub(get(hzj1, e), get(hz, e)));
-                                if (own) p.psi_e_out[3][qb + e] = psi;
+                                if (own) if (FDTD_IN(qb + e, pext_y(p, 3))) p.psi_e_out[3][qb + e] = psi;
                                 set(ex, e, fadd(get(ex, e), fmul(get(cex, e), tc)));
                             }
                         }
@@ -861,15 +870,15 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (e ? k1_gt : k0_gt) {
-                                    float psi = xm ? sP(psl, 2)[er * EC + 4 + eko + e] : p.psi_h[0][qb + e];
+                                    float psi = xm ? sP(psl, 2)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 0)) ? p.psi_h[0][qb + e] : 0.f);
                                     const float tc = corr(psi, c, fsub(get(oez, e), get(prev_ez, e)));
-                                    p.psi_h[0][qb + e] = psi;
+                                    if (FDTD_IN(qb + e, pext_y(p, 0))) p.psi_h[0][qb + e] = psi;
                                     set(hy, e, fadd(get(hy, e), fmul(0.5f, tc)));
                                 }
                                 if (j_gt) {
-                                    float psi = xm ? sP(psl, 3)[er * EC + 4 + eko + e] : p.psi_h[1][qb + e];
+                                    float psi = xm ? sP(psl, 3)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 1)) ? p.psi_h[1][qb + e] : 0.f);
                                     const float tc = corr(psi, c, fsub(get(oey, e), get(prev_ey, e)));
-                                    p.psi_h[1][qb + e] = psi;
+                                    if (FDTD_IN(qb + e, pext_y(p, 1))) p.psi_h[1][qb + e] = psi;
                                     set(hz, e, fsub(get(hz, e), fmul(0.5f, tc)));
                                 }
                             }
@@ -881,15 +890,15 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                             for (int e = 0; e < 2; e++) {
                                 if (!(e ? in1 : in0) || (e ? hb1 : hb0)) continue;
                                 if (i_gt) {
-                                    float psi = ym ? sP(psl, 2)[er * EC + 4 + eko + e] : p.psi_h[2][qb + e];
+                                    float psi = ym ? sP(psl, 2)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 2)) ? p.psi_h[2][qb + e] : 0.f);
                                     const float tc = corr(psi, cyh, fsub(get(oex, e), get(ex_jm, e)));
-                                    p.psi_h[2][qb + e] = psi;
+                                    if (FDTD_IN(qb + e, pext_y(p, 2))) p.psi_h[2][qb + e] = psi;
                                     set(hz, e, fadd(get(hz, e), fmul(0.5f, tc)));
                                 }
                                 if (e ? k1_gt : k0_gt) {
-                                    float psi = ym ? sP(psl, 3)[er * EC + 4 + eko + e] : p.psi_h[3][qb + e];
+                                    float psi = ym ? sP(psl, 3)[er * EC + 4 + eko + e] : (FDTD_IN(qb + e, pext_y(p, 3)) ? p.psi_h[3][qb + e] : 0.f);
                                     const float tc = corr(psi, cyh, fsub(get(oez, e), get(ez_jm, e)));
-                                    p.psi_h[3][qb + e] = psi;
+                                    if (FDTD_IN(qb + e, pext_y(p, 3))) p.psi_h[3][qb + e] = psi;
                                     set(hx, e, fsub(get(hx, e), fmul(0.5f, tc)));
                                 }
                             }
@@ -901,19 +910,19 @@ k_yee_fused(const __grid_constant__ TMaps mk, const __grid_constant__ Params pk,
                     }
                     const int64_t gi = i * p.sx + jj * p.sy + kk;
                     if (in1) {
-                        st2(p.out[0] + gi, oex);
-                        st2(p.out[1] + gi, oey);
-                        st2(p.out[2] + gi, oez);
-                        st2(p.out[3] + gi, hx);
-                        st2(p.out[4] + gi, hy);
-                        st2(p.out[5] + gi, hz);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[0] + gi, oex);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[1] + gi, oey);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[2] + gi, oez);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[3] + gi, hx);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[4] + gi, hy);
+                        if (FDTD_IN(gi + 1, fext_y(p))) st2(p.out[5] + gi, hz);
                     } else if (in0) {
-                        p.out[0][gi] = oex.x;
-                        p.out[1][gi] = oey.x;
-                        p.out[2][gi] = oez.x;
-                        p.out[3][gi] = hx.x;
-                        p.out[4][gi] = hy.x;
-                        p.out[5][gi] = hz.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[0][gi] = oex.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[1][gi] = oey.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[2][gi] = oez.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[3][gi] = hx.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[4][gi] = hy.x;
+                        if (FDTD_IN(gi, fext_y(p))) p.out[5][gi] = hz.x;
                     }
                 }
                 prev_ey = oey;
@@ -1016,26 +1025,26 @@ __device__ __forceinline__ void zband_e_at(const Params &p, int64_t tstep, int64
     const bool ux = j < p.ny - 1, uy = i < p.nx - 1;  // exz / eyz elements that exist
     float px = 0.f, py = 0.f, hyd = 0.f, hxd = 0.f, ex = 0.f, ey = 0.f, cx = 0.f, cy = 0.f;
     if (ux) {
-        px = p.psi_e_in[4][qz];
-        hyd = fsub(p.in[4][c + 1], p.in[4][c]);
-        ex = p.out[0][c];
-        cx = p.in_ce[0][c];
+        px = (FDTD_IN(qz, pext_y(p, 4)) ? p.psi_e_in[4][qz] : 0.f);
+        hyd = fsub((FDTD_IN(c + 1, fext_y(p)) ? p.in[4][c + 1] : 0.f), (FDTD_IN(c, fext_y(p)) ? p.in[4][c] : 0.f));
+        ex = (FDTD_IN(c, fext_y(p)) ? p.out[0][c] : 0.f);
+        cx = (FDTD_IN(c, fext_y(p)) ? p.in_ce[0][c] : 0.f);
     }
     if (uy) {
-        py = p.psi_e_in[5][qz];
-        hxd = fsub(p.in[3][c + 1], p.in[3][c]);
-        ey = p.out[1][c];
-        cy = p.in_ce[1][c];
+        py = (FDTD_IN(qz, pext_y(p, 5)) ? p.psi_e_in[5][qz] : 0.f);
+        hxd = fsub((FDTD_IN(c + 1, fext_y(p)) ? p.in[3][c + 1] : 0.f), (FDTD_IN(c, fext_y(p)) ? p.in[3][c] : 0.f));
+        ey = (FDTD_IN(c, fext_y(p)) ? p.out[1][c] : 0.f);
+        cy = (FDTD_IN(c, fext_y(p)) ? p.in_ce[1][c] : 0.f);
     }
     if (ux) {  // ex -= cex (..dHy/dz..)
         const float tc = corr(px, cf, hyd);
-        p.psi_e_out[4][qz] = px;
-        p.out[0][c] = fsub(ex, fmul(cx, tc));
+        if (FDTD_IN(qz, pext_y(p, 4))) p.psi_e_out[4][qz] = px;
+        if (FDTD_IN(c, fext_y(p))) p.out[0][c] = fsub(ex, fmul(cx, tc));
     }
     if (uy) {  // ey += cey (..dHx/dz..)
         const float tc = corr(py, cf, hxd);
-        p.psi_e_out[5][qz] = py;
-        p.out[1][c] = fadd(ey, fmul(cy, tc));
+        if (FDTD_IN(qz, pext_y(p, 5))) p.psi_e_out[5][qz] = py;
+        if (FDTD_IN(c, fext_y(p))) p.out[1][c] = fadd(ey, fmul(cy, tc));
     }
     if (tstep >= 0 && tstep < p.namp) {  // sources on this cell, list order
         const int n = p.nbsrc < 0 ? p.nsrc : p.nbsrc;
@@ -1043,7 +1052,7 @@ __device__ __forceinline__ void zband_e_at(const Params &p, int64_t tstep, int64
             const int s = p.nbsrc < 0 ? b : p.bsrc[b];
             if (p.src_ijk[3 * s] != i || p.src_ijk[3 * s + 1] != j || p.src_ijk[3 * s + 2] != k) continue;
             float *f = p.out[p.src_comp[s]] + c;
-            *f = fadd(*f, p.src_amp[(int64_t)s * p.namp + tstep]);
+            if (FDTD_IN(c, fext_y(p))) *f = fadd(*f, p.src_amp[(int64_t)s * p.namp + tstep]);
         }
     }
 }
@@ -1080,26 +1089,26 @@ __device__ __forceinline__ void zband_h_at(const Params &p, int64_t i, int64_t j
     const float *__restrict__ ex = p.out[0];
     const float *__restrict__ ey = p.out[1];
     const float *__restrict__ ez = p.out[2];
-    const float hx0 = p.in[3][c], hy0 = p.in[4][c], hz0 = p.in[5][c];
-    const float ex_c = ex[c], ey_c = ey[c], ez_c = ez[c];
-    const float ez_j = j > 0 ? ez[c - p.sy] : 0.f, ex_j = j > 0 ? ex[c - p.sy] : 0.f;
-    const float ey_i = i > 0 ? ey[c - p.sx] : 0.f, ez_i = i > 0 ? ez[c - p.sx] : 0.f;
-    const float ey_k = ey[c - 1], ex_k = ex[c - 1];  // k >= 1 in the band
+    const float hx0 = (FDTD_IN(c, fext_y(p)) ? p.in[3][c] : 0.f), hy0 = (FDTD_IN(c, fext_y(p)) ? p.in[4][c] : 0.f), hz0 = (FDTD_IN(c, fext_y(p)) ? p.in[5][c] : 0.f);
+    const float ex_c = (FDTD_IN(c, fext_y(p)) ? ex[c] : 0.f), ey_c = (FDTD_IN(c, fext_y(p)) ? ey[c] : 0.f), ez_c = (FDTD_IN(c, fext_y(p)) ? ez[c] : 0.f);
+    const float ez_j = j > 0 ? (FDTD_IN(c - p.sy, fext_y(p)) ? ez[c - p.sy] : 0.f) : 0.f, ex_j = j > 0 ? (FDTD_IN(c - p.sy, fext_y(p)) ? ex[c - p.sy] : 0.f) : 0.f;
+    const float ey_i = i > 0 ? (FDTD_IN(c - p.sx, fext_y(p)) ? ey[c - p.sx] : 0.f) : 0.f, ez_i = i > 0 ? (FDTD_IN(c - p.sx, fext_y(p)) ? ez[c - p.sx] : 0.f) : 0.f;
+    const float ey_k = (FDTD_IN(c - 1, fext_y(p)) ? ey[c - 1] : 0.f), ex_k = (FDTD_IN(c - 1, fext_y(p)) ? ex[c - 1] : 0.f);  // k >= 1 in the band
     const int64_t qy = syh >= 0 ? (i * 2 * P1 + syh) * nz + k : 0;
     const int64_t qx = sxh >= 0 ? ((int64_t)sxh * ny + j) * nz + k : 0;
     const int64_t qz = szh >= 0 ? (i * ny + j) * 2 * P + szh : 0;
     float ps_hxy = 0.f, ps_hxz = 0.f, ps_hyx = 0.f, ps_hyz = 0.f, ps_hzx = 0.f, ps_hzy = 0.f;
     if (syh >= 0) {
-        if (ux) ps_hxy = p.psi_h[3][qy];
-        if (uz) ps_hzy = p.psi_h[2][qy];
+        if (ux) ps_hxy = (FDTD_IN(qy, pext_y(p, 3)) ? p.psi_h[3][qy] : 0.f);
+        if (uz) ps_hzy = (FDTD_IN(qy, pext_y(p, 2)) ? p.psi_h[2][qy] : 0.f);
     }
     if (sxh >= 0) {
-        if (uy) ps_hyx = p.psi_h[0][qx];
-        if (uz) ps_hzx = p.psi_h[1][qx];
+        if (uy) ps_hyx = (FDTD_IN(qx, pext_y(p, 0)) ? p.psi_h[0][qx] : 0.f);
+        if (uz) ps_hzx = (FDTD_IN(qx, pext_y(p, 1)) ? p.psi_h[1][qx] : 0.f);
     }
     if (szh >= 0) {
-        if (ux) ps_hxz = p.psi_h[4][qz];
-        if (uy) ps_hyz = p.psi_h[5][qz];
+        if (ux) ps_hxz = (FDTD_IN(qz, pext_y(p, 4)) ? p.psi_h[4][qz] : 0.f);
+        if (uy) ps_hyz = (FDTD_IN(qz, pext_y(p, 5)) ? p.psi_h[5][qz] : 0.f);
     }
     // ---- arithmetic
     float hx = hx0, hy = hy0, hz = hz0;
@@ -1125,20 +1134,20 @@ __device__ __forceinline__ void zband_h_at(const Params &p, int64_t i, int64_t j
             hz = fadd(hz, fmul(0.5f, corr(ps_hzy, gcoef(p.tb_h[1], p.ta_h[1], p.tk_h[1], syh), fsub(ex_c, ex_j))));
     }
     // ---- stores
-    p.out[3][c] = hx;
-    p.out[4][c] = hy;
-    p.out[5][c] = hz;
+    if (FDTD_IN(c, fext_y(p))) p.out[3][c] = hx;
+    if (FDTD_IN(c, fext_y(p))) p.out[4][c] = hy;
+    if (FDTD_IN(c, fext_y(p))) p.out[5][c] = hz;
     if (syh >= 0) {
-        if (ux) p.psi_h[3][qy] = ps_hxy;
-        if (uz) p.psi_h[2][qy] = ps_hzy;
+        if (ux) if (FDTD_IN(qy, pext_y(p, 3))) p.psi_h[3][qy] = ps_hxy;
+        if (uz) if (FDTD_IN(qy, pext_y(p, 2))) p.psi_h[2][qy] = ps_hzy;
     }
     if (sxh >= 0) {
-        if (uy) p.psi_h[0][qx] = ps_hyx;
-        if (uz) p.psi_h[1][qx] = ps_hzx;
+        if (uy) if (FDTD_IN(qx, pext_y(p, 0))) p.psi_h[0][qx] = ps_hyx;
+        if (uz) if (FDTD_IN(qx, pext_y(p, 1))) p.psi_h[1][qx] = ps_hzx;
     }
     if (szh >= 0) {
-        if (ux) p.psi_h[4][qz] = ps_hxz;
-        if (uy) p.psi_h[5][qz] = ps_hyz;
+        if (ux) if (FDTD_IN(qz, pext_y(p, 4))) p.psi_h[4][qz] = ps_hxz;
+        if (uy) if (FDTD_IN(qz, pext_y(p, 5))) p.psi_h[5][qz] = ps_hyz;
     }
 }
 

@@ -157,6 +157,14 @@ typedef struct {
 
 const char *fdtd_status_string(int status);
 int fdtd_last_cuda_error(void);
+/* Bounds-checked debug build (the library compiled with -DFDTD_CHECK,
+ * libfdtd_gb300_check.so; no reference counterpart: the reference has no
+ * checked build): kernels compare each wrapped global index with its array's
+ * extent and skip an access outside it.  Writes the first miss recorded since
+ * the last call, (1 << 63) | (source line << 40) | (index & (2^40 - 1)), or 0,
+ * and clears the record; waits for the device.  The product build returns
+ * FDTD_ERR_UNSUPPORTED. */
+int fdtd_debug_check(uint64_t *first_bad);
 
 /* ---- reference-shaped kernels (in place) ---------------------------- */
 int fdtd_update_e_f32(const fdtd_grid *g, float *ex, float *ey, float *ez,

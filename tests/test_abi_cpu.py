@@ -47,6 +47,17 @@ def test_status_strings(lib):
     assert N.status_string(0) == "ok"
 
 
+def test_debug_check_outside_the_checked_build(lib):
+    """The product library is not the bounds-checked build: fdtd_debug_check
+    reports that (no CUDA call) and writes 0."""
+    import ctypes as C
+    from fdtd_accelerate_gb300 import _native as N
+    word = C.c_uint64(7)
+    assert lib.fdtd_debug_check(C.byref(word)) == N.FDTD_ERR_UNSUPPORTED
+    assert word.value == 0
+    assert lib.fdtd_debug_check(None) == N.FDTD_ERR_ARG
+
+
 def test_validation_before_cuda(lib):
     """Null pointers and inconsistent grids are rejected on the host."""
     from fdtd_accelerate_gb300 import _native as N

@@ -732,6 +732,7 @@ struct Edge {
     int32_t n;                           // boxes
     int32_t j0[4], j1[4], k0[4], k1[4];  // rows [j0, j1), columns [k0, k1), every x plane
     uint32_t off[5];                     // first cell of each box within one x plane
+    uint32_t rcp[4];                     // ceil(2^32 / width) of each box (division by the width)
 };
 constexpr int EDGE_BLOCK = 256;
 
@@ -743,7 +744,9 @@ __device__ __forceinline__ bool edge_cell(const Edge &eb, int &i, int &j, int &k
     int b = 0;
     while (b + 1 < eb.n && u >= eb.off[b + 1]) b++;
     const uint32_t v = u - eb.off[b], nk = (uint32_t)(eb.k1[b] - eb.k0[b]);
-    const uint32_t r = v / nk;
+    uint32_t r = __umulhi(v, eb.rcp[b]);  // v / nk, or one off
+    if (r * nk > v) r--;
+    else if ((r + 1) * nk <= v) r++;
     k = eb.k0[b] + (int)(v - r * nk);
     j = eb.j0[b] + (int)r;
     i = blockIdx.y;
@@ -755,7 +758,7 @@ __global__ void __launch_bounds__(EDGE_BLOCK)
 k_edge_h(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     int i, j, k;
     if (!edge_cell(eb, i, j, k)) return;
-    const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
+    const uint32_t X = p.sx, Y = p.sy, c = (uint32_t)i * X + (uint32_t)j * Y + (uint32_t)k;
     const float *ex = p.in[0], *ey = p.in[1], *ez = p.in[2];
     [[maybe_unused]] const int64_t FE = fext(p);
     [[maybe_unused]] const int64_t PE0 = pext(p, 0, p.ha[0].P), PE1 = PE0, PE2 = pext(p, 1, p.ha[1].P),
@@ -840,7 +843,7 @@ __global__ void __launch_bounds__(EDGE_BLOCK)
 k_edge_e(const __grid_constant__ Params p, const __grid_constant__ Edge eb) {
     int i, j, k;
     if (!edge_cell(eb, i, j, k)) return;
-    const int64_t X = p.sx, Y = p.sy, c = (int64_t)i * X + (int64_t)j * Y + k;
+    const uint32_t X = p.sx, Y = p.sy, c = (uint32_t)i * X + (uint32_t)j * Y + (uint32_t)k;
     const float *hx = p.out[3], *hy = p.out[4], *hz = p.out[5];
     [[maybe_unused]] const int64_t FE = fext(p);
     [[maybe_unused]] const int64_t PE0 = pext(p, 0, p.ea[0].P), PE1 = PE0, PE2 = pext(p, 1, p.ea[1].P),
@@ -1143,6 +1146,8 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
         if (j1 <= j0 || k1 <= k0) return;
         eb.j0[eb.n] = (int)j0; eb.j1[eb.n] = (int)j1; eb.k0[eb.n] = (int)k0; eb.k1[eb.n] = (int)k1;
         eb.off[eb.n + 1] = eb.off[eb.n] + (uint32_t)((j1 - j0) * (k1 - k0));
+        eb.rcp[eb.n] = (uint32_t)std::min<uint64_t>((((uint64_t)1 << 32) + (uint64_t)(k1 - k0) - 1) / (uint64_t)(k1 - k0),
+                                                    0xFFFFFFFFull);
         eb.n++;
     };
     if (p.nty_in == 0 || p.ntz_in == 0) {

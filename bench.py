@@ -739,8 +739,10 @@ def run_adjoint256(args):
     from fdtd_accelerate_gb300 import configs
     dev = torch.device("cuda", 0)
     w = configs.adjoint256(steps=args.steps)
+    # the gradient the workload asks for: every design-cell eps (dL/dCE is
+    # accumulated over the design region only)
     eng = F.YeeAdjoint(w.shape, w.steps, npml=w.npml, sources=w.sources, monitors=w.monitors,
-                       segment=w.segment, device=dev)
+                       segment=w.segment, device=dev, grad_region=w.design)
     eps = w.eps.to(dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -803,7 +805,8 @@ def run_adjoint256(args):
                       {"higher_is_better": False,
                        "forward": {"ms": fwd, "Mcells_per_s": nc * w.steps / (fwd / 1e3) / 1e6},
                        "backward": {"ms": bwd, "Mcells_per_s": nc * w.steps / (bwd / 1e3) / 1e6,
-                                    "what": "segment recompute from checkpoints + reverse-time adjoint steps"},
+                                    "what": "segment recompute from checkpoints + reverse-time adjoint steps, "
+                                            "dL/dCE accumulated over the 128x128x64 design region"},
                        "gradient_over_forward": (fwd + bwd) / fwd,
                        "fd_check": {"cells": len(cells), "h": h, "loss": L0,
                                     "median_rel_err": float(np.median(errs)) if errs else None,

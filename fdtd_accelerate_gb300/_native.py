@@ -127,6 +127,8 @@ _SIGS = {
                                         C.POINTER(Points), P, P]),
     "fdtd_adjoint_step_noalloc_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P,
                                                 P, C.POINTER(Points), P, P]),
+    "fdtd_adjoint_step_region_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Cpml), C.POINTER(AdjointState), P, P,
+                                               P, C.POINTER(Points), P, P, P]),
     "fdtd_gather_points_f32": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),
     "fdtd_step_unfused_f64": (C.c_int, [C.POINTER(Grid), P, P, C.POINTER(Cpml), P, P, C.POINTER(Sources), I64, P]),
     "fdtd_gather_points_f64": (C.c_int, [C.POINTER(Grid), C.POINTER(Points), P, P, P]),

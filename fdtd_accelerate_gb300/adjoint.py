@@ -42,10 +42,14 @@ class YeeAdjoint:
 
     monitors: list of (component, (i, j, k)); component in ex..hz.
     segment: checkpoint interval K (steps).
+    grad_region: three slices (a design region): dL/dCE is accumulated only
+    there (fdtd_adjoint_step_region_f32) and returned as zero elsewhere; the
+    reverse steps then skip the forward-H reads and the accumulator traffic of
+    every other cell.  None: every cell.
     """
 
     def __init__(self, shape, nsteps, npml=0, faces=0x3F, cpml_params=None, sources=(), monitors=(),
-                 segment=100, device="cuda", tile=None):
+                 segment=100, device="cuda", tile=None, grad_region=None):
         nx, ny, nz = (int(v) for v in shape)
         self.shape = (nx, ny, nz)
         self.nsteps = int(nsteps)
@@ -79,6 +83,15 @@ class YeeAdjoint:
         self._plans = None
         self._slots_hold = None   # (run id, segment) whose states the slots hold
         self._run_id = 0
+        self._gbox = None
+        if grad_region is not None:
+            box = []
+            for sl, n in zip(grad_region, self.shape):
+                a, b, st = sl.indices(n)
+                if st != 1 or b <= a:
+                    raise ValueError("grad_region needs three non-empty unit-step slices: %r" % (grad_region,))
+                box.append((a, b - a))
+            self._gbox = (C.c_int64 * 6)(*[v[0] for v in box], *[v[1] for v in box])
 
     # ------------------------------------------------------------ helpers
     @staticmethod
@@ -246,15 +259,16 @@ class YeeAdjoint:
                     for m in range(L):
                         self._step_slot(m, t0 + m + 1)
                     self._slots_hold = (run_id, c)
-                fn = N.lib().fdtd_adjoint_step_f32
+                fn = N.lib().fdtd_adjoint_step_f32 if self._gbox is None else N.lib().fdtd_adjoint_step_region_f32
                 gp, cpp, stp = C.byref(g), C.byref(cp), C.byref(st)
+                extra = () if self._gbox is None else (self._gbox,)
                 ptsp = C.byref(pts) if gm is not None else None
                 row = gm.stride(0) * 4 if gm is not None else 0
                 base = gm.data_ptr() if gm is not None else 0
                 for n in range(L, 0, -1):
                     T = t0 + n
                     mon_ptr = C.c_void_p(base + (T - 1) * row) if gm is not None else None
-                    rc = fn(gp, cpp, stp, hps[n - 1], pes[n], ce_p, ptsp, mon_ptr, stream)
+                    rc = fn(gp, cpp, stp, hps[n - 1], pes[n], ce_p, ptsp, mon_ptr, *extra, stream)
                     if rc:
                         N.check(rc, "fdtd_adjoint_step_f32")
         return gce[:, :, :, :nz]

@@ -44,6 +44,10 @@ struct Args {
     const float *ce[3];
     const float *be[3], *ae[3], *ke[3];
     const float *bh[3], *ah[3], *kh[3];
+    // gbox = 1: dL/dCE accumulated only on cells [gb0, gb1) (a design region);
+    // the adjoint fields are the same either way
+    int32_t gbox;
+    int64_t gb0[3], gb1[3];
 };
 
 // dense psi indices: x (2P, ny, nz), y (nx, 2P, nz), z (nx, ny, 2P)
@@ -169,6 +173,8 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
     const int sye = slab_of_e(j, A.P[1], g.ny, A.front[1], A.back[1]);
     const int sze = slab_of_e(k, A.P[2], g.nz, A.front[2], A.back[2]);
     const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
+    const bool gin = !A.gbox || (i >= A.gb0[0] && i < A.gb1[0] && j >= A.gb0[1] && j < A.gb1[1] &&
+                                 k >= A.gb0[2] && k < A.gb1[2]);
 
     // ex: E source of hzy (y axis, psi 0 of h) and hyz (z axis, psi 1 of h)
     if (em(g, 0, i, j, k)) {
@@ -179,17 +185,19 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
         if (szh1 >= 0) d = fsub(d, A.wh[5][pz(g, Pz, i, j, szh1)]);
         const float l = fadd(A.lf[0][c], d);
         A.lf[0][c] = l;
-        // G = curl_f(H) + (exy: +) + (exz: -)
-        float G = curl4(hz[c + g.sy], hz[c], hy[c + 1], hy[c]);
-        if (sye >= 0) {
-            const float dd = fsub(hz[c + g.sy], hz[c]);
-            G = fadd(G, fadd(fmul(A.ke[1][sye], dd), A.pe[3][py(g, Py, i, sye, k)]));
+        if (gin) {
+            // G = curl_f(H) + (exy: +) + (exz: -)
+            float G = curl4(hz[c + g.sy], hz[c], hy[c + 1], hy[c]);
+            if (sye >= 0) {
+                const float dd = fsub(hz[c + g.sy], hz[c]);
+                G = fadd(G, fadd(fmul(A.ke[1][sye], dd), A.pe[3][py(g, Py, i, sye, k)]));
+            }
+            if (sze >= 0) {
+                const float dd = fsub(hy[c + 1], hy[c]);
+                G = fsub(G, fadd(fmul(A.ke[2][sze], dd), A.pe[4][pz(g, Pz, i, j, sze)]));
+            }
+            A.gce[0][c] = fadd(A.gce[0][c], fmul(l, G));
         }
-        if (sze >= 0) {
-            const float dd = fsub(hy[c + 1], hy[c]);
-            G = fsub(G, fadd(fmul(A.ke[2][sze], dd), A.pe[4][pz(g, Pz, i, j, sze)]));
-        }
-        A.gce[0][c] = fadd(A.gce[0][c], fmul(l, G));
     }
     // ey: E source of hzx (x axis, psi 1) and hxz (z axis, psi 0)
     if (em(g, 1, i, j, k)) {
@@ -200,17 +208,19 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
         if (szh1 >= 0) d = fsub(d, A.wh[4][pz(g, Pz, i, j, szh1)]);
         const float l = fadd(A.lf[1][c], d);
         A.lf[1][c] = l;
-        // G = curl_f(H) + (eyx: -) + (eyz: +)
-        float G = curl4(hx[c + 1], hx[c], hz[c + g.sx], hz[c]);
-        if (sxe >= 0) {
-            const float dd = fsub(hz[c + g.sx], hz[c]);
-            G = fsub(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[0][px(g, sxe, j, k)]));
+        if (gin) {
+            // G = curl_f(H) + (eyx: -) + (eyz: +)
+            float G = curl4(hx[c + 1], hx[c], hz[c + g.sx], hz[c]);
+            if (sxe >= 0) {
+                const float dd = fsub(hz[c + g.sx], hz[c]);
+                G = fsub(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[0][px(g, sxe, j, k)]));
+            }
+            if (sze >= 0) {
+                const float dd = fsub(hx[c + 1], hx[c]);
+                G = fadd(G, fadd(fmul(A.ke[2][sze], dd), A.pe[5][pz(g, Pz, i, j, sze)]));
+            }
+            A.gce[1][c] = fadd(A.gce[1][c], fmul(l, G));
         }
-        if (sze >= 0) {
-            const float dd = fsub(hx[c + 1], hx[c]);
-            G = fadd(G, fadd(fmul(A.ke[2][sze], dd), A.pe[5][pz(g, Pz, i, j, sze)]));
-        }
-        A.gce[1][c] = fadd(A.gce[1][c], fmul(l, G));
     }
     // ez: E source of hyx (x axis, psi 0) and hxy (y axis, psi 1)
     if (em(g, 2, i, j, k)) {
@@ -221,17 +231,19 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
         if (syh1 >= 0) d = fsub(d, A.wh[3][py(g, Py, i, syh1, k)]);
         const float l = fadd(A.lf[2][c], d);
         A.lf[2][c] = l;
-        // G = curl_f(H) + (ezx: +) + (ezy: -)
-        float G = curl4(hy[c + g.sx], hy[c], hx[c + g.sy], hx[c]);
-        if (sxe >= 0) {
-            const float dd = fsub(hy[c + g.sx], hy[c]);
-            G = fadd(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[1][px(g, sxe, j, k)]));
+        if (gin) {
+            // G = curl_f(H) + (ezx: +) + (ezy: -)
+            float G = curl4(hy[c + g.sx], hy[c], hx[c + g.sy], hx[c]);
+            if (sxe >= 0) {
+                const float dd = fsub(hy[c + g.sx], hy[c]);
+                G = fadd(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[1][px(g, sxe, j, k)]));
+            }
+            if (sye >= 0) {
+                const float dd = fsub(hx[c + g.sy], hx[c]);
+                G = fsub(G, fadd(fmul(A.ke[1][sye], dd), A.pe[2][py(g, Py, i, sye, k)]));
+            }
+            A.gce[2][c] = fadd(A.gce[2][c], fmul(l, G));
         }
-        if (sye >= 0) {
-            const float dd = fsub(hx[c + g.sy], hx[c]);
-            G = fsub(G, fadd(fmul(A.ke[1][sye], dd), A.pe[2][py(g, Py, i, sye, k)]));
-        }
-        A.gce[2][c] = fadd(A.gce[2][c], fmul(l, G));
     }
     (void)Px;
 }
@@ -401,9 +413,13 @@ using namespace fdtd::adj;
 
 extern "C" {
 
-int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
-                          const float *const h_prev[3], const float *const psi_e_cur[6], const float *const ce[3],
-                          const fdtd_points *mon, const float *mon_grad, void *stream) {
+}  // extern "C"
+
+// one reverse step; box (i0, j0, k0, ni, nj, nk) limits the dL/dCE
+// accumulation, NULL: every cell
+static int adjoint_step(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
+                        const float *const h_prev[3], const float *const psi_e_cur[6], const float *const ce[3],
+                        const fdtd_points *mon, const float *mon_grad, const int64_t *box, void *stream) {
     NvtxRange nvtx_range("fdtd_adjoint_step");
     Grid g;
     FDTD_TRY(validate_grid(gp, &g));
@@ -445,6 +461,15 @@ int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_a
         A.hp[q] = h_prev[q];
         A.ce[q] = ce[q];
     }
+    if (box) {
+        const int64_t n3[3] = {g.nx, g.ny, g.nz};
+        for (int a = 0; a < 3; a++) {
+            if (box[a] < 0 || box[3 + a] < 0 || box[a] + box[3 + a] > n3[a]) return FDTD_ERR_SHAPE;
+            A.gb0[a] = box[a];
+            A.gb1[a] = box[a] + box[3 + a];
+        }
+        A.gbox = 1;
+    }
     cudaStream_t st = as_stream(stream);
     if (mon && mon->n > 0) {
         FDTD_TRY(validate_points(g, mon));
@@ -462,6 +487,22 @@ int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_a
     if (A.P[2]) launch_slab<2>(g, A.P[2], true, A, st);
     k_adj_h<<<cells(g), kB, 0, st>>>(A);
     return check_launch();
+}
+
+extern "C" {
+
+int fdtd_adjoint_step_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
+                          const float *const h_prev[3], const float *const psi_e_cur[6], const float *const ce[3],
+                          const fdtd_points *mon, const float *mon_grad, void *stream) {
+    return adjoint_step(gp, cp, s, h_prev, psi_e_cur, ce, mon, mon_grad, nullptr, stream);
+}
+
+int fdtd_adjoint_step_region_f32(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adjoint_state *s,
+                                 const float *const h_prev[3], const float *const psi_e_cur[6],
+                                 const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
+                                 const int64_t grad_box[6], void *stream) {
+    if (!grad_box) return FDTD_ERR_ARG;
+    return adjoint_step(gp, cp, s, h_prev, psi_e_cur, ce, mon, mon_grad, grad_box, stream);
 }
 
 }  // extern "C"

@@ -388,6 +388,16 @@ int fdtd_adjoint_step_f32(const fdtd_grid *g, const fdtd_cpml *c, const fdtd_adj
                           const float *const h_prev[3], const float *const psi_e_cur[6],
                           const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
                           void *stream);
+/* fdtd_adjoint_step_f32 with dL/dCE accumulated only on the cells of the box
+ * grad_box = {i0, j0, k0, ni, nj, nk} (a design region; grad_ce is left
+ * untouched outside it).  The adjoint fields lf / lpsi evolve exactly as in
+ * fdtd_adjoint_step_f32; cells outside the box skip the forward-H reads and
+ * the accumulator's read and write.  A box outside the grid: FDTD_ERR_SHAPE.
+ * No reference counterpart. */
+int fdtd_adjoint_step_region_f32(const fdtd_grid *g, const fdtd_cpml *c, const fdtd_adjoint_state *s,
+                                 const float *const h_prev[3], const float *const psi_e_cur[6],
+                                 const float *const ce[3], const fdtd_points *mon, const float *mon_grad,
+                                 const int64_t grad_box[6], void *stream);
 /* fdtd_adjoint_step_f32 without caller scratch: s->w_e / s->w_h are ignored
  * and a device array of 4 Mi floats (16 MiB) inside the library is used
  * instead, for callers that cannot allocate device memory.  A CPML layer

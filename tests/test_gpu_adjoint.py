@@ -198,6 +198,32 @@ def test_gradient_vs_fp64_autograd(F, shape, npml, nsteps):
         assert err < max(1e-4, 3 * floor), "dL/dce%d relative error %.2e (FP32 floor %.2e)" % (q, err, floor)
 
 
+def test_design_region_gradient_equals_full_gradient_inside(F):
+    """grad_region (fdtd_adjoint_step_region_f32): inside the box the gradient
+    equals the whole-grid run bit for bit (the adjoint fields do not depend on
+    the box), outside it is zero; the box may touch the CPML slabs."""
+    shape, npml, nsteps = (30, 28, 36), 5, 60
+    ce, src, mons = make_case(shape, npml, nsteps, seed=4)
+    region = (slice(3, 21), slice(7, 28), slice(0, 17))
+    grads = []
+    for reg in (None, region):
+        eng = F.YeeAdjoint(shape, nsteps, npml=npml, sources=src, monitors=mons, segment=16, grad_region=reg)
+        cg = ce.cuda().requires_grad_(True)
+        mon, _ = F.fdtd_run(cg, eng)
+        (mon.double() ** 2).sum().backward()
+        grads.append(cg.grad.detach().cpu())
+        eng.close()
+    full, part = grads
+    mask = torch.zeros(shape, dtype=torch.bool)
+    mask[region] = True
+    for q in range(3):
+        np.testing.assert_array_equal(part[q][mask].numpy(), full[q][mask].numpy(), err_msg="dL/dce%d inside" % q)
+        assert not part[q][~mask].any(), "dL/dce%d outside the region" % q
+    assert full[:, ~mask].abs().max() > 0   # the whole-grid gradient is not zero there
+    with pytest.raises(ValueError):
+        F.YeeAdjoint(shape, nsteps, npml=npml, grad_region=(slice(0, 0), slice(None), slice(None)))
+
+
 def test_gradient_vs_finite_differences(F):
     """Central differences in eps (h = 1e-3) at cells near the monitors against
     dL/deps from the adjoint run with CE = 0.5/eps for all three components of

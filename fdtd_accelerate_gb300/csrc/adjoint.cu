@@ -110,12 +110,14 @@ __global__ void __launch_bounds__(kB) k_adj_hpsi(Args A) {
         if (k >= g.nz) return;
         j = slab_node_h(s, P, g.ny);
         p = py(g, P, i, s, k);
-    } else {
-        const int64_t t = (int64_t)blockIdx.x * kB + threadIdx.x;
-        if (t >= g.nx * g.ny * 2 * P) return;
-        s = t % (2 * P); j = (t / (2 * P)) % g.ny; i = t / (2 * P * g.ny);
+    } else {  // blockIdx.y = i; u = j * 2P + s within the plane
+        const uint32_t u = blockIdx.x * kB + threadIdx.x, w = 2u * (uint32_t)P;
+        if (u >= (uint32_t)g.ny * w) return;
+        i = blockIdx.y;
+        j = u / w;
+        s = u - (uint32_t)j * w;
         k = slab_node_h(s, P, g.nz);
-        p = t;
+        p = i * g.ny * w + u;
     }
     if (!(s < P ? A.front[AX] : A.back[AX])) return;
     const int64_t c = i * g.sx + j * g.sy + k;
@@ -146,21 +148,18 @@ __global__ void __launch_bounds__(kB) k_adj_hpsi(Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// 2. reverse H part on E cells + gradient.  One thread per cell.
+// 2. reverse H part on E cells + gradient.  One thread per cell.  Every load
+//    comes first, then the arithmetic, then the stores: a store could alias a
+//    later load as far as the compiler knows, and loads placed after stores
+//    would wait for them instead of overlapping.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
     const Grid &g = A.g;
     const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
     const int64_t j = blockIdx.y, i = blockIdx.z;
     if (k >= g.nz) return;
-    const int64_t c = i * g.sx + j * g.sy + k;
-    const float *lhx = A.lf[3], *lhy = A.lf[4], *lhz = A.lf[5];
-    const float *hx = A.hp[0], *hy = A.hp[1], *hz = A.hp[2];
-    // masked adjoint H reads
-    auto LH = [&](int q, const float *f, int64_t di, int64_t dj, int64_t dk) {
-        const int64_t ii = i + di, jj = j + dj, kk = k + dk;
-        return hm(q, ii, jj, kk) ? f[c + di * g.sx + dj * g.sy + dk] : 0.f;
-    };
+    const int64_t c = i * g.sx + j * g.sy + k, X = g.sx, Y = g.sy;
+    const bool e0 = em(g, 0, i, j, k), e1 = em(g, 1, i, j, k), e2 = em(g, 2, i, j, k);
     // slab indices of this cell's nodes (H-node form for the w_h gather,
     // E-node form for the gradient's psi terms)
     const int sxh0 = slab_of_h(i, A.P[0], g.nx, A.front[0], A.back[0]);
@@ -172,80 +171,110 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
     const int sxe = slab_of_e(i, A.P[0], g.nx, A.front[0], A.back[0]);
     const int sye = slab_of_e(j, A.P[1], g.ny, A.front[1], A.back[1]);
     const int sze = slab_of_e(k, A.P[2], g.nz, A.front[2], A.back[2]);
-    const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
+    const int Py = A.P[1], Pz = A.P[2];
     const bool gin = !A.gbox || (i >= A.gb0[0] && i < A.gb1[0] && j >= A.gb0[1] && j < A.gb1[1] &&
                                  k >= A.gb0[2] && k < A.gb1[2]);
 
-    // ex: E source of hzy (y axis, psi 0 of h) and hyz (z axis, psi 1 of h)
-    if (em(g, 0, i, j, k)) {
-        float d = fmul(-0.5f, curl4(LH(2, lhz, 0, 1, 0), LH(2, lhz, 0, 0, 0), LH(1, lhy, 0, 0, 1), LH(1, lhy, 0, 0, 0)));
-        if (syh0 >= 0) d = fadd(d, A.wh[2][py(g, Py, i, syh0, k)]);
-        if (syh1 >= 0) d = fsub(d, A.wh[2][py(g, Py, i, syh1, k)]);
-        if (szh0 >= 0) d = fadd(d, A.wh[5][pz(g, Pz, i, j, szh0)]);
-        if (szh1 >= 0) d = fsub(d, A.wh[5][pz(g, Pz, i, j, szh1)]);
-        const float l = fadd(A.lf[0][c], d);
+    // ---- loads
+    auto L = [&](const float *f, bool m, int64_t o) { return m ? __ldg(f + c + o) : 0.f; };
+    auto W = [&](int q, bool m, int64_t p) { return m ? __ldg(A.wh[q] + p) : 0.f; };
+    const float *lhx = A.lf[3], *lhy = A.lf[4], *lhz = A.lf[5];
+    // adjoint H through the H update masks: the cell, and the +1 neighbours
+    // each E component differentiates (their loads only where it is updated)
+    const float hz0 = L(lhz, i > 0 && j > 0, 0), hy0 = L(lhy, i > 0 && k > 0, 0), hx0 = L(lhx, j > 0 && k > 0, 0);
+    const float hzj = L(lhz, e0 && i > 0, Y), hyk = L(lhy, e0 && i > 0, 1);  // ex
+    const float hxk = L(lhx, e1 && j > 0, 1), hzi = L(lhz, e1 && j > 0, X);  // ey
+    const float hyi = L(lhy, e2 && k > 0, X), hxj = L(lhx, e2 && k > 0, Y);  // ez
+    // w_h of the slab nodes at this index (+) and one above (-), per component
+    // ex: hzy (y, psi 0 of h) and hyz (z, psi 1); ey: hzx (x, psi 1) and hxz
+    // (z, psi 0); ez: hyx (x, psi 0) and hxy (y, psi 1)
+    const float wx0 = W(2, e0 && syh0 >= 0, py(g, Py, i, syh0, k)), wx1 = W(2, e0 && syh1 >= 0, py(g, Py, i, syh1, k));
+    const float wx2 = W(5, e0 && szh0 >= 0, pz(g, Pz, i, j, szh0)), wx3 = W(5, e0 && szh1 >= 0, pz(g, Pz, i, j, szh1));
+    const float wy0 = W(1, e1 && sxh0 >= 0, px(g, sxh0, j, k)), wy1 = W(1, e1 && sxh1 >= 0, px(g, sxh1, j, k));
+    const float wy2 = W(4, e1 && szh0 >= 0, pz(g, Pz, i, j, szh0)), wy3 = W(4, e1 && szh1 >= 0, pz(g, Pz, i, j, szh1));
+    const float wz0 = W(0, e2 && sxh0 >= 0, px(g, sxh0, j, k)), wz1 = W(0, e2 && sxh1 >= 0, px(g, sxh1, j, k));
+    const float wz2 = W(3, e2 && syh0 >= 0, py(g, Py, i, syh0, k)), wz3 = W(3, e2 && syh1 >= 0, py(g, Py, i, syh1, k));
+    const float le0 = e0 ? A.lf[0][c] : 0.f, le1 = e1 ? A.lf[1][c] : 0.f, le2 = e2 ? A.lf[2][c] : 0.f;
+    // gradient: forward H entering the step (unmasked), forward E-psi, accumulators
+    float Hz0 = 0.f, Hzj = 0.f, Hzi = 0.f, Hy0 = 0.f, Hyk = 0.f, Hyi = 0.f, Hx0 = 0.f, Hxk = 0.f, Hxj = 0.f;
+    float pe3 = 0.f, pe4 = 0.f, pe0 = 0.f, pe5 = 0.f, pe1 = 0.f, pe2 = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    if (gin) {
+        const float *hx = A.hp[0], *hy = A.hp[1], *hz = A.hp[2];
+        Hz0 = __ldg(hz + c);
+        Hy0 = __ldg(hy + c);
+        Hx0 = __ldg(hx + c);
+        if (e0) {
+            Hzj = __ldg(hz + c + Y);
+            Hyk = __ldg(hy + c + 1);
+            if (sye >= 0) pe3 = __ldg(A.pe[3] + py(g, Py, i, sye, k));
+            if (sze >= 0) pe4 = __ldg(A.pe[4] + pz(g, Pz, i, j, sze));
+            g0 = A.gce[0][c];
+        }
+        if (e1) {
+            Hxk = __ldg(hx + c + 1);
+            Hzi = __ldg(hz + c + X);
+            if (sxe >= 0) pe0 = __ldg(A.pe[0] + px(g, sxe, j, k));
+            if (sze >= 0) pe5 = __ldg(A.pe[5] + pz(g, Pz, i, j, sze));
+            g1 = A.gce[1][c];
+        }
+        if (e2) {
+            Hyi = __ldg(hy + c + X);
+            Hxj = __ldg(hx + c + Y);
+            if (sxe >= 0) pe1 = __ldg(A.pe[1] + px(g, sxe, j, k));
+            if (sye >= 0) pe2 = __ldg(A.pe[2] + py(g, Py, i, sye, k));
+            g2 = A.gce[2][c];
+        }
+    }
+
+    // ---- arithmetic and stores
+    if (e0) {  // ex
+        float d = fmul(-0.5f, curl4(hzj, hz0, hyk, hy0));
+        if (syh0 >= 0) d = fadd(d, wx0);
+        if (syh1 >= 0) d = fsub(d, wx1);
+        if (szh0 >= 0) d = fadd(d, wx2);
+        if (szh1 >= 0) d = fsub(d, wx3);
+        const float l = fadd(le0, d);
         A.lf[0][c] = l;
         if (gin) {
             // G = curl_f(H) + (exy: +) + (exz: -)
-            float G = curl4(hz[c + g.sy], hz[c], hy[c + 1], hy[c]);
-            if (sye >= 0) {
-                const float dd = fsub(hz[c + g.sy], hz[c]);
-                G = fadd(G, fadd(fmul(A.ke[1][sye], dd), A.pe[3][py(g, Py, i, sye, k)]));
-            }
-            if (sze >= 0) {
-                const float dd = fsub(hy[c + 1], hy[c]);
-                G = fsub(G, fadd(fmul(A.ke[2][sze], dd), A.pe[4][pz(g, Pz, i, j, sze)]));
-            }
-            A.gce[0][c] = fadd(A.gce[0][c], fmul(l, G));
+            float G = curl4(Hzj, Hz0, Hyk, Hy0);
+            if (sye >= 0) G = fadd(G, fadd(fmul(__ldg(A.ke[1] + sye), fsub(Hzj, Hz0)), pe3));
+            if (sze >= 0) G = fsub(G, fadd(fmul(__ldg(A.ke[2] + sze), fsub(Hyk, Hy0)), pe4));
+            A.gce[0][c] = fadd(g0, fmul(l, G));
         }
     }
-    // ey: E source of hzx (x axis, psi 1) and hxz (z axis, psi 0)
-    if (em(g, 1, i, j, k)) {
-        float d = fmul(-0.5f, curl4(LH(0, lhx, 0, 0, 1), LH(0, lhx, 0, 0, 0), LH(2, lhz, 1, 0, 0), LH(2, lhz, 0, 0, 0)));
-        if (sxh0 >= 0) d = fadd(d, A.wh[1][px(g, sxh0, j, k)]);
-        if (sxh1 >= 0) d = fsub(d, A.wh[1][px(g, sxh1, j, k)]);
-        if (szh0 >= 0) d = fadd(d, A.wh[4][pz(g, Pz, i, j, szh0)]);
-        if (szh1 >= 0) d = fsub(d, A.wh[4][pz(g, Pz, i, j, szh1)]);
-        const float l = fadd(A.lf[1][c], d);
+    if (e1) {  // ey
+        float d = fmul(-0.5f, curl4(hxk, hx0, hzi, hz0));
+        if (sxh0 >= 0) d = fadd(d, wy0);
+        if (sxh1 >= 0) d = fsub(d, wy1);
+        if (szh0 >= 0) d = fadd(d, wy2);
+        if (szh1 >= 0) d = fsub(d, wy3);
+        const float l = fadd(le1, d);
         A.lf[1][c] = l;
         if (gin) {
             // G = curl_f(H) + (eyx: -) + (eyz: +)
-            float G = curl4(hx[c + 1], hx[c], hz[c + g.sx], hz[c]);
-            if (sxe >= 0) {
-                const float dd = fsub(hz[c + g.sx], hz[c]);
-                G = fsub(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[0][px(g, sxe, j, k)]));
-            }
-            if (sze >= 0) {
-                const float dd = fsub(hx[c + 1], hx[c]);
-                G = fadd(G, fadd(fmul(A.ke[2][sze], dd), A.pe[5][pz(g, Pz, i, j, sze)]));
-            }
-            A.gce[1][c] = fadd(A.gce[1][c], fmul(l, G));
+            float G = curl4(Hxk, Hx0, Hzi, Hz0);
+            if (sxe >= 0) G = fsub(G, fadd(fmul(__ldg(A.ke[0] + sxe), fsub(Hzi, Hz0)), pe0));
+            if (sze >= 0) G = fadd(G, fadd(fmul(__ldg(A.ke[2] + sze), fsub(Hxk, Hx0)), pe5));
+            A.gce[1][c] = fadd(g1, fmul(l, G));
         }
     }
-    // ez: E source of hyx (x axis, psi 0) and hxy (y axis, psi 1)
-    if (em(g, 2, i, j, k)) {
-        float d = fmul(-0.5f, curl4(LH(1, lhy, 1, 0, 0), LH(1, lhy, 0, 0, 0), LH(0, lhx, 0, 1, 0), LH(0, lhx, 0, 0, 0)));
-        if (sxh0 >= 0) d = fadd(d, A.wh[0][px(g, sxh0, j, k)]);
-        if (sxh1 >= 0) d = fsub(d, A.wh[0][px(g, sxh1, j, k)]);
-        if (syh0 >= 0) d = fadd(d, A.wh[3][py(g, Py, i, syh0, k)]);
-        if (syh1 >= 0) d = fsub(d, A.wh[3][py(g, Py, i, syh1, k)]);
-        const float l = fadd(A.lf[2][c], d);
+    if (e2) {  // ez
+        float d = fmul(-0.5f, curl4(hyi, hy0, hxj, hx0));
+        if (sxh0 >= 0) d = fadd(d, wz0);
+        if (sxh1 >= 0) d = fsub(d, wz1);
+        if (syh0 >= 0) d = fadd(d, wz2);
+        if (syh1 >= 0) d = fsub(d, wz3);
+        const float l = fadd(le2, d);
         A.lf[2][c] = l;
         if (gin) {
             // G = curl_f(H) + (ezx: +) + (ezy: -)
-            float G = curl4(hy[c + g.sx], hy[c], hx[c + g.sy], hx[c]);
-            if (sxe >= 0) {
-                const float dd = fsub(hy[c + g.sx], hy[c]);
-                G = fadd(G, fadd(fmul(A.ke[0][sxe], dd), A.pe[1][px(g, sxe, j, k)]));
-            }
-            if (sye >= 0) {
-                const float dd = fsub(hx[c + g.sy], hx[c]);
-                G = fsub(G, fadd(fmul(A.ke[1][sye], dd), A.pe[2][py(g, Py, i, sye, k)]));
-            }
-            A.gce[2][c] = fadd(A.gce[2][c], fmul(l, G));
+            float G = curl4(Hyi, Hy0, Hxj, Hx0);
+            if (sxe >= 0) G = fadd(G, fadd(fmul(__ldg(A.ke[0] + sxe), fsub(Hyi, Hy0)), pe1));
+            if (sye >= 0) G = fsub(G, fadd(fmul(__ldg(A.ke[1] + sye), fsub(Hxj, Hx0)), pe2));
+            A.gce[2][c] = fadd(g2, fmul(l, G));
         }
     }
-    (void)Px;
 }
 
 // ---------------------------------------------------------------------------
@@ -268,12 +297,14 @@ __global__ void __launch_bounds__(kB) k_adj_epsi(Args A) {
         if (k >= g.nz) return;
         j = slab_node_e(s, P, g.ny);
         p = py(g, P, i, s, k);
-    } else {
-        const int64_t t = (int64_t)blockIdx.x * kB + threadIdx.x;
-        if (t >= g.nx * g.ny * 2 * P) return;
-        s = t % (2 * P); j = (t / (2 * P)) % g.ny; i = t / (2 * P * g.ny);
+    } else {  // blockIdx.y = i; u = j * 2P + s within the plane
+        const uint32_t u = blockIdx.x * kB + threadIdx.x, w = 2u * (uint32_t)P;
+        if (u >= (uint32_t)g.ny * w) return;
+        i = blockIdx.y;
+        j = u / w;
+        s = u - (uint32_t)j * w;
         k = slab_node_e(s, P, g.nz);
-        p = t;
+        p = i * g.ny * w + u;
     }
     if (!(s < P ? A.front[AX] : A.back[AX])) return;
     const int64_t c = i * g.sx + j * g.sy + k;
@@ -303,19 +334,16 @@ __global__ void __launch_bounds__(kB) k_adj_epsi(Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// 4. reverse E part on H cells: lH += curl_b(CE*lE) + scatter of w_e.
+// 4. reverse E part on H cells: lH += curl_b(CE*lE) + scatter of w_e.  Loads
+//    first, as in k_adj_e.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kB) k_adj_h(Args A) {
     const Grid &g = A.g;
     const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
     const int64_t j = blockIdx.y, i = blockIdx.z;
     if (k >= g.nz) return;
-    const int64_t c = i * g.sx + j * g.sy + k;
-    auto NU = [&](int q, int64_t di, int64_t dj, int64_t dk) {
-        const int64_t ii = i + di, jj = j + dj, kk = k + dk;
-        const int64_t cc = c + di * g.sx + dj * g.sy + dk;
-        return em(g, q, ii, jj, kk) ? fmul(A.ce[q][cc], A.lf[q][cc]) : 0.f;
-    };
+    const int64_t c = i * g.sx + j * g.sy + k, X = g.sx, Y = g.sy;
+    const bool h0 = hm(0, i, j, k), h1 = hm(1, i, j, k), h2 = hm(2, i, j, k);
     const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
     // E-node slabs at this index and one below (H cell h: +w at node h-1, -w at node h)
     const int sx0 = slab_of_e(i - 1, Px, g.nx, A.front[0], A.back[0]);
@@ -324,32 +352,54 @@ __global__ void __launch_bounds__(kB) k_adj_h(Args A) {
     const int sy1 = slab_of_e(j, Py, g.ny, A.front[1], A.back[1]);
     const int sz0 = slab_of_e(k - 1, Pz, g.nz, A.front[2], A.back[2]);
     const int sz1 = slab_of_e(k, Pz, g.nz, A.front[2], A.back[2]);
-    // hx: H source of ezy (y axis, psi 0 of e) and eyz (z axis, psi 1)
-    if (hm(0, i, j, k)) {
-        float d = curl4(NU(2, 0, 0, 0), NU(2, 0, -1, 0), NU(1, 0, 0, 0), NU(1, 0, 0, -1));
-        if (sy0 >= 0) d = fadd(d, A.we[2][py(g, Py, i, sy0, k)]);
-        if (sy1 >= 0) d = fsub(d, A.we[2][py(g, Py, i, sy1, k)]);
-        if (sz0 >= 0) d = fadd(d, A.we[5][pz(g, Pz, i, j, sz0)]);
-        if (sz1 >= 0) d = fsub(d, A.we[5][pz(g, Pz, i, j, sz1)]);
-        A.lf[3][c] = fadd(A.lf[3][c], d);
+
+    // ---- loads
+    // nu = CE * lE of component q at offset o, zero outside q's update mask
+    // (m: the mask at that cell; the load only where it is needed)
+    auto NU = [&](int q, bool need, bool m, int64_t o) {
+        return need && m ? fmul(__ldg(A.ce[q] + c + o), __ldg(A.lf[q] + c + o)) : 0.f;
+    };
+    auto W = [&](int q, bool m, int64_t p) { return m ? __ldg(A.we[q] + p) : 0.f; };
+    const float n0 = NU(0, h1 || h2, em(g, 0, i, j, k), 0), n1 = NU(1, h0 || h2, em(g, 1, i, j, k), 0),
+                n2 = NU(2, h0 || h1, em(g, 2, i, j, k), 0);
+    const float n2j = NU(2, h0, em(g, 2, i, j - 1, k), -Y), n1k = NU(1, h0, em(g, 1, i, j, k - 1), -1);  // hx
+    const float n0k = NU(0, h1, em(g, 0, i, j, k - 1), -1), n2i = NU(2, h1, em(g, 2, i - 1, j, k), -X);  // hy
+    const float n1i = NU(1, h2, em(g, 1, i - 1, j, k), -X), n0j = NU(0, h2, em(g, 0, i, j - 1, k), -Y);  // hz
+    // w_e of the slab nodes one below (+) and at this index (-), per component
+    // hx: ezy (y, psi 0 of e) and eyz (z, psi 1); hy: ezx (x, psi 1) and exz
+    // (z, psi 0); hz: eyx (x, psi 0) and exy (y, psi 1)
+    const float wx0 = W(2, h0 && sy0 >= 0, py(g, Py, i, sy0, k)), wx1 = W(2, h0 && sy1 >= 0, py(g, Py, i, sy1, k));
+    const float wx2 = W(5, h0 && sz0 >= 0, pz(g, Pz, i, j, sz0)), wx3 = W(5, h0 && sz1 >= 0, pz(g, Pz, i, j, sz1));
+    const float wy0 = W(1, h1 && sx0 >= 0, px(g, sx0, j, k)), wy1 = W(1, h1 && sx1 >= 0, px(g, sx1, j, k));
+    const float wy2 = W(4, h1 && sz0 >= 0, pz(g, Pz, i, j, sz0)), wy3 = W(4, h1 && sz1 >= 0, pz(g, Pz, i, j, sz1));
+    const float wz0 = W(0, h2 && sx0 >= 0, px(g, sx0, j, k)), wz1 = W(0, h2 && sx1 >= 0, px(g, sx1, j, k));
+    const float wz2 = W(3, h2 && sy0 >= 0, py(g, Py, i, sy0, k)), wz3 = W(3, h2 && sy1 >= 0, py(g, Py, i, sy1, k));
+    const float lh0 = h0 ? A.lf[3][c] : 0.f, lh1 = h1 ? A.lf[4][c] : 0.f, lh2 = h2 ? A.lf[5][c] : 0.f;
+
+    // ---- arithmetic and stores
+    if (h0) {  // hx
+        float d = curl4(n2, n2j, n1, n1k);
+        if (sy0 >= 0) d = fadd(d, wx0);
+        if (sy1 >= 0) d = fsub(d, wx1);
+        if (sz0 >= 0) d = fadd(d, wx2);
+        if (sz1 >= 0) d = fsub(d, wx3);
+        A.lf[3][c] = fadd(lh0, d);
     }
-    // hy: H source of ezx (x axis, psi 1) and exz (z axis, psi 0)
-    if (hm(1, i, j, k)) {
-        float d = curl4(NU(0, 0, 0, 0), NU(0, 0, 0, -1), NU(2, 0, 0, 0), NU(2, -1, 0, 0));
-        if (sx0 >= 0) d = fadd(d, A.we[1][px(g, sx0, j, k)]);
-        if (sx1 >= 0) d = fsub(d, A.we[1][px(g, sx1, j, k)]);
-        if (sz0 >= 0) d = fadd(d, A.we[4][pz(g, Pz, i, j, sz0)]);
-        if (sz1 >= 0) d = fsub(d, A.we[4][pz(g, Pz, i, j, sz1)]);
-        A.lf[4][c] = fadd(A.lf[4][c], d);
+    if (h1) {  // hy
+        float d = curl4(n0, n0k, n2, n2i);
+        if (sx0 >= 0) d = fadd(d, wy0);
+        if (sx1 >= 0) d = fsub(d, wy1);
+        if (sz0 >= 0) d = fadd(d, wy2);
+        if (sz1 >= 0) d = fsub(d, wy3);
+        A.lf[4][c] = fadd(lh1, d);
     }
-    // hz: H source of eyx (x axis, psi 0) and exy (y axis, psi 1)
-    if (hm(2, i, j, k)) {
-        float d = curl4(NU(1, 0, 0, 0), NU(1, -1, 0, 0), NU(0, 0, 0, 0), NU(0, 0, -1, 0));
-        if (sx0 >= 0) d = fadd(d, A.we[0][px(g, sx0, j, k)]);
-        if (sx1 >= 0) d = fsub(d, A.we[0][px(g, sx1, j, k)]);
-        if (sy0 >= 0) d = fadd(d, A.we[3][py(g, Py, i, sy0, k)]);
-        if (sy1 >= 0) d = fsub(d, A.we[3][py(g, Py, i, sy1, k)]);
-        A.lf[5][c] = fadd(A.lf[5][c], d);
+    if (h2) {  // hz
+        float d = curl4(n1, n1i, n0, n0j);
+        if (sx0 >= 0) d = fadd(d, wz0);
+        if (sx1 >= 0) d = fsub(d, wz1);
+        if (sy0 >= 0) d = fadd(d, wz2);
+        if (sy1 >= 0) d = fsub(d, wz3);
+        A.lf[5][c] = fadd(lh2, d);
     }
 }
 
@@ -372,9 +422,28 @@ __global__ void k_gather_points(Grid g, fdtd_points pts, fdtd_fields6 f, float *
     out[p] = c >= 0 ? f.f[pts.comp[p]][c] : __int_as_float(0x7fc00000);
 }
 
-// one thread walks the list so repeated points add in list order;
-// out-of-range points are skipped
+// Adds vals[p] to the cell of every point p, as a walk of the list in order
+// would (out-of-range points are skipped).  Lists of up to kAddThreads
+// points: one thread per point, one block.  A point whose cell and component
+// an earlier point also names is skipped by its thread; the thread of the
+// first such point adds the values of all of them in list order.
+constexpr int kAddThreads = 1024;
 __global__ void k_add_points(Grid g, fdtd_points pts, fdtd_fields6 f, const float *vals) {
+    const int p = threadIdx.x;
+    if (blockIdx.x != 0 || p >= pts.n) return;
+    const int64_t c = point_offset(g, pts, p);
+    if (c < 0) return;
+    const int q = pts.comp[p];
+    for (int r = 0; r < p; r++)
+        if (pts.comp[r] == q && point_offset(g, pts, r) == c) return;
+    float *fp = f.f[q] + c;
+    float v = *fp;
+    for (int r = p; r < pts.n; r++)
+        if (pts.comp[r] == q && point_offset(g, pts, r) == c) v = fadd(v, vals[r]);
+    *fp = v;
+}
+// longer lists: one thread walks the list
+__global__ void k_add_points_walk(Grid g, fdtd_points pts, fdtd_fields6 f, const float *vals) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     for (int p = 0; p < pts.n; p++) {
         const int64_t c = point_offset(g, pts, p);
@@ -382,6 +451,13 @@ __global__ void k_add_points(Grid g, fdtd_points pts, fdtd_fields6 f, const floa
         float *fp = f.f[pts.comp[p]] + c;
         *fp = fadd(*fp, vals[p]);
     }
+}
+static void add_points(const Grid &g, const fdtd_points &pts, const fdtd_fields6 &f, const float *vals,
+                       cudaStream_t st) {
+    if (pts.n <= kAddThreads)
+        k_add_points<<<1, (pts.n + 31) / 32 * 32, 0, st>>>(g, pts, f, vals);
+    else
+        k_add_points_walk<<<1, 32, 0, st>>>(g, pts, f, vals);
 }
 
 static dim3 cells(const Grid &g) {
@@ -393,7 +469,7 @@ static void launch_slab(const Grid &g, int P, bool e, const Args &A, cudaStream_
     dim3 grid;
     if (AX == 0) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)g.ny, (unsigned)(2 * P));
     else if (AX == 1) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)(2 * P), (unsigned)g.nx);
-    else grid = dim3((unsigned)((g.nx * g.ny * 2 * P + kB - 1) / kB));
+    else grid = dim3((unsigned)((g.ny * 2 * P + kB - 1) / kB), (unsigned)g.nx);
     if (e) k_adj_epsi<AX><<<grid, kB, 0, st>>>(A);
     else k_adj_hpsi<AX><<<grid, kB, 0, st>>>(A);
 }
@@ -476,7 +552,7 @@ static int adjoint_step(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adj
         if (!mon_grad) return FDTD_ERR_ARG;
         fdtd_fields6 lf;
         for (int q = 0; q < 6; q++) lf.f[q] = s->lf[q];
-        k_add_points<<<1, 32, 0, st>>>(g, *mon, lf, mon_grad);
+        add_points(g, *mon, lf, mon_grad, st);
     }
     if (A.P[0]) launch_slab<0>(g, A.P[0], false, A, st);
     if (A.P[1]) launch_slab<1>(g, A.P[1], false, A, st);
@@ -656,7 +732,7 @@ int fdtd_add_points_f32(const fdtd_grid *gp, const fdtd_points *pts, float *cons
     if (!f || !vals) return FDTD_ERR_ARG;
     fdtd_fields6 ff;
     for (int q = 0; q < 6; q++) ff.f[q] = f[q];
-    k_add_points<<<1, 32, 0, as_stream(stream)>>>(g, *pts, ff, vals);
+    add_points(g, *pts, ff, vals, as_stream(stream));
     return check_launch();
 }
 

@@ -46,6 +46,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <functional>
+#include <queue>
 #include <vector>
 
 #include "common.cuh"
@@ -970,6 +972,41 @@ static int map3(EncodeFn enc, CUtensorMap *m, const float *ptr, const Grid &g, i
     return r == CUDA_SUCCESS ? FDTD_OK : FDTD_ERR_CUDA;
 }
 
+// x planes per work item when the caller leaves the choice to the plan: of
+// the chunks 48 .. 256 (steps of 8), the one whose greedy schedule of a
+// pass's items over the resident CTAs ends first.  The queue hands items out
+// x chunk by x chunk; an item costs its planes (x-slab planes, which carry
+// the CPML terms, twice) plus the 6 iterations that fill the pipeline.  The
+// largest chunk wins ties (fewer fills).
+static int choose_x_chunk(int nx, int64_t tiles, int slots, int pf, int pb) {
+    int best = std::min(nx, 128);
+    int64_t best_t = -1;
+    std::vector<int64_t> heap;
+    int last = -1;
+    for (int xc = 256; xc >= 48; xc -= 8) {
+        const int c = std::min(xc, nx);
+        if (c == last) continue;  // chunks past nx are all the whole grid
+        last = c;
+        heap.assign((size_t)slots, 0);
+        for (int x0 = 0; x0 < nx; x0 += c) {
+            const int x1 = std::min(nx, x0 + c);
+            int64_t cost = 6;
+            for (int i = x0; i < x1; i++) cost += ((pf > 0 && i <= pf + 1) || (pb > 0 && i >= nx - pb - 2)) ? 2 : 1;
+            for (int64_t t = 0; t < tiles; t++) {  // the CTA free first takes the item
+                std::pop_heap(heap.begin(), heap.end(), std::greater<int64_t>());
+                heap.back() += cost;
+                std::push_heap(heap.begin(), heap.end(), std::greater<int64_t>());
+            }
+        }
+        const int64_t t = *std::max_element(heap.begin(), heap.end());
+        if (best_t < 0 || t < best_t) {
+            best_t = t;
+            best = c;
+        }
+    }
+    return best;
+}
+
 struct fdtd_symp_plan {
     Grid g;
     Maps maps[2];
@@ -979,6 +1016,9 @@ struct fdtd_symp_plan {
     std::vector<int32_t> src_ijk;  // host copy of the source positions
     int slots;                     // resident CTAs of the pair kernel (SMs x CTAs per SM)
     int cur;
+    bool auto_chunk;               // x_chunk chosen per tiling (the caller passed 0)
+    int64_t chunk_key[4] = {-1, -1, -1, -1};  // tiling the cached choice was made for
+    int chunk_val = 0;
 };
 
 extern "C" {
@@ -1009,6 +1049,7 @@ int fdtd_symp_pair_plan_create(fdtd_symp_plan **out, const fdtd_grid *gp, const 
     p.ntz = (int32_t)((g.nz + TZ - 1) / TZ);
     p.nty = (int32_t)((g.ny + TY - 1) / TY);
     if (x_chunk < 0) { delete pl; return FDTD_ERR_ARG; }
+    pl->auto_chunk = x_chunk == 0;  // chosen per tiling at run time; 128 until then
     p.x_chunk = (int32_t)std::min<int64_t>(x_chunk > 0 ? x_chunk : 128, g.nx);
     p.nxc = (int32_t)((g.nx + p.x_chunk - 1) / p.x_chunk);
     for (int q = 0; q < 3; q++) p.ce[q] = s->ce[q];
@@ -1139,6 +1180,15 @@ int fdtd_symp_pair_run(fdtd_symp_plan *pl, const fdtd_cpml *ch_tabs_a, const fdt
     // [k_lo, k_hi)
     p.kt0 = p.k_lo / TZ * TZ;
     p.ntz_in = p.k_hi > p.k_lo ? (p.k_hi - p.kt0 + TZ - 1) / TZ : 0;
+    if (pl->auto_chunk && p.nty_in > 0 && p.ntz_in > 0) {
+        const int64_t key[4] = {p.nty_in, p.ntz_in, pf(0), pb(0)};
+        if (!std::equal(key, key + 4, pl->chunk_key)) {
+            pl->chunk_val = choose_x_chunk(p.nx, (int64_t)p.nty_in * p.ntz_in, pl->slots, pf(0), pb(0));
+            std::copy(key, key + 4, pl->chunk_key);
+        }
+        p.x_chunk = pl->chunk_val;
+        p.nxc = (p.nx + p.x_chunk - 1) / p.x_chunk;
+    }
     // the edge shell: rows outside [j_lo, j_hi), then the columns outside
     // [k_lo, k_hi) of those rows (every x plane)
     Edge eb{};

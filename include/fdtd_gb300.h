@@ -297,7 +297,8 @@ typedef struct {
 
 typedef struct fdtd_symp_plan fdtd_symp_plan;
 
-/* x_chunk: x planes per work item (0: 128); cur: buffer holding the state;
+/* x_chunk: x planes per work item (0: the plan picks it per tiling, from a model of the
+ * work-queue schedule); cur: buffer holding the state;
  * status_dev: device int32 set non-zero when a bounded wait expires;
  * queue_dev: device int32[2], zero at plan creation, the work queue the
  * CTAs draw items from (the kernel leaves it zero after each run; runs of

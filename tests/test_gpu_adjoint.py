@@ -270,3 +270,36 @@ def test_gradient_vs_finite_differences(F):
         errs.append(abs(fd - float(g[c])) / max(abs(fd), 1e-30))
     print("FD relative errors", ["%.2e" % e for e in errs])
     assert max(errs) < 1e-3, errs
+
+
+@pytest.mark.parametrize("n", [40, 1500])
+def test_add_points_repeats_in_list_order(F, n):
+    """fdtd_add_points_f32 equals a walk of the list in order (FP32 adds),
+    with repeated (cell, component) pairs, one cell under several components
+    and out-of-range points; 40 points take the one-thread-per-point kernel,
+    1500 the list walk."""
+    from fdtd_accelerate_gb300 import _native as N
+    shape = (6, 5, 8)
+    rng = np.random.default_rng(3 + n)
+    f = [torch.tensor(rng.standard_normal(shape).astype(np.float32), device="cuda") for _ in range(6)]
+    ijk = np.stack([rng.integers(0, s, n) for s in shape], axis=1).astype(np.int32)
+    comp = rng.integers(0, 6, n).astype(np.int32)
+    ijk[1::7] = ijk[0]                           # many repeats of one point, mixed components
+    ijk[n // 2 + 1] = (9, 0, 0)                  # out of range: skipped
+    vals = rng.standard_normal(n).astype(np.float32)
+    want = [t.cpu().numpy().copy() for t in f]
+    for p in range(n):
+        i, j, k = ijk[p]
+        if i < shape[0] and j < shape[1] and k < shape[2]:
+            want[comp[p]][i, j, k] = np.float32(want[comp[p]][i, j, k] + vals[p])
+    d_ijk = torch.tensor(ijk.ravel(), device="cuda")
+    d_comp = torch.tensor(comp, device="cuda")
+    d_vals = torch.tensor(vals, device="cuda")
+    pts = N.Points(n, d_ijk.data_ptr(), d_comp.data_ptr())
+    g = N.Grid(*shape, shape[1] * shape[2], shape[2])
+    fp = (C.c_void_p * 6)(*[t.data_ptr() for t in f])
+    rc = N.lib().fdtd_add_points_f32(C.byref(g), C.byref(pts), fp, C.c_void_p(d_vals.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    for q in range(6):
+        np.testing.assert_array_equal(f[q].cpu().numpy(), want[q])

@@ -25,6 +25,7 @@
 
 #include "common.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace fdtd {
@@ -50,42 +51,9 @@ struct Args {
     int64_t gb0[3], gb1[3];
 };
 
-// dense psi indices: x (2P, ny, nz), y (nx, 2P, nz), z (nx, ny, 2P)
-__device__ __forceinline__ int64_t px(const Grid &g, int64_t s, int64_t j, int64_t k) { return (s * g.ny + j) * g.nz + k; }
-__device__ __forceinline__ int64_t py(const Grid &g, int P, int64_t i, int64_t s, int64_t k) {
-    return (i * 2 * P + s) * g.nz + k;
-}
-__device__ __forceinline__ int64_t pz(const Grid &g, int P, int64_t i, int64_t j, int64_t s) {
-    return (i * g.ny + j) * 2 * P + s;
-}
-
-// node index -> slab index (or -1) on an enabled face; inverse of slab_node_e/h
-__device__ __forceinline__ int slab_of_e(int64_t x, int P, int64_t n, int front, int back) {
-    if (P == 0) return -1;
-    if (front && x >= 1 && x <= P) return (int)(x - 1);
-    if (back && x >= n - P - 1 && x <= n - 2) return (int)(P + x - (n - P - 1));
-    return -1;
-}
-__device__ __forceinline__ int slab_of_h(int64_t x, int P, int64_t n, int front, int back) {
-    if (P == 0) return -1;
-    if (front && x >= 1 && x <= P) return (int)(x - 1);
-    if (back && x >= n - P && x <= n - 1) return (int)(P + x - (n - P));
-    return -1;
-}
-
-// update masks (2nd_order-Yee/Numpy/fdtd3d.py:4-13)
-__device__ __forceinline__ bool em(const Grid &g, int q, int64_t i, int64_t j, int64_t k) {
-    return q == 0 ? (j < g.ny - 1 && k < g.nz - 1) : q == 1 ? (i < g.nx - 1 && k < g.nz - 1) : (i < g.nx - 1 && j < g.ny - 1);
-}
-__device__ __forceinline__ bool hm(int q, int64_t i, int64_t j, int64_t k) {
-    return q == 0 ? (j > 0 && k > 0) : q == 1 ? (i > 0 && k > 0) : (i > 0 && j > 0);
-}
-
-// ---------------------------------------------------------------------------
-// 1. transpose of cpml_h on one axis: lpsi_h <- b*mu, w_h <- adjoint of d
-//    (mu = lpsi + sigma*0.5*lH_target).  Invalid elements get w = 0.
-//    psi order per axis: x (hyx, hzx), y (hzy, hxy), z (hxz, hyz); sigma (+, -)
-// ---------------------------------------------------------------------------
+// transpose of one psi recursion at one slab element: mu = lpsi + sigma *
+// coef * lt (lt the adjoint of the component the psi corrects), lpsi <- b*mu,
+// w <- sigma*km1*coef*lt + a*mu (the adjoint of the psi-driving difference)
 __device__ __forceinline__ void adj_psi(float &lpsi, float &w, float lt, float coef, int sigma, float b, float a,
                                         float km1) {
     const float h = fmul(coef, lt);
@@ -95,109 +63,194 @@ __device__ __forceinline__ void adj_psi(float &lpsi, float &w, float lt, float c
     w = fadd(sigma > 0 ? t : -t, fmul(a, mu));
 }
 
-template <int AX>
-__global__ void __launch_bounds__(kB) k_adj_hpsi(Args A) {
-    const Grid &g = A.g;
-    const int P = A.P[AX];
-    int64_t i, j, k, s, p;
-    if (AX == 0) {
-        k = (int64_t)blockIdx.x * kB + threadIdx.x; j = blockIdx.y; s = blockIdx.z;
-        if (k >= g.nz) return;
-        i = slab_node_h(s, P, g.nx);
-        p = px(g, s, j, k);
-    } else if (AX == 1) {
-        k = (int64_t)blockIdx.x * kB + threadIdx.x; s = blockIdx.y; i = blockIdx.z;
-        if (k >= g.nz) return;
-        j = slab_node_h(s, P, g.ny);
-        p = py(g, P, i, s, k);
-    } else {  // blockIdx.y = i; u = j * 2P + s within the plane
-        const uint32_t u = blockIdx.x * kB + threadIdx.x, w = 2u * (uint32_t)P;
-        if (u >= (uint32_t)g.ny * w) return;
-        i = blockIdx.y;
-        j = u / w;
-        s = u - (uint32_t)j * w;
-        k = slab_node_h(s, P, g.nz);
-        p = i * g.ny * w + u;
+// ---------------------------------------------------------------------------
+// 1. and 3. The psi transposes of one family, all three axes in one launch
+//    (E false: transpose of cpml_h, lpsi_h <- b*mu, w_h <- adjoint of d with
+//    mu = lpsi + sigma*0.5*lH_target; E true: transpose of cpml_e, nu =
+//    CE*lE_target, mu = lpsi + sigma*nu, lpsi_e <- b*mu, w_e <- sigma*km1*nu +
+//    a*mu).  Invalid elements get w = 0.  Blocks [nb[a-1], nb[a]) take axis a,
+//    kB consecutive elements of its dense psi array each; indices in I.
+//    psi order per axis: x (y, z targets), y (z, x), z (x, y); H sigma (+, -),
+//    E sigma (-, +).
+// ---------------------------------------------------------------------------
+struct PsiBlocks {
+    int32_t nb[3];  // cumulative block counts of the x, y and z slabs
+};
+template <bool E, typename I>
+__global__ void __launch_bounds__(kB) k_adj_psi3(Args A, PsiBlocks R) {
+    const int b = blockIdx.x;
+    const int ax = b < R.nb[0] ? 0 : (b < R.nb[1] ? 1 : 2);
+    const I nx = A.g.nx, ny = A.g.ny, nz = A.g.nz;
+    const int P = A.P[ax];
+    const I tp = 2 * P;
+    const I t = (I)(b - (ax ? R.nb[ax - 1] : 0)) * kB + threadIdx.x;  // element of the dense psi array
+    I i, j, k;
+    int s;
+    auto node = [&](int sl, I n) { return (I)(E ? slab_node_e(sl, P, n) : slab_node_h(sl, P, n)); };
+    if (ax == 0) {  // (2P, ny, nz)
+        if (t >= tp * ny * nz) return;
+        k = t % nz;
+        const I r = t / nz;
+        j = r % ny;
+        s = (int)(r / ny);
+        i = node(s, nx);
+    } else if (ax == 1) {  // (nx, 2P, nz)
+        if (t >= nx * tp * nz) return;
+        k = t % nz;
+        const I r = t / nz;
+        s = (int)(r % tp);
+        i = r / tp;
+        j = node(s, ny);
+    } else {  // (nx, ny, 2P)
+        if (t >= nx * ny * tp) return;
+        s = (int)(t % tp);
+        const I r = t / tp;
+        j = r % ny;
+        i = r / ny;
+        k = node(s, nz);
     }
-    if (!(s < P ? A.front[AX] : A.back[AX])) return;
-    const int64_t c = i * g.sx + j * g.sy + k;
-    const float b = A.bh[AX][s], a = A.ah[AX][s], km1 = A.kh[AX][s];
-    // (target H component, validity) of psi1 / psi2 on this axis
-    const int t1 = AX == 0 ? 1 : AX == 1 ? 2 : 0;   // hy, hz, hx
-    const int t2 = AX == 0 ? 2 : AX == 1 ? 0 : 1;   // hz, hx, hy
-    const bool v1 = AX == 0 ? k > 0 : AX == 1 ? i > 0 : j > 0;
-    const bool v2 = AX == 0 ? j > 0 : AX == 1 ? k > 0 : i > 0;
-    float *lp1 = A.lph[2 * AX], *lp2 = A.lph[2 * AX + 1];
-    float *w1 = A.wh[2 * AX], *w2 = A.wh[2 * AX + 1];
-    if (v1) {
-        float l = lp1[p], w;
-        adj_psi(l, w, A.lf[3 + t1][c], 0.5f, +1, b, a, km1);
-        lp1[p] = l;
-        w1[p] = w;
+    if (!(s < P ? A.front[ax] : A.back[ax])) return;
+    const I c = i * (I)A.g.sx + j * (I)A.g.sy + k;
+    const float b_ = E ? A.be[ax][s] : A.bh[ax][s], a = E ? A.ae[ax][s] : A.ah[ax][s],
+                km1 = E ? A.ke[ax][s] : A.kh[ax][s];
+    // target components of psi1 / psi2 on this axis (x: y, z; y: z, x; z: x, y)
+    // and their validity (the update masks of the target family)
+    const int t1 = ax == 0 ? 1 : ax == 1 ? 2 : 0, t2 = ax == 0 ? 2 : ax == 1 ? 0 : 1;
+    bool v1, v2;
+    if (E) {
+        v1 = ax == 0 ? k < nz - 1 : ax == 1 ? i < nx - 1 : j < ny - 1;
+        v2 = ax == 0 ? j < ny - 1 : ax == 1 ? k < nz - 1 : i < nx - 1;
     } else {
-        w1[p] = 0.f;
+        v1 = ax == 0 ? k > 0 : ax == 1 ? i > 0 : j > 0;
+        v2 = ax == 0 ? j > 0 : ax == 1 ? k > 0 : i > 0;
+    }
+    float *lp1 = E ? A.lpe[2 * ax] : A.lph[2 * ax], *lp2 = E ? A.lpe[2 * ax + 1] : A.lph[2 * ax + 1];
+    float *w1 = E ? A.we[2 * ax] : A.wh[2 * ax], *w2 = E ? A.we[2 * ax + 1] : A.wh[2 * ax + 1];
+    if (v1) {
+        float l = lp1[t], w;
+        if (E) adj_psi(l, w, A.lf[t1][c], A.ce[t1][c], -1, b_, a, km1);
+        else adj_psi(l, w, A.lf[3 + t1][c], 0.5f, +1, b_, a, km1);
+        lp1[t] = l;
+        w1[t] = w;
+    } else {
+        w1[t] = 0.f;
     }
     if (v2) {
-        float l = lp2[p], w;
-        adj_psi(l, w, A.lf[3 + t2][c], 0.5f, -1, b, a, km1);
-        lp2[p] = l;
-        w2[p] = w;
+        float l = lp2[t], w;
+        if (E) adj_psi(l, w, A.lf[t2][c], A.ce[t2][c], +1, b_, a, km1);
+        else adj_psi(l, w, A.lf[3 + t2][c], 0.5f, -1, b_, a, km1);
+        lp2[t] = l;
+        w2[t] = w;
     } else {
-        w2[p] = 0.f;
+        w2[t] = 0.f;
     }
 }
 
 // ---------------------------------------------------------------------------
-// 2. reverse H part on E cells + gradient.  One thread per cell.  Every load
-//    comes first, then the arithmetic, then the stores: a store could alias a
-//    later load as far as the compiler knows, and loads placed after stores
-//    would wait for them instead of overlapping.
+// Index helpers of the cell kernels, in the index type I of the launch
+// (int32_t when every field and psi array has fewer than 2^31 elements):
+// dense psi offsets, slab indices of a node, and whether any slab node of an
+// axis sits at index x (then the cell takes the CPML terms).
 // ---------------------------------------------------------------------------
+template <typename I>
+__device__ __forceinline__ I psi_x(int ny, int nz, int s, int j, int k) { return ((I)s * ny + j) * nz + k; }
+template <typename I>
+__device__ __forceinline__ I psi_y(int nz, int P, int i, int s, int k) { return ((I)i * (2 * P) + s) * nz + k; }
+template <typename I>
+__device__ __forceinline__ I psi_z(int ny, int P, int i, int j, int s) { return ((I)i * ny + j) * (2 * P) + s; }
+__device__ __forceinline__ int slab_e(int x, int P, int n, int front, int back) {
+    if (P == 0) return -1;
+    if (front && x >= 1 && x <= P) return x - 1;
+    if (back && x >= n - P - 1 && x <= n - 2) return P + x - (n - P - 1);
+    return -1;
+}
+__device__ __forceinline__ int slab_h(int x, int P, int n, int front, int back) {
+    if (P == 0) return -1;
+    if (front && x >= 1 && x <= P) return x - 1;
+    if (back && x >= n - P && x <= n - 1) return P + x - (n - P);
+    return -1;
+}
+// k_adj_e reads the H nodes x and x+1 and the E node x: front nodes 1..P,
+// back H nodes n-P..n-1 and E nodes n-P-1..n-2
+__device__ __forceinline__ bool near_e(const Args &A, int a, int x, int n) {
+    const int P = A.P[a];
+    return P > 0 && ((A.front[a] && x <= P) || (A.back[a] && x >= n - P - 1));
+}
+// k_adj_h reads the E nodes x-1 and x
+__device__ __forceinline__ bool near_h(const Args &A, int a, int x, int n) {
+    const int P = A.P[a];
+    return P > 0 && ((A.front[a] && x <= P + 1) || (A.back[a] && x >= n - P - 1));
+}
+
+// ---------------------------------------------------------------------------
+// 2. reverse H part on E cells + gradient.  One thread per cell.  Every load
+//    comes first, then the arithmetic, then the stores (a store could alias a
+//    later load as far as the compiler knows, and loads placed after stores
+//    would wait for them).  Cells with no CPML node skip the slab code.
+// ---------------------------------------------------------------------------
+template <typename I>
 __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
-    const Grid &g = A.g;
-    const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
-    const int64_t j = blockIdx.y, i = blockIdx.z;
-    if (k >= g.nz) return;
-    const int64_t c = i * g.sx + j * g.sy + k, X = g.sx, Y = g.sy;
-    const bool e0 = em(g, 0, i, j, k), e1 = em(g, 1, i, j, k), e2 = em(g, 2, i, j, k);
-    // slab indices of this cell's nodes (H-node form for the w_h gather,
-    // E-node form for the gradient's psi terms)
-    const int sxh0 = slab_of_h(i, A.P[0], g.nx, A.front[0], A.back[0]);
-    const int sxh1 = slab_of_h(i + 1, A.P[0], g.nx, A.front[0], A.back[0]);
-    const int syh0 = slab_of_h(j, A.P[1], g.ny, A.front[1], A.back[1]);
-    const int syh1 = slab_of_h(j + 1, A.P[1], g.ny, A.front[1], A.back[1]);
-    const int szh0 = slab_of_h(k, A.P[2], g.nz, A.front[2], A.back[2]);
-    const int szh1 = slab_of_h(k + 1, A.P[2], g.nz, A.front[2], A.back[2]);
-    const int sxe = slab_of_e(i, A.P[0], g.nx, A.front[0], A.back[0]);
-    const int sye = slab_of_e(j, A.P[1], g.ny, A.front[1], A.back[1]);
-    const int sze = slab_of_e(k, A.P[2], g.nz, A.front[2], A.back[2]);
-    const int Py = A.P[1], Pz = A.P[2];
+    const int k = blockIdx.x * kB + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    const int nx = (int)A.g.nx, ny = (int)A.g.ny, nz = (int)A.g.nz;
+    if (k >= nz) return;
+    const I X = (I)A.g.sx, Y = (I)A.g.sy, c = (I)i * X + (I)j * Y + k;
+    // E update masks (2nd_order-Yee/Numpy/fdtd3d.py:10-13)
+    const bool e0 = j < ny - 1 && k < nz - 1, e1 = i < nx - 1 && k < nz - 1, e2 = i < nx - 1 && j < ny - 1;
     const bool gin = !A.gbox || (i >= A.gb0[0] && i < A.gb1[0] && j >= A.gb0[1] && j < A.gb1[1] &&
                                  k >= A.gb0[2] && k < A.gb1[2]);
+    const int Py = A.P[1], Pz = A.P[2];
 
     // ---- loads
-    auto L = [&](const float *f, bool m, int64_t o) { return m ? __ldg(f + c + o) : 0.f; };
-    auto W = [&](int q, bool m, int64_t p) { return m ? __ldg(A.wh[q] + p) : 0.f; };
+    auto L = [&](const float *f, bool m, I o) { return m ? __ldg(f + c + o) : 0.f; };
     const float *lhx = A.lf[3], *lhy = A.lf[4], *lhz = A.lf[5];
     // adjoint H through the H update masks: the cell, and the +1 neighbours
-    // each E component differentiates (their loads only where it is updated)
+    // each E component differentiates (loaded only where it is updated)
     const float hz0 = L(lhz, i > 0 && j > 0, 0), hy0 = L(lhy, i > 0 && k > 0, 0), hx0 = L(lhx, j > 0 && k > 0, 0);
     const float hzj = L(lhz, e0 && i > 0, Y), hyk = L(lhy, e0 && i > 0, 1);  // ex
     const float hxk = L(lhx, e1 && j > 0, 1), hzi = L(lhz, e1 && j > 0, X);  // ey
     const float hyi = L(lhy, e2 && k > 0, X), hxj = L(lhx, e2 && k > 0, Y);  // ez
-    // w_h of the slab nodes at this index (+) and one above (-), per component
-    // ex: hzy (y, psi 0 of h) and hyz (z, psi 1); ey: hzx (x, psi 1) and hxz
-    // (z, psi 0); ez: hyx (x, psi 0) and hxy (y, psi 1)
-    const float wx0 = W(2, e0 && syh0 >= 0, py(g, Py, i, syh0, k)), wx1 = W(2, e0 && syh1 >= 0, py(g, Py, i, syh1, k));
-    const float wx2 = W(5, e0 && szh0 >= 0, pz(g, Pz, i, j, szh0)), wx3 = W(5, e0 && szh1 >= 0, pz(g, Pz, i, j, szh1));
-    const float wy0 = W(1, e1 && sxh0 >= 0, px(g, sxh0, j, k)), wy1 = W(1, e1 && sxh1 >= 0, px(g, sxh1, j, k));
-    const float wy2 = W(4, e1 && szh0 >= 0, pz(g, Pz, i, j, szh0)), wy3 = W(4, e1 && szh1 >= 0, pz(g, Pz, i, j, szh1));
-    const float wz0 = W(0, e2 && sxh0 >= 0, px(g, sxh0, j, k)), wz1 = W(0, e2 && sxh1 >= 0, px(g, sxh1, j, k));
-    const float wz2 = W(3, e2 && syh0 >= 0, py(g, Py, i, syh0, k)), wz3 = W(3, e2 && syh1 >= 0, py(g, Py, i, syh1, k));
     const float le0 = e0 ? A.lf[0][c] : 0.f, le1 = e1 ? A.lf[1][c] : 0.f, le2 = e2 ? A.lf[2][c] : 0.f;
+    // slab nodes: H-node form at this index and one above (the w_h gathers),
+    // E-node form at this index (the gradient's psi terms); -1 off the slabs
+    int sxh0 = -1, sxh1 = -1, syh0 = -1, syh1 = -1, szh0 = -1, szh1 = -1, sxe = -1, sye = -1, sze = -1;
+    // w_h per component, (+) at this index and (-) one above: ex: hzy (y, psi 0
+    // of h) and hyz (z, psi 1); ey: hzx (x, psi 1) and hxz (z, psi 0); ez: hyx
+    // (x, psi 0) and hxy (y, psi 1)
+    float wx0 = 0.f, wx1 = 0.f, wx2 = 0.f, wx3 = 0.f, wy0 = 0.f, wy1 = 0.f, wy2 = 0.f, wy3 = 0.f;
+    float wz0 = 0.f, wz1 = 0.f, wz2 = 0.f, wz3 = 0.f;
+    if (near_e(A, 0, i, nx) || near_e(A, 1, j, ny) || near_e(A, 2, k, nz)) {
+        sxh0 = slab_h(i, A.P[0], nx, A.front[0], A.back[0]);
+        sxh1 = slab_h(i + 1, A.P[0], nx, A.front[0], A.back[0]);
+        syh0 = slab_h(j, Py, ny, A.front[1], A.back[1]);
+        syh1 = slab_h(j + 1, Py, ny, A.front[1], A.back[1]);
+        szh0 = slab_h(k, Pz, nz, A.front[2], A.back[2]);
+        szh1 = slab_h(k + 1, Pz, nz, A.front[2], A.back[2]);
+        sxe = slab_e(i, A.P[0], nx, A.front[0], A.back[0]);
+        sye = slab_e(j, Py, ny, A.front[1], A.back[1]);
+        sze = slab_e(k, Pz, nz, A.front[2], A.back[2]);
+        auto W = [&](int q, bool m, I p) { return m ? __ldg(A.wh[q] + p) : 0.f; };
+        if (e0) {
+            wx0 = W(2, syh0 >= 0, psi_y<I>(nz, Py, i, syh0, k));
+            wx1 = W(2, syh1 >= 0, psi_y<I>(nz, Py, i, syh1, k));
+            wx2 = W(5, szh0 >= 0, psi_z<I>(ny, Pz, i, j, szh0));
+            wx3 = W(5, szh1 >= 0, psi_z<I>(ny, Pz, i, j, szh1));
+        }
+        if (e1) {
+            wy0 = W(1, sxh0 >= 0, psi_x<I>(ny, nz, sxh0, j, k));
+            wy1 = W(1, sxh1 >= 0, psi_x<I>(ny, nz, sxh1, j, k));
+            wy2 = W(4, szh0 >= 0, psi_z<I>(ny, Pz, i, j, szh0));
+            wy3 = W(4, szh1 >= 0, psi_z<I>(ny, Pz, i, j, szh1));
+        }
+        if (e2) {
+            wz0 = W(0, sxh0 >= 0, psi_x<I>(ny, nz, sxh0, j, k));
+            wz1 = W(0, sxh1 >= 0, psi_x<I>(ny, nz, sxh1, j, k));
+            wz2 = W(3, syh0 >= 0, psi_y<I>(nz, Py, i, syh0, k));
+            wz3 = W(3, syh1 >= 0, psi_y<I>(nz, Py, i, syh1, k));
+        }
+    }
     // gradient: forward H entering the step (unmasked), forward E-psi, accumulators
     float Hz0 = 0.f, Hzj = 0.f, Hzi = 0.f, Hy0 = 0.f, Hyk = 0.f, Hyi = 0.f, Hx0 = 0.f, Hxk = 0.f, Hxj = 0.f;
-    float pe3 = 0.f, pe4 = 0.f, pe0 = 0.f, pe5 = 0.f, pe1 = 0.f, pe2 = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    float pe0 = 0.f, pe1 = 0.f, pe2 = 0.f, pe3 = 0.f, pe4 = 0.f, pe5 = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f;
     if (gin) {
         const float *hx = A.hp[0], *hy = A.hp[1], *hz = A.hp[2];
         Hz0 = __ldg(hz + c);
@@ -206,22 +259,22 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
         if (e0) {
             Hzj = __ldg(hz + c + Y);
             Hyk = __ldg(hy + c + 1);
-            if (sye >= 0) pe3 = __ldg(A.pe[3] + py(g, Py, i, sye, k));
-            if (sze >= 0) pe4 = __ldg(A.pe[4] + pz(g, Pz, i, j, sze));
+            if (sye >= 0) pe3 = __ldg(A.pe[3] + psi_y<I>(nz, Py, i, sye, k));
+            if (sze >= 0) pe4 = __ldg(A.pe[4] + psi_z<I>(ny, Pz, i, j, sze));
             g0 = A.gce[0][c];
         }
         if (e1) {
             Hxk = __ldg(hx + c + 1);
             Hzi = __ldg(hz + c + X);
-            if (sxe >= 0) pe0 = __ldg(A.pe[0] + px(g, sxe, j, k));
-            if (sze >= 0) pe5 = __ldg(A.pe[5] + pz(g, Pz, i, j, sze));
+            if (sxe >= 0) pe0 = __ldg(A.pe[0] + psi_x<I>(ny, nz, sxe, j, k));
+            if (sze >= 0) pe5 = __ldg(A.pe[5] + psi_z<I>(ny, Pz, i, j, sze));
             g1 = A.gce[1][c];
         }
         if (e2) {
             Hyi = __ldg(hy + c + X);
             Hxj = __ldg(hx + c + Y);
-            if (sxe >= 0) pe1 = __ldg(A.pe[1] + px(g, sxe, j, k));
-            if (sye >= 0) pe2 = __ldg(A.pe[2] + py(g, Py, i, sye, k));
+            if (sxe >= 0) pe1 = __ldg(A.pe[1] + psi_x<I>(ny, nz, sxe, j, k));
+            if (sye >= 0) pe2 = __ldg(A.pe[2] + psi_y<I>(nz, Py, i, sye, k));
             g2 = A.gce[2][c];
         }
     }
@@ -278,103 +331,65 @@ __global__ void __launch_bounds__(kB) k_adj_e(Args A) {
 }
 
 // ---------------------------------------------------------------------------
-// 3. transpose of cpml_e on one axis: nu = CE*lE_target, mu = lpsi + sigma*nu,
-//    lpsi_e <- b*mu, w_e <- sigma*km1*nu + a*mu.
-//    psi order per axis: x (eyx -, ezx +), y (ezy -, exy +), z (exz -, eyz +)
-// ---------------------------------------------------------------------------
-template <int AX>
-__global__ void __launch_bounds__(kB) k_adj_epsi(Args A) {
-    const Grid &g = A.g;
-    const int P = A.P[AX];
-    int64_t i, j, k, s, p;
-    if (AX == 0) {
-        k = (int64_t)blockIdx.x * kB + threadIdx.x; j = blockIdx.y; s = blockIdx.z;
-        if (k >= g.nz) return;
-        i = slab_node_e(s, P, g.nx);
-        p = px(g, s, j, k);
-    } else if (AX == 1) {
-        k = (int64_t)blockIdx.x * kB + threadIdx.x; s = blockIdx.y; i = blockIdx.z;
-        if (k >= g.nz) return;
-        j = slab_node_e(s, P, g.ny);
-        p = py(g, P, i, s, k);
-    } else {  // blockIdx.y = i; u = j * 2P + s within the plane
-        const uint32_t u = blockIdx.x * kB + threadIdx.x, w = 2u * (uint32_t)P;
-        if (u >= (uint32_t)g.ny * w) return;
-        i = blockIdx.y;
-        j = u / w;
-        s = u - (uint32_t)j * w;
-        k = slab_node_e(s, P, g.nz);
-        p = i * g.ny * w + u;
-    }
-    if (!(s < P ? A.front[AX] : A.back[AX])) return;
-    const int64_t c = i * g.sx + j * g.sy + k;
-    const float b = A.be[AX][s], a = A.ae[AX][s], km1 = A.ke[AX][s];
-    const int t1 = AX == 0 ? 1 : AX == 1 ? 2 : 0;   // ey, ez, ex
-    const int t2 = AX == 0 ? 2 : AX == 1 ? 0 : 1;   // ez, ex, ey
-    const bool v1 = AX == 0 ? k < g.nz - 1 : AX == 1 ? i < g.nx - 1 : j < g.ny - 1;
-    const bool v2 = AX == 0 ? j < g.ny - 1 : AX == 1 ? k < g.nz - 1 : i < g.nx - 1;
-    float *lp1 = A.lpe[2 * AX], *lp2 = A.lpe[2 * AX + 1];
-    float *w1 = A.we[2 * AX], *w2 = A.we[2 * AX + 1];
-    if (v1) {
-        float l = lp1[p], w;
-        adj_psi(l, w, A.lf[t1][c], A.ce[t1][c], -1, b, a, km1);
-        lp1[p] = l;
-        w1[p] = w;
-    } else {
-        w1[p] = 0.f;
-    }
-    if (v2) {
-        float l = lp2[p], w;
-        adj_psi(l, w, A.lf[t2][c], A.ce[t2][c], +1, b, a, km1);
-        lp2[p] = l;
-        w2[p] = w;
-    } else {
-        w2[p] = 0.f;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // 4. reverse E part on H cells: lH += curl_b(CE*lE) + scatter of w_e.  Loads
-//    first, as in k_adj_e.
+//    first, as in k_adj_e; cells with no CPML node skip the slab code.
 // ---------------------------------------------------------------------------
+template <typename I>
 __global__ void __launch_bounds__(kB) k_adj_h(Args A) {
-    const Grid &g = A.g;
-    const int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x;
-    const int64_t j = blockIdx.y, i = blockIdx.z;
-    if (k >= g.nz) return;
-    const int64_t c = i * g.sx + j * g.sy + k, X = g.sx, Y = g.sy;
-    const bool h0 = hm(0, i, j, k), h1 = hm(1, i, j, k), h2 = hm(2, i, j, k);
-    const int Px = A.P[0], Py = A.P[1], Pz = A.P[2];
-    // E-node slabs at this index and one below (H cell h: +w at node h-1, -w at node h)
-    const int sx0 = slab_of_e(i - 1, Px, g.nx, A.front[0], A.back[0]);
-    const int sx1 = slab_of_e(i, Px, g.nx, A.front[0], A.back[0]);
-    const int sy0 = slab_of_e(j - 1, Py, g.ny, A.front[1], A.back[1]);
-    const int sy1 = slab_of_e(j, Py, g.ny, A.front[1], A.back[1]);
-    const int sz0 = slab_of_e(k - 1, Pz, g.nz, A.front[2], A.back[2]);
-    const int sz1 = slab_of_e(k, Pz, g.nz, A.front[2], A.back[2]);
+    const int k = blockIdx.x * kB + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+    const int nx = (int)A.g.nx, ny = (int)A.g.ny, nz = (int)A.g.nz;
+    if (k >= nz) return;
+    const I X = (I)A.g.sx, Y = (I)A.g.sy, c = (I)i * X + (I)j * Y + k;
+    // H update masks (2nd_order-Yee/Numpy/fdtd3d.py:4-7)
+    const bool h0 = j > 0 && k > 0, h1 = i > 0 && k > 0, h2 = i > 0 && j > 0;
+    const int Py = A.P[1], Pz = A.P[2];
 
     // ---- loads
-    // nu = CE * lE of component q at offset o, zero outside q's update mask
-    // (m: the mask at that cell; the load only where it is needed)
-    auto NU = [&](int q, bool need, bool m, int64_t o) {
+    // nu = CE * lE of component q at offset o, zero outside q's update mask m
+    // (loaded only where an H component needs it)
+    auto NU = [&](int q, bool need, bool m, I o) {
         return need && m ? fmul(__ldg(A.ce[q] + c + o), __ldg(A.lf[q] + c + o)) : 0.f;
     };
-    auto W = [&](int q, bool m, int64_t p) { return m ? __ldg(A.we[q] + p) : 0.f; };
-    const float n0 = NU(0, h1 || h2, em(g, 0, i, j, k), 0), n1 = NU(1, h0 || h2, em(g, 1, i, j, k), 0),
-                n2 = NU(2, h0 || h1, em(g, 2, i, j, k), 0);
-    const float n2j = NU(2, h0, em(g, 2, i, j - 1, k), -Y), n1k = NU(1, h0, em(g, 1, i, j, k - 1), -1);  // hx
-    const float n0k = NU(0, h1, em(g, 0, i, j, k - 1), -1), n2i = NU(2, h1, em(g, 2, i - 1, j, k), -X);  // hy
-    const float n1i = NU(1, h2, em(g, 1, i - 1, j, k), -X), n0j = NU(0, h2, em(g, 0, i, j - 1, k), -Y);  // hz
-    // w_e of the slab nodes one below (+) and at this index (-), per component
-    // hx: ezy (y, psi 0 of e) and eyz (z, psi 1); hy: ezx (x, psi 1) and exz
-    // (z, psi 0); hz: eyx (x, psi 0) and exy (y, psi 1)
-    const float wx0 = W(2, h0 && sy0 >= 0, py(g, Py, i, sy0, k)), wx1 = W(2, h0 && sy1 >= 0, py(g, Py, i, sy1, k));
-    const float wx2 = W(5, h0 && sz0 >= 0, pz(g, Pz, i, j, sz0)), wx3 = W(5, h0 && sz1 >= 0, pz(g, Pz, i, j, sz1));
-    const float wy0 = W(1, h1 && sx0 >= 0, px(g, sx0, j, k)), wy1 = W(1, h1 && sx1 >= 0, px(g, sx1, j, k));
-    const float wy2 = W(4, h1 && sz0 >= 0, pz(g, Pz, i, j, sz0)), wy3 = W(4, h1 && sz1 >= 0, pz(g, Pz, i, j, sz1));
-    const float wz0 = W(0, h2 && sx0 >= 0, px(g, sx0, j, k)), wz1 = W(0, h2 && sx1 >= 0, px(g, sx1, j, k));
-    const float wz2 = W(3, h2 && sy0 >= 0, py(g, Py, i, sy0, k)), wz3 = W(3, h2 && sy1 >= 0, py(g, Py, i, sy1, k));
+    const bool em0 = j < ny - 1 && k < nz - 1, em1 = i < nx - 1 && k < nz - 1, em2 = i < nx - 1 && j < ny - 1;
+    const float n0 = NU(0, h1 || h2, em0, 0), n1 = NU(1, h0 || h2, em1, 0), n2 = NU(2, h0 || h1, em2, 0);
+    const float n2j = NU(2, h0, i < nx - 1, -Y), n1k = NU(1, h0, i < nx - 1, -1);  // hx: (i, j-1), (i, k-1)
+    const float n0k = NU(0, h1, j < ny - 1, -1), n2i = NU(2, h1, j < ny - 1, -X);  // hy: (k-1), (i-1)
+    const float n1i = NU(1, h2, k < nz - 1, -X), n0j = NU(0, h2, k < nz - 1, -Y);  // hz: (i-1), (j-1)
     const float lh0 = h0 ? A.lf[3][c] : 0.f, lh1 = h1 ? A.lf[4][c] : 0.f, lh2 = h2 ? A.lf[5][c] : 0.f;
+    // E-node slabs one below and at this index (H cell h: +w at node h-1, -w
+    // at node h); -1 off the slabs
+    int sx0 = -1, sx1 = -1, sy0 = -1, sy1 = -1, sz0 = -1, sz1 = -1;
+    // w_e per component: hx: ezy (y, psi 0 of e) and eyz (z, psi 1); hy: ezx
+    // (x, psi 1) and exz (z, psi 0); hz: eyx (x, psi 0) and exy (y, psi 1)
+    float wx0 = 0.f, wx1 = 0.f, wx2 = 0.f, wx3 = 0.f, wy0 = 0.f, wy1 = 0.f, wy2 = 0.f, wy3 = 0.f;
+    float wz0 = 0.f, wz1 = 0.f, wz2 = 0.f, wz3 = 0.f;
+    if (near_h(A, 0, i, nx) || near_h(A, 1, j, ny) || near_h(A, 2, k, nz)) {
+        sx0 = slab_e(i - 1, A.P[0], nx, A.front[0], A.back[0]);
+        sx1 = slab_e(i, A.P[0], nx, A.front[0], A.back[0]);
+        sy0 = slab_e(j - 1, Py, ny, A.front[1], A.back[1]);
+        sy1 = slab_e(j, Py, ny, A.front[1], A.back[1]);
+        sz0 = slab_e(k - 1, Pz, nz, A.front[2], A.back[2]);
+        sz1 = slab_e(k, Pz, nz, A.front[2], A.back[2]);
+        auto W = [&](int q, bool m, I p) { return m ? __ldg(A.we[q] + p) : 0.f; };
+        if (h0) {
+            wx0 = W(2, sy0 >= 0, psi_y<I>(nz, Py, i, sy0, k));
+            wx1 = W(2, sy1 >= 0, psi_y<I>(nz, Py, i, sy1, k));
+            wx2 = W(5, sz0 >= 0, psi_z<I>(ny, Pz, i, j, sz0));
+            wx3 = W(5, sz1 >= 0, psi_z<I>(ny, Pz, i, j, sz1));
+        }
+        if (h1) {
+            wy0 = W(1, sx0 >= 0, psi_x<I>(ny, nz, sx0, j, k));
+            wy1 = W(1, sx1 >= 0, psi_x<I>(ny, nz, sx1, j, k));
+            wy2 = W(4, sz0 >= 0, psi_z<I>(ny, Pz, i, j, sz0));
+            wy3 = W(4, sz1 >= 0, psi_z<I>(ny, Pz, i, j, sz1));
+        }
+        if (h2) {
+            wz0 = W(0, sx0 >= 0, psi_x<I>(ny, nz, sx0, j, k));
+            wz1 = W(0, sx1 >= 0, psi_x<I>(ny, nz, sx1, j, k));
+            wz2 = W(3, sy0 >= 0, psi_y<I>(nz, Py, i, sy0, k));
+            wz3 = W(3, sy1 >= 0, psi_y<I>(nz, Py, i, sy1, k));
+        }
+    }
 
     // ---- arithmetic and stores
     if (h0) {  // hx
@@ -464,15 +479,6 @@ static dim3 cells(const Grid &g) {
     return dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)g.ny, (unsigned)g.nx);
 }
 
-template <int AX>
-static void launch_slab(const Grid &g, int P, bool e, const Args &A, cudaStream_t st) {
-    dim3 grid;
-    if (AX == 0) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)g.ny, (unsigned)(2 * P));
-    else if (AX == 1) grid = dim3((unsigned)((g.nz + kB - 1) / kB), (unsigned)(2 * P), (unsigned)g.nx);
-    else grid = dim3((unsigned)((g.ny * 2 * P + kB - 1) / kB), (unsigned)g.nx);
-    if (e) k_adj_epsi<AX><<<grid, kB, 0, st>>>(A);
-    else k_adj_hpsi<AX><<<grid, kB, 0, st>>>(A);
-}
 
 static int validate_points(const Grid &g, const fdtd_points *pts) {
     if (!pts || pts->n < 0) return FDTD_ERR_ARG;
@@ -554,14 +560,30 @@ static int adjoint_step(const fdtd_grid *gp, const fdtd_cpml *cp, const fdtd_adj
         for (int q = 0; q < 6; q++) lf.f[q] = s->lf[q];
         add_points(g, *mon, lf, mon_grad, st);
     }
-    if (A.P[0]) launch_slab<0>(g, A.P[0], false, A, st);
-    if (A.P[1]) launch_slab<1>(g, A.P[1], false, A, st);
-    if (A.P[2]) launch_slab<2>(g, A.P[2], false, A, st);
-    k_adj_e<<<cells(g), kB, 0, st>>>(A);
-    if (A.P[0]) launch_slab<0>(g, A.P[0], true, A, st);
-    if (A.P[1]) launch_slab<1>(g, A.P[1], true, A, st);
-    if (A.P[2]) launch_slab<2>(g, A.P[2], true, A, st);
-    k_adj_h<<<cells(g), kB, 0, st>>>(A);
+    // 32-bit offsets in the kernels when every field and psi array has fewer
+    // than 2^31 elements
+    int64_t most = g.nx * g.sx;
+    PsiBlocks R{};
+    for (int a = 0; a < 3; a++) {
+        const int64_t np = 2 * (int64_t)A.P[a] * (n[0] * n[1] * n[2] / n[a]);
+        most = std::max(most, np);
+        const int64_t nb = (a ? R.nb[a - 1] : 0) + (np + kB - 1) / kB;
+        if (nb >= ((int64_t)1 << 31)) return FDTD_ERR_UNSUPPORTED;
+        R.nb[a] = (int32_t)nb;
+    }
+    const bool i32 = most < ((int64_t)1 << 31);
+    if (R.nb[2] > 0) {
+        if (i32) k_adj_psi3<false, int32_t><<<R.nb[2], kB, 0, st>>>(A, R);
+        else k_adj_psi3<false, int64_t><<<R.nb[2], kB, 0, st>>>(A, R);
+    }
+    if (i32) k_adj_e<int32_t><<<cells(g), kB, 0, st>>>(A);
+    else k_adj_e<int64_t><<<cells(g), kB, 0, st>>>(A);
+    if (R.nb[2] > 0) {
+        if (i32) k_adj_psi3<true, int32_t><<<R.nb[2], kB, 0, st>>>(A, R);
+        else k_adj_psi3<true, int64_t><<<R.nb[2], kB, 0, st>>>(A, R);
+    }
+    if (i32) k_adj_h<int32_t><<<cells(g), kB, 0, st>>>(A);
+    else k_adj_h<int64_t><<<cells(g), kB, 0, st>>>(A);
     return check_launch();
 }
 

@@ -11,7 +11,10 @@ and its backward pass walks the segments last to first: it recomputes the K
 states of a segment from its checkpoint into K+1 state slots (one fused launch
 per step, each writing its own slot), then applies the hand-written adjoint
 step (fdtd_adjoint_step_f32) from the last state of the segment down to the
-first, accumulating dL/dCE.  Memory: ceil(N/K) checkpoints + (K+1) slots.
+first, accumulating dL/dCE.  With overlap (the default), a second set of
+slots lets the recompute of the segment before run on a second stream while
+the reverse steps of the current one run.  Memory: ceil(N/K) checkpoints +
+(K+1) slots (twice that with overlap).
 
 ``fdtd_run(ce, engine)`` is the differentiable call:
 
@@ -46,10 +49,13 @@ class YeeAdjoint:
     there (fdtd_adjoint_step_region_f32) and returned as zero elsewhere; the
     reverse steps then skip the forward-H reads and the accumulator traffic of
     every other cell.  None: every cell.
+    overlap: in the backward pass, recompute segment c-1 into a second set of
+    state slots on a second stream while the reverse steps of segment c run
+    (the same kernels and results; K+1 more slots of device memory).
     """
 
     def __init__(self, shape, nsteps, npml=0, faces=0x3F, cpml_params=None, sources=(), monitors=(),
-                 segment=100, device="cuda", tile=None, grad_region=None):
+                 segment=100, device="cuda", tile=None, grad_region=None, overlap=True):
         nx, ny, nz = (int(v) for v in shape)
         self.shape = (nx, ny, nz)
         self.nsteps = int(nsteps)
@@ -80,8 +86,13 @@ class YeeAdjoint:
                                      dtype=torch.int32, device=dev)
         self._mon_comp = torch.tensor([COMPONENTS6.index(c) for c, _ in mons] or [0],
                                       dtype=torch.int32, device=dev)
-        self._plans = None
-        self._slots_hold = None   # (run id, segment) whose states the slots hold
+        self.overlap = bool(overlap)
+        # slot sets: set 0 is (slots, slot_psi_e); set 1 (overlapped backward)
+        # is allocated by the first backward pass that uses it
+        self._sets = [(self.slots, self.slot_psi_e)]
+        self._plans = None        # per set: one fused plan per slot pair
+        self._ptrs = {}
+        self._slots_hold = None   # (run id, segment) whose states slot set 0 holds
         self._run_id = 0
         self._gbox = None
         if grad_region is not None:
@@ -109,12 +120,13 @@ class YeeAdjoint:
         p.comp = self._mon_comp.data_ptr()
         return p
 
-    def _plan_state(self, m):
+    def _plan_state(self, m, k=0):
+        slots, slot_psi_e = self._sets[k]
         s = N.YeeState()
         for b, slot in ((0, m), (1, m + 1)):
             for q in range(6):
-                s.f[b][q] = self.slots[slot, q].data_ptr()
-                e = self.slot_psi_e[slot][q]
+                s.f[b][q] = slots[slot, q].data_ptr()
+                e = slot_psi_e[slot][q]
                 s.psi_e[b][q] = e.data_ptr() if e is not None else None
         for q in range(6):
             h = self.psi_h[q]
@@ -123,9 +135,11 @@ class YeeAdjoint:
             s.ce[q] = self._ce[q].data_ptr()
         return s
 
-    def plans(self):
-        """One fused plan per slot pair (m -> m+1)."""
+    def plans(self, k=0):
+        """One fused plan per slot pair (m -> m+1) of slot set k."""
         if self._plans is None:
+            self._plans = {}
+        if k not in self._plans:
             g = self.grid()
             cp = self.cpml.struct()
             src = self.sources.struct()
@@ -134,33 +148,34 @@ class YeeAdjoint:
             with torch.cuda.device(self.device):
                 for m in range(self.K):
                     h = C.c_void_p()
-                    st = self._plan_state(m)
+                    st = self._plan_state(m, k)
                     N.call("fdtd_yee_plan_create", C.byref(h), C.byref(g), C.byref(st), C.byref(cp),
                            C.byref(src), C.byref(tile), C.c_void_p(self.status.data_ptr()), 0, self._stream())
                     plans.append(h)
-            self._plans = plans
-        return self._plans
+            self._plans[k] = plans
+        return self._plans[k]
 
     def _stream(self):
         return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
-    def _step_slot(self, m, t):
-        """Fused step from slot m to slot m+1 with step number t."""
+    def _step_slot(self, m, t, k=0):
+        """Fused step from slot m to slot m+1 of set k with step number t."""
         L = N.lib()
-        plan = self.plans()[m]
+        plan = self.plans(k)[m]
         L.fdtd_yee_plan_set_current(plan, 0)
         N.call("fdtd_yee_plan_run", plan, int(t), 1, self._stream())
 
-    def _slot_ptrs(self):
-        """Per-slot pointer arrays (fields, H, E-psi) built once."""
-        if getattr(self, "_ptrs", None) is None:
+    def _slot_ptrs(self, k=0):
+        """Per-slot pointer arrays (fields, H, E-psi) of slot set k, built once."""
+        if k not in self._ptrs:
+            slots, slot_psi_e = self._sets[k]
             f, h, pe = [], [], []
             for m in range(self.K + 1):
-                f.append((C.c_void_p * 6)(*[self.slots[m, q].data_ptr() for q in range(6)]))
-                h.append((C.c_void_p * 3)(*[self.slots[m, 3 + q].data_ptr() for q in range(3)]))
-                pe.append((C.c_void_p * 6)(*[t.data_ptr() if t is not None else None for t in self.slot_psi_e[m]]))
-            self._ptrs = (f, h, pe, self.grid(), self.points())
-        return self._ptrs
+                f.append((C.c_void_p * 6)(*[slots[m, q].data_ptr() for q in range(6)]))
+                h.append((C.c_void_p * 3)(*[slots[m, 3 + q].data_ptr() for q in range(3)]))
+                pe.append((C.c_void_p * 6)(*[t.data_ptr() if t is not None else None for t in slot_psi_e[m]]))
+            self._ptrs[k] = (f, h, pe, self.grid(), self.points())
+        return self._ptrs[k]
 
     def _gather(self, slot, out_row):
         if not self.nmon:
@@ -177,10 +192,11 @@ class YeeAdjoint:
         nz = self.shape[2]
         self._ce[:, :, :, :nz].copy_(ce.detach().to(device=self.device, dtype=torch.float32))
 
-    def _load(self, ck):
+    def _load(self, ck, k=0):
         state, pe, ph = ck
-        self.slots[0].copy_(state)
-        for dst, src in zip(self.slot_psi_e[0], pe):
+        slots, slot_psi_e = self._sets[k]
+        slots[0].copy_(state)
+        for dst, src in zip(slot_psi_e[0], pe):
             if dst is not None:
                 dst.copy_(src)
         for dst, src in zip(self.psi_h, ph):
@@ -243,34 +259,76 @@ class YeeAdjoint:
                 arr[q] = lst[q].data_ptr() if lst[q] is not None else None
         for q in range(3):
             st.grad_ce[q] = gce[q].data_ptr()
-        _, hps, pes, g, pts = self._slot_ptrs()
         cp = self.cpml.struct()
         ce_p = (C.c_void_p * 3)(*[self._ce[q].data_ptr() for q in range(3)])
         gm = None
         if grad_mon is not None and self.nmon:
             gm = grad_mon.detach().to(device=dev, dtype=torch.float32).contiguous()
         segs = self._segments()
+        nseg = len(segs)
+        overlap = self.overlap and nseg > 1
+        if overlap and len(self._sets) == 1:
+            try:
+                self._sets.append((torch.zeros_like(self.slots), [self._psi_like(p) for p in self.slot_psi_e]))
+            except torch.cuda.OutOfMemoryError:
+                overlap = False   # no room for a second slot set: recompute in line
+        fn = N.lib().fdtd_adjoint_step_f32 if self._gbox is None else N.lib().fdtd_adjoint_step_region_f32
+        extra = () if self._gbox is None else (self._gbox,)
+        row = gm.stride(0) * 4 if gm is not None else 0
+        base = gm.data_ptr() if gm is not None else 0
+        # slot set of segment c: the last segment in set 0 (where the forward
+        # run left it), then alternating
+        set_of = (lambda c: (nseg - 1 - c) % 2) if overlap else (lambda c: 0)
         with torch.cuda.device(dev):
-            stream = self._stream()
-            for c in range(len(segs) - 1, -1, -1):
+            main = torch.cuda.current_stream(dev)
+            side = torch.cuda.Stream(dev) if overlap else main
+            recomputed = [None] * nseg   # event: segment c's states are in its set
+            released = {}                # set -> event: the reverse steps using it are done
+            if overlap:
+                side.wait_stream(main)   # CE, the checkpoints and the forward run's states
+
+            def recompute(c):
+                k = set_of(c)
                 t0, L = segs[c]
-                if self._slots_hold != (run_id, c):
-                    self._load(checkpoints[c])
+                if k in released:
+                    side.wait_event(released[k])
+                with torch.cuda.stream(side):
+                    self._load(checkpoints[c], k)
                     for m in range(L):
-                        self._step_slot(m, t0 + m + 1)
-                    self._slots_hold = (run_id, c)
-                fn = N.lib().fdtd_adjoint_step_f32 if self._gbox is None else N.lib().fdtd_adjoint_step_region_f32
+                        self._step_slot(m, t0 + m + 1, k)
+                    ev = torch.cuda.Event()
+                    ev.record(side)
+                recomputed[c] = ev
+
+            if self._slots_hold != (run_id, nseg - 1):
+                recompute(nseg - 1)
+            for c in range(nseg - 1, -1, -1):
+                if overlap and c > 0:
+                    recompute(c - 1)     # on the side stream, beside the reverse steps below
+                elif not overlap and c < nseg - 1:
+                    recompute(c)
+                if recomputed[c] is not None:
+                    main.wait_event(recomputed[c])
+                t0, L = segs[c]
+                k = set_of(c)
+                _, hps, pes, g, pts = self._slot_ptrs(k)
                 gp, cpp, stp = C.byref(g), C.byref(cp), C.byref(st)
-                extra = () if self._gbox is None else (self._gbox,)
                 ptsp = C.byref(pts) if gm is not None else None
-                row = gm.stride(0) * 4 if gm is not None else 0
-                base = gm.data_ptr() if gm is not None else 0
+                stream = C.c_void_p(main.cuda_stream)
                 for n in range(L, 0, -1):
                     T = t0 + n
                     mon_ptr = C.c_void_p(base + (T - 1) * row) if gm is not None else None
                     rc = fn(gp, cpp, stp, hps[n - 1], pes[n], ce_p, ptsp, mon_ptr, *extra, stream)
                     if rc:
                         N.check(rc, "fdtd_adjoint_step_f32")
+                if overlap:
+                    ev = torch.cuda.Event()
+                    ev.record(main)
+                    released[k] = ev
+            if overlap:
+                main.wait_stream(side)
+        # slot set 0 holds segment 0 now when it is its set, else an older one
+        self._slots_hold = (run_id, 0) if set_of(0) == 0 else None
         return gce[:, :, :, :nz]
 
     def check_status(self):
@@ -282,8 +340,9 @@ class YeeAdjoint:
     def close(self):
         if self._plans is not None:
             L = N.lib()
-            for h in self._plans:
-                L.fdtd_yee_plan_destroy(h)
+            for plans in self._plans.values():
+                for h in plans:
+                    L.fdtd_yee_plan_destroy(h)
             self._plans = None
 
     def __del__(self):

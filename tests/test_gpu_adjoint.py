@@ -224,6 +224,32 @@ def test_design_region_gradient_equals_full_gradient_inside(F):
         F.YeeAdjoint(shape, nsteps, npml=npml, grad_region=(slice(0, 0), slice(None), slice(None)))
 
 
+@pytest.mark.parametrize("region", [None, (slice(4, 20), slice(6, 22), slice(3, 30))])
+def test_overlapped_backward_equals_serial(F, region):
+    """overlap=True (segment c-1 recomputed into a second slot set on a side
+    stream beside the reverse steps of segment c) gives the same gradient and
+    monitor series bit for bit as the serial backward, over several segments
+    (the last one ragged), twice in a row on the same engine."""
+    shape, npml, nsteps = (26, 28, 34), 5, 47
+    ce, src, mons = make_case(shape, npml, nsteps, seed=6)
+    out = []
+    for overlap in (False, True):
+        eng = F.YeeAdjoint(shape, nsteps, npml=npml, sources=src, monitors=mons, segment=9,
+                           grad_region=region, overlap=overlap)
+        for _ in range(2):
+            cg = ce.cuda().requires_grad_(True)
+            mon, _ = F.fdtd_run(cg, eng)
+            (mon.double() ** 2).sum().backward()
+            out.append((mon.detach().cpu(), cg.grad.detach().cpu()))
+        eng.check_status()
+        eng.close()
+    ref_mon, ref_g = out[0]
+    for mon, g in out[1:]:
+        np.testing.assert_array_equal(mon.numpy(), ref_mon.numpy())
+        np.testing.assert_array_equal(g.numpy(), ref_g.numpy())
+    assert ref_g.abs().max() > 0
+
+
 def test_gradient_vs_finite_differences(F):
     """Central differences in eps (h = 1e-3) at cells near the monitors against
     dL/deps from the adjoint run with CE = 0.5/eps for all three components of

@@ -33,6 +33,7 @@ each rank runs an independent replica and `value` sums over ranks.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -731,6 +732,19 @@ def run_batched64(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_launches(nsteps, segment, monitors, cpml):
+    """Kernel launches of one forward + backward run of YeeAdjoint: a forward
+    step is the fused kernel and the two z-band kernels (CPML on the z faces)
+    plus the probe gather; the backward recomputes every segment but the
+    last (three launches a step) and runs one reverse step per step (probe
+    injection, the two psi-transpose launches, the E and H cell kernels)."""
+    fused = 3 if cpml else 1
+    last = nsteps - (math.ceil(nsteps / segment) - 1) * segment
+    forward = nsteps * (fused + (1 if monitors else 0))
+    reverse = nsteps * ((1 if monitors else 0) + (2 if cpml else 0) + 2)
+    return forward + (nsteps - last) * fused + reverse
+
+
 def run_adjoint256(args):
     """Gradient of a probe loss w.r.t. the permittivity of a 128x128x64 design
     region: forward and backward cost, and central differences at 32 cells."""
@@ -816,7 +830,7 @@ def run_adjoint256(args):
                                     "how": "dL/deps from the FP32 adjoint against central differences "
                                            "(h = 1e-3 in eps) of the loss computed by the FP64 step on the GPU "
                                            "(fdtd_step_unfused_f64) for the same FP32-rounded CE"},
-                       "gpu_launches": None})
+                       "gpu_launches": adjoint_launches(w.steps, w.segment, bool(w.monitors), w.npml > 0)})
     print(json.dumps(line), flush=True)
 
 

@@ -343,25 +343,35 @@ def run_ours(args, rank, world):
             host_f[k].copy_(v)
         for q in range(3):
             host_ce[q].copy_(solver.ce[q])
+        # one untimed pass over the same buffers first: the first DMA from
+        # freshly pinned pages also pays for mapping them
+        solver.load_host(host_f, host_ce)
+        solver.step(1)
+        solver.store_host(host_f)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
         solver.load_host(host_f, host_ce)
+        ev[1].record(stream)
         solver.step(args.steps)
+        ev[2].record(stream)
         solver.store_host(host_f)
-        e1.record(stream)
+        ev[3].record(stream)
         torch.cuda.synchronize()
         solver.check_status()
-        e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
+        e_ms = max_over_ranks(ev[0].elapsed_time(ev[3]), dev)
         h2d = 9 * cells * 4
         d2h = 6 * cells * 4
+        h2d_ms, run_ms, d2h_ms = (ev[q].elapsed_time(ev[q + 1]) for q in range(3))
         e2e = {"value": cells * args.steps * world / (e_ms / 1e3) / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "h2d_ms": h2d_ms, "steps_ms": run_ms, "d2h_ms": d2h_ms,
+               "h2d_GBs": h2d / (h2d_ms / 1e3) / 1e9, "d2h_GBs": d2h / (d2h_ms / 1e3) / 1e9,
                "note": "one public-API run of %d steps: H2D of fields+coefficients from pinned host "
-                       "memory, %d fused steps, D2H of the fields" % (args.steps, args.steps)}
+                       "memory, %d fused steps, D2H of the fields (after one untimed pass over the "
+                       "same buffers)" % (args.steps, args.steps)}
         del host_f, host_ce
 
     accuracy = None

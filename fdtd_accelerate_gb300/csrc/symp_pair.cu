@@ -736,7 +736,7 @@ struct Edge {
     uint32_t off[5];                     // first cell of each box within one x plane
     uint32_t rcp[4];                     // ceil(2^32 / width) of each box (division by the width)
 };
-constexpr int EDGE_BLOCK = 256;
+constexpr int EDGE_BLOCK = 128;
 
 // launch: blockIdx.y = x plane, blockIdx.x * EDGE_BLOCK + threadIdx.x = cell of
 // the plane's part of the shell (box by box, z fastest)

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kB) k_adj_psi3(Args A, PsiBlocks R) {
     }
     if (!(s < P ? A.front[ax] : A.back[ax])) return;
     const I c = i * (I)A.g.sx + j * (I)A.g.sy + k;
-    const float b_ = E ? A.be[ax][s] : A.bh[ax][s], a = E ? A.ae[ax][s] : A.ah[ax][s],
+    const float bcoef = E ? A.be[ax][s] : A.bh[ax][s], a = E ? A.ae[ax][s] : A.ah[ax][s],
                 km1 = E ? A.ke[ax][s] : A.kh[ax][s];
     // target components of psi1 / psi2 on this axis (x: y, z; y: z, x; z: x, y)
     // and their validity (the update masks of the target family)
@@ -128,8 +128,8 @@ __global__ void __launch_bounds__(kB) k_adj_psi3(Args A, PsiBlocks R) {
     float *w1 = E ? A.we[2 * ax] : A.wh[2 * ax], *w2 = E ? A.we[2 * ax + 1] : A.wh[2 * ax + 1];
     if (v1) {
         float l = lp1[t], w;
-        if (E) adj_psi(l, w, A.lf[t1][c], A.ce[t1][c], -1, b_, a, km1);
-        else adj_psi(l, w, A.lf[3 + t1][c], 0.5f, +1, b_, a, km1);
+        if (E) adj_psi(l, w, A.lf[t1][c], A.ce[t1][c], -1, bcoef, a, km1);
+        else adj_psi(l, w, A.lf[3 + t1][c], 0.5f, +1, bcoef, a, km1);
         lp1[t] = l;
         w1[t] = w;
     } else {
@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(kB) k_adj_psi3(Args A, PsiBlocks R) {
     }
     if (v2) {
         float l = lp2[t], w;
-        if (E) adj_psi(l, w, A.lf[t2][c], A.ce[t2][c], +1, b_, a, km1);
-        else adj_psi(l, w, A.lf[3 + t2][c], 0.5f, -1, b_, a, km1);
+        if (E) adj_psi(l, w, A.lf[t2][c], A.ce[t2][c], +1, bcoef, a, km1);
+        else adj_psi(l, w, A.lf[3 + t2][c], 0.5f, -1, bcoef, a, km1);
         lp2[t] = l;
         w2[t] = w;
     } else {

@@ -187,7 +187,7 @@ class SymplecticSolver:
     fused: take the stage-pair path (one pass per H + E stage pair: the pair
     kernel inside, the edge kernels on the y/z CPML shell) where pair_path()
     allows; bit-identical to the per-stage kernels and faster than them
-    (8.3 against 12.3 ms per step on the 512^3 workload); fused=False keeps
+    (8.25 against 12.3 ms per step on the 512^3 workload); fused=False keeps
     the one-launch-per-stage path.  x_chunk: x planes per work item of the
     pair kernel (0: chosen per tiling by the plan).
     """

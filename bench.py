@@ -59,6 +59,11 @@ FALLBACK_HBM_GBS = 6790.7
 # z-band kernels' bytes per band cell (nx * ny * 2P z-slab E nodes).
 NCU_FUSED_DRAM_BYTES_PER_CELL = 63.48
 NCU_BAND_DRAM_BYTES_PER_BAND_CELL = 193.0
+# The plain 128^3 step (one fused launch, no CPML): DRAM bytes of one launch
+# after an L2 flush, from an ncu capture of that workload (three launches,
+# within 2 %); part of the 50 MB of field writes is still in L2 when the
+# launch ends, so the write count is low.
+NCU_PLAIN128_DRAM_BYTES = 92.9e6
 
 
 def step_traffic_bytes(shape, npml):
@@ -485,7 +490,10 @@ def run_plain128(args):
                       "f32", "plain Yee 128x128x128, PEC walls, vacuum, Ez source at the centre (L2 flushed "
                       "before every timed step)",
                       {"roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                                    "frac": achieved / peak, "traffic": None, "peak_source": src},
+                                    "frac": achieved / peak,
+                                    "traffic": NCU_PLAIN128_DRAM_BYTES if w.shape == (128, 128, 128) else None,
+                                    "traffic_source": "ncu dram bytes of one launch of this workload",
+                                    "alg_bytes_per_launch": alg, "peak_source": src},
                        "clocks": clocks, "gpu_launches": args.steps * info["launches_per_step"],
                        "accuracy": "bit-exact against the FP32 oracle after 1000 steps; FP32-vs-FP64 floor in "
                                    "tests/test_gpu_accuracy.py"})

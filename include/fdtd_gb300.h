@@ -233,7 +233,9 @@ typedef struct {
  * resident CTAs per SM (persistent grid), pipeline stages (planes staged in
  * shared memory), L2 promotion of the tile loads (0 = 256 B, 1 = none,
  * 2 = 64 B, 3 = 128 B).  x_chunk 0 picks a chunk that gives every SM
- * about three work items. */
+ * about three work items, and for a grid without CPML (work items of equal
+ * cost) the chunk of 128 .. 8 planes whose persistent launch is shortest
+ * (ceil(items / CTAs) items of chunk + 3 plane steps). */
 typedef struct {
     int32_t tile_y;
     int32_t x_chunk;
